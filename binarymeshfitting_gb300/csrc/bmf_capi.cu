@@ -1,0 +1,687 @@
+// C ABI (include/bmf.h): context, scratch arena, per-chunk entry points and
+// the batched, CUDA-graph-captured update.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bmf.h"
+#include "bmf_device.cuh"
+#include "bmf_internal.h"
+
+using namespace bmf;
+
+namespace {
+
+enum Slot {
+  S_CHUNKS, S_UNITS, S_FLAGS, S_TOT, S_INFO, S_TOTALS, S_WORDS, S_DENS, S_VCNT, S_ICNT, S_GPL,
+  S_OFF, S_CURSOR, S_ADJ, S_DUALP, S_DUALN, S_SCANTMP, S_NUM
+};
+
+constexpr int kMaxDim = 512;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct bmf_ctx {
+  int device = 0;
+  std::string err;
+  int64_t launches = 0;
+  DevBuf bufs[S_NUM];
+  int64_t* h_pinned = nullptr;  // readback staging
+};
+
+struct bmf_batch {
+  bmf_ctx* ctx = nullptr;
+  int n = 0, n_units = 0, max_dim = 0;
+  bmf_extract_opts opts{};
+  FieldDev field{};
+  std::vector<ChunkDev> h_chunks;
+  ChunkDev* d_chunks = nullptr;
+  int* d_units = nullptr;
+  uint32_t* d_flags = nullptr;
+  uint32_t* d_tot = nullptr;
+  int64_t* d_totals = nullptr;
+  float* d_dens = nullptr;
+  uint32_t* d_words = nullptr;
+  WordScratch ws{};
+  // processing scratch (grown with the output capacity)
+  int64_t proc_vcap = 0, proc_icap = 0;
+  ProcessScratch ps{};
+  uint32_t* d_idxg = nullptr;
+  uint8_t* d_valence = nullptr;
+  uint8_t* d_boundary = nullptr;
+  // captured graph and the output it was captured for
+  cudaGraphExec_t exec = nullptr;
+  bmf_batch_out graph_out{};
+  int64_t graph_kernels = 0;
+  int64_t* h_pinned = nullptr;
+  ChunkDev* h_stage = nullptr;       // pinned staging for bmf_batch_set_descs
+  cudaEvent_t stage_done = nullptr;  // the last staging copy has been consumed
+};
+
+namespace {
+
+bmf_status fail(bmf_ctx* ctx, bmf_status s, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return s;
+}
+
+bmf_status cuda_check(bmf_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return BMF_OK;
+  return fail(ctx, e == cudaErrorMemoryAllocation ? BMF_ERR_OUT_OF_MEMORY : BMF_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define BMF_CUDA(ctx, call)                                      \
+  do {                                                           \
+    bmf_status _s = cuda_check((ctx), (call), #call);            \
+    if (_s != BMF_OK) return _s;                                 \
+  } while (0)
+
+#define BMF_LAUNCHED(ctx, k)                                                   \
+  do {                                                                         \
+    (ctx)->launches += (k);                                                    \
+    bmf_status _s = cuda_check((ctx), cudaPeekAtLastError(), "kernel launch"); \
+    if (_s != BMF_OK) return _s;                                               \
+  } while (0)
+
+template <class T>
+bmf_status scratch(bmf_ctx* ctx, Slot s, size_t count, T** out) {
+  const size_t bytes = count * sizeof(T) + 256;
+  DevBuf& b = ctx->bufs[s];
+  if (b.bytes < bytes) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    const size_t want = bytes + bytes / 4;
+    BMF_CUDA(ctx, cudaMalloc(&b.p, want));
+    b.bytes = want;
+  }
+  *out = (T*)b.p;
+  return BMF_OK;
+}
+
+uint64_t splitmix64(uint64_t* st) {
+  uint64_t z = (*st += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Noise permutation: Fisher-Yates over 0..255 driven by splitmix64(seed).
+FieldDev make_field(const bmf_field* f) {
+  FieldDev d{};
+  d.kind = f->kind;
+  for (int i = 0; i < BMF_FIELD_MAX_PARAMS; ++i) d.p[i] = f->params[i];
+  for (int i = 0; i < 256; ++i) d.perm[i] = (uint8_t)i;
+  if (f->kind == BMF_FIELD_TERRAIN_FBM) {
+    uint64_t st = (uint64_t)(int64_t)f->params[6];
+    for (int i = 255; i > 0; --i) {
+      const int j = (int)(splitmix64(&st) % (uint64_t)(i + 1));
+      const uint8_t t = d.perm[i];
+      d.perm[i] = d.perm[j];
+      d.perm[j] = t;
+    }
+  }
+  return d;
+}
+
+bool field_ok(const bmf_field* f) {
+  return f && f->kind >= BMF_FIELD_GRID && f->kind <= BMF_FIELD_PLANE_Y &&
+         (f->kind != BMF_FIELD_TERRAIN_FBM || (f->params[5] >= 0 && f->params[5] <= 32));
+}
+
+bool dim_ok(int dim) { return dim >= 2 && dim <= kMaxDim; }
+
+ChunkDev chunk_of(const bmf_chunk_desc* d) {
+  ChunkDev c{};
+  c.ox = d->origin[0];
+  c.oy = d->origin[1];
+  c.oz = d->origin[2];
+  c.scale = d->scale;
+  c.dim = d->dim;
+  c.zc = (d->dim + 31) / 32;
+  return c;
+}
+
+// Uploads a single chunk record and its unit range [0, dim).
+bmf_status upload_single(bmf_ctx* ctx, const ChunkDev& c, cudaStream_t st, ChunkDev** d_c, int** d_u) {
+  bmf_status s;
+  if ((s = scratch(ctx, S_CHUNKS, 1, d_c)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_UNITS, 2, d_u)) != BMF_OK) return s;
+  const int units[2] = {0, c.dim};
+  BMF_CUDA(ctx, cudaMemcpyAsync(*d_c, &c, sizeof(ChunkDev), cudaMemcpyHostToDevice, st));
+  BMF_CUDA(ctx, cudaMemcpyAsync(*d_u, units, sizeof(units), cudaMemcpyHostToDevice, st));
+  return BMF_OK;
+}
+
+// Count -> scan -> offsets -> emit for chunks already labelled.  Totals land
+// in d_totals[0..1] (vertices, indices); flags must be set.
+bmf_status extract_core(bmf_ctx* ctx, int mode, int placement, ChunkDev* d_chunks, int n_chunks, const int* d_units,
+                        int n_units, const uint32_t* d_words, const float* d_dens, const uint32_t* d_flags,
+                        int64_t words_total, const MeshOut& mo, int64_t* d_info, int64_t* d_totals,
+                        cudaStream_t st) {
+  WordScratch ws{};
+  uint32_t* tot = nullptr;
+  bmf_status s;
+  if ((s = scratch(ctx, S_VCNT, (size_t)words_total, &ws.vcnt)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_ICNT, (size_t)words_total, &ws.icnt)) != BMF_OK) return s;
+  if (mode == BMF_MODE_Q && (s = scratch(ctx, S_GPL, (size_t)words_total * 3, &ws.gpl)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_TOT, (size_t)n_chunks * 2, &tot)) != BMF_OK) return s;
+  launch_count(mode, d_chunks, n_chunks, d_units, n_units, d_words, d_flags, ws, st);
+  BMF_LAUNCHED(ctx, 1);
+  launch_scan_chunks(d_chunks, n_chunks, ws, tot, st);
+  BMF_LAUNCHED(ctx, 1);
+  launch_chunk_offsets(d_chunks, n_chunks, tot, d_flags, mo.vcap, mo.icap, d_info, d_totals, st);
+  BMF_LAUNCHED(ctx, 1);
+  launch_emit(mode, placement, d_chunks, n_chunks, d_units, n_units, d_words, d_dens, d_flags, ws, mo, st);
+  BMF_LAUNCHED(ctx, 1);
+  return BMF_OK;
+}
+
+bmf_status mesh_valid(bmf_ctx* ctx, const bmf_mesh* m) {
+  if (!m || !m->d_pos || !m->d_idx || m->vcap < 0 || m->icap < 0)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "mesh output: d_pos and d_idx are required");
+  return BMF_OK;
+}
+
+bmf_status process_mesh(bmf_ctx* ctx, bmf_mesh* mesh, int iters, int pb, int sn, cudaStream_t st) {
+  const int N = mesh->prim_size;
+  if (N != 3 && N != 4) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "prim_size must be 3 or 4");
+  if (!mesh->d_valence || !mesh->d_boundary)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_process needs d_valence and d_boundary");
+  const int64_t nv = mesh->n_verts, n_prims = mesh->n_idx / N;
+  // MeshProcessor::init returns early without work on an empty mesh (MeshProcessor.cpp:28-29)
+  if (iters <= 0 || nv == 0 || mesh->n_idx < N) return BMF_OK;
+  ProcessScratch ps{};
+  bmf_status s;
+  if ((s = scratch(ctx, S_OFF, (size_t)nv + 1, &ps.off)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_CURSOR, (size_t)nv, &ps.cursor)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_ADJ, (size_t)n_prims * N, &ps.adj)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_DUALP, (size_t)n_prims * 3, &ps.dual_p)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_DUALN, (size_t)n_prims * 3, &ps.dual_n)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_SCANTMP, (size_t)(nv / 4096 + 2), &ps.tmp)) != BMF_OK) return s;
+  launch_process(N, nv, n_prims, nullptr, mesh->d_pos, mesh->d_nrm, mesh->d_boundary, mesh->d_valence, mesh->d_idx,
+                 iters, pb, sn, ps, st);
+  BMF_LAUNCHED(ctx, 4 + 2 * iters);
+  return BMF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bmf_status_string(bmf_status s) {
+  switch (s) {
+    case BMF_OK: return "ok";
+    case BMF_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case BMF_ERR_CUDA: return "CUDA error";
+    case BMF_ERR_CAPACITY: return "output capacity exceeded";
+    case BMF_ERR_TIMEOUT: return "device wait timed out";
+    case BMF_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case BMF_ERR_NOT_SUPPORTED: return "not supported";
+  }
+  return "unknown status";
+}
+
+bmf_status bmf_create(const bmf_config* cfg, bmf_ctx** out) {
+  if (!out) return BMF_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return BMF_ERR_CUDA;
+  const int dev = cfg ? cfg->device : 0;
+  if (dev < 0 || dev >= n) return BMF_ERR_INVALID_ARGUMENT;
+  if (cudaSetDevice(dev) != cudaSuccess) return BMF_ERR_CUDA;
+  bmf_ctx* ctx = new bmf_ctx();
+  ctx->device = dev;
+  if (cudaMallocHost(&ctx->h_pinned, 64 * sizeof(int64_t)) != cudaSuccess) {
+    delete ctx;
+    return BMF_ERR_OUT_OF_MEMORY;
+  }
+  *out = ctx;
+  return BMF_OK;
+}
+
+bmf_status bmf_destroy(bmf_ctx* ctx) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  for (auto& b : ctx->bufs)
+    if (b.p) cudaFree(b.p);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  delete ctx;
+  return BMF_OK;
+}
+
+const char* bmf_last_error(const bmf_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+int64_t bmf_launch_count(const bmf_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+bmf_status bmf_sample_label(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
+                            uint32_t* d_words, int32_t* h_contains_mesh, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  if (!desc || !dim_ok(desc->dim) || !field_ok(field) || !d_words)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_sample_label: bad descriptor, field or words pointer");
+  if (field->kind == BMF_FIELD_GRID && !d_density)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "BMF_FIELD_GRID reads d_density, which must be given");
+  cudaStream_t st = (cudaStream_t)stream;
+  ChunkDev c = chunk_of(desc);
+  ChunkDev* d_c;
+  int* d_u;
+  uint32_t* d_flags;
+  bmf_status s;
+  if ((s = upload_single(ctx, c, st, &d_c, &d_u)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_FLAGS, 1, &d_flags)) != BMF_OK) return s;
+  BMF_CUDA(ctx, cudaMemsetAsync(d_flags, 0, sizeof(uint32_t), st));
+  const FieldDev fd = make_field(field);
+  launch_sample_label(d_c, 1, d_u, c.dim, c.dim, fd, d_density, field->kind == BMF_FIELD_GRID ? nullptr : d_density,
+                      d_words, d_flags, st);
+  BMF_LAUNCHED(ctx, 1);
+  if (h_contains_mesh) {
+    uint32_t f = 0;
+    BMF_CUDA(ctx, cudaMemcpyAsync(&f, d_flags, sizeof(f), cudaMemcpyDeviceToHost, st));
+    BMF_CUDA(ctx, cudaStreamSynchronize(st));
+    *h_contains_mesh = ((f & 1u) || ((f & 6u) == 6u)) ? 1 : 0;
+  }
+  return BMF_OK;
+}
+
+bmf_status bmf_sample_block(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
+                            void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  if (!desc || !dim_ok(desc->dim) || !field_ok(field) || field->kind == BMF_FIELD_GRID || !d_density)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_sample_block: bad descriptor, field or density pointer");
+  const int dim = desc->dim, zc = (dim + 31) / 32;
+  uint32_t* words;
+  bmf_status s;
+  if ((s = scratch(ctx, S_WORDS, (size_t)dim * dim * zc, &words)) != BMF_OK) return s;
+  return bmf_sample_label(ctx, desc, field, d_density, words, nullptr, stream);
+}
+
+bmf_status bmf_label_grid(bmf_ctx* ctx, int32_t dim, const float* d_density, uint32_t* d_words,
+                          int32_t* h_contains_mesh, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_chunk_desc d{};
+  d.scale = 1.0f;
+  d.dim = dim;
+  bmf_field f{};
+  f.kind = BMF_FIELD_GRID;
+  return bmf_sample_label(ctx, &d, &f, const_cast<float*>(d_density), d_words, h_contains_mesh, stream);
+}
+
+bmf_status bmf_cell_masks(bmf_ctx* ctx, int32_t dim, const uint32_t* d_words, uint8_t* d_masks, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  if (!dim_ok(dim) || !d_words || !d_masks) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_cell_masks: bad args");
+  launch_cell_masks(dim, d_words, d_masks, (cudaStream_t)stream);
+  BMF_LAUNCHED(ctx, 1);
+  return BMF_OK;
+}
+
+bmf_status bmf_polygonize(bmf_ctx* ctx, int32_t dim, const float* d_density, const uint32_t* d_words, int32_t mode,
+                          int32_t placement, bmf_mesh* out, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_status s;
+  if ((s = mesh_valid(ctx, out)) != BMF_OK) return s;
+  if (!dim_ok(dim) || !d_words || (mode != BMF_MODE_R && mode != BMF_MODE_Q) || placement < 0 || placement > 2)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_polygonize: bad dim, words, mode or placement");
+  if (!d_density && (mode == BMF_MODE_R || placement != BMF_PLACE_CENTER))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_polygonize: this mode needs d_density");
+  cudaStream_t st = (cudaStream_t)stream;
+  ChunkDev c{};
+  c.scale = 1.0f;
+  c.dim = dim;
+  c.zc = (dim + 31) / 32;
+  ChunkDev* d_c;
+  int* d_u;
+  uint32_t* d_flags;
+  int64_t* d_totals;
+  if ((s = upload_single(ctx, c, st, &d_c, &d_u)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_FLAGS, 1, &d_flags)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_TOTALS, 2, &d_totals)) != BMF_OK) return s;
+  launch_word_flags(d_c, 1, d_words, d_flags, st);
+  BMF_LAUNCHED(ctx, 1);
+  MeshOut mo{out->d_pos, out->d_nrm, out->d_boundary, out->d_valence, out->d_idx, nullptr, out->vcap, out->icap};
+  if ((s = extract_core(ctx, mode, placement, d_c, 1, d_u, dim, d_words, d_density, d_flags,
+                        (int64_t)dim * dim * c.zc, mo, nullptr, d_totals, st)) != BMF_OK)
+    return s;
+  BMF_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, d_totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  BMF_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned + 2, d_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  BMF_CUDA(ctx, cudaStreamSynchronize(st));
+  out->n_verts = ctx->h_pinned[0];
+  out->n_idx = ctx->h_pinned[1];
+  const uint32_t f = (uint32_t)ctx->h_pinned[2];
+  out->contains_mesh = ((f & 1u) || ((f & 6u) == 6u)) ? 1 : 0;
+  out->prim_size = mode == BMF_MODE_R ? 3 : 4;
+  if (out->n_verts > out->vcap || out->n_idx > out->icap)
+    return fail(ctx, BMF_ERR_CAPACITY, "bmf_polygonize: output capacity exceeded (needed counts reported)");
+  return BMF_OK;
+}
+
+bmf_status bmf_process(bmf_ctx* ctx, bmf_mesh* mesh, int32_t iters, int32_t process_boundary,
+                       int32_t smooth_normals, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_status s;
+  if ((s = mesh_valid(ctx, mesh)) != BMF_OK) return s;
+  if (mesh->n_verts > mesh->vcap || mesh->n_idx > mesh->icap || iters < 0)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_process: counts exceed capacities or negative iters");
+  return process_mesh(ctx, mesh, iters, process_boundary, smooth_normals, (cudaStream_t)stream);
+}
+
+bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field,
+                             const bmf_extract_opts* opts, bmf_mesh* out, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_status s;
+  if ((s = mesh_valid(ctx, out)) != BMF_OK) return s;
+  if (!desc || !dim_ok(desc->dim) || !field_ok(field) || field->kind == BMF_FIELD_GRID || !opts ||
+      (opts->mode != BMF_MODE_R && opts->mode != BMF_MODE_Q) || opts->placement < 0 || opts->placement > 2 ||
+      opts->iters < 0)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_extract_chunk: bad descriptor, field or options");
+  if (opts->iters > 0 && (!out->d_valence || !out->d_boundary))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_extract_chunk: smoothing needs d_valence and d_boundary");
+  cudaStream_t st = (cudaStream_t)stream;
+  const ChunkDev c = chunk_of(desc);
+  const int dim = c.dim;
+  ChunkDev* d_c;
+  int* d_u;
+  uint32_t* d_flags;
+  int64_t* d_totals;
+  float* d_dens;
+  uint32_t* d_words;
+  if ((s = upload_single(ctx, c, st, &d_c, &d_u)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_FLAGS, 1, &d_flags)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_TOTALS, 2, &d_totals)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_DENS, (size_t)dim * dim * dim, &d_dens)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_WORDS, (size_t)dim * dim * c.zc, &d_words)) != BMF_OK) return s;
+  BMF_CUDA(ctx, cudaMemsetAsync(d_flags, 0, sizeof(uint32_t), st));
+  const FieldDev fd = make_field(field);
+  launch_sample_label(d_c, 1, d_u, dim, dim, fd, nullptr, d_dens, d_words, d_flags, st);
+  BMF_LAUNCHED(ctx, 1);
+  MeshOut mo{out->d_pos, out->d_nrm, out->d_boundary, out->d_valence, out->d_idx, nullptr, out->vcap, out->icap};
+  if ((s = extract_core(ctx, opts->mode, opts->placement, d_c, 1, d_u, dim, d_words, d_dens, d_flags,
+                        (int64_t)dim * dim * c.zc, mo, nullptr, d_totals, st)) != BMF_OK)
+    return s;
+  BMF_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, d_totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  BMF_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned + 2, d_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  BMF_CUDA(ctx, cudaStreamSynchronize(st));
+  out->n_verts = ctx->h_pinned[0];
+  out->n_idx = ctx->h_pinned[1];
+  const uint32_t f = (uint32_t)ctx->h_pinned[2];
+  out->contains_mesh = ((f & 1u) || ((f & 6u) == 6u)) ? 1 : 0;
+  out->prim_size = opts->mode == BMF_MODE_R ? 3 : 4;
+  if (out->n_verts > out->vcap || out->n_idx > out->icap)
+    return fail(ctx, BMF_ERR_CAPACITY, "bmf_extract_chunk: output capacity exceeded (needed counts reported)");
+  // ChunkGenerator.cpp:112: processing only when the chunk has a mesh
+  if (opts->iters > 0 && out->contains_mesh && out->n_verts && out->n_idx) {
+    if ((s = process_mesh(ctx, out, opts->iters, opts->process_boundary, opts->smooth_normals, st)) != BMF_OK)
+      return s;
+    BMF_CUDA(ctx, cudaStreamSynchronize(st));
+  }
+  return BMF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched update
+// ---------------------------------------------------------------------------
+
+bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t n_chunks, const bmf_field* field,
+                            const bmf_extract_opts* opts, bmf_batch** out) {
+  if (!ctx || !out) return BMF_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (!h_descs || n_chunks <= 0 || !field_ok(field) || field->kind == BMF_FIELD_GRID || !opts ||
+      (opts->mode != BMF_MODE_R && opts->mode != BMF_MODE_Q) || opts->placement < 0 || opts->placement > 2 ||
+      opts->iters < 0)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_create: bad descriptors, field or options");
+  bmf_batch* b = new bmf_batch();
+  b->ctx = ctx;
+  b->n = n_chunks;
+  b->opts = *opts;
+  b->field = make_field(field);
+  b->h_chunks.resize(n_chunks);
+  std::vector<int> units(n_chunks + 1);
+  int64_t dens = 0, words = 0;
+  int n_units = 0;
+  for (int i = 0; i < n_chunks; ++i) {
+    if (!dim_ok(h_descs[i].dim)) {
+      delete b;
+      return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_create: chunk dim out of range");
+    }
+    ChunkDev c = chunk_of(h_descs + i);
+    c.dens = dens;
+    c.words = words;
+    dens += (int64_t)c.dim * c.dim * c.dim;
+    words += (int64_t)c.dim * c.dim * c.zc;
+    units[i] = n_units;
+    n_units += c.dim;
+    b->max_dim = c.dim > b->max_dim ? c.dim : b->max_dim;
+    b->h_chunks[i] = c;
+  }
+  units[n_chunks] = n_units;
+  b->n_units = n_units;
+  auto bail = [&](cudaError_t e, const char* what) {
+    bmf_status s = cuda_check(ctx, e, what);
+    if (s != BMF_OK) bmf_batch_destroy(b);
+    return s;
+  };
+  bmf_status s;
+  if ((s = bail(cudaMalloc(&b->d_chunks, sizeof(ChunkDev) * n_chunks), "chunks")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->d_units, sizeof(int) * (n_chunks + 1)), "units")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->d_flags, sizeof(uint32_t) * n_chunks), "flags")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->d_tot, sizeof(uint32_t) * 2 * n_chunks), "tot")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->d_totals, sizeof(int64_t) * 2), "totals")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->d_dens, sizeof(float) * dens), "density")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->d_words, sizeof(uint32_t) * words), "words")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->ws.vcnt, sizeof(uint32_t) * words), "vcnt")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->ws.icnt, sizeof(uint32_t) * words), "icnt")) != BMF_OK) return s;
+  if (opts->mode == BMF_MODE_Q &&
+      (s = bail(cudaMalloc(&b->ws.gpl, sizeof(uint32_t) * 3 * words), "gpl")) != BMF_OK)
+    return s;
+  if ((s = bail(cudaMallocHost(&b->h_pinned, sizeof(int64_t) * 4), "pinned")) != BMF_OK) return s;
+  if ((s = bail(cudaMemcpy(b->d_chunks, b->h_chunks.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice),
+                "upload chunks")) != BMF_OK)
+    return s;
+  if ((s = bail(cudaMemcpy(b->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice),
+                "upload units")) != BMF_OK)
+    return s;
+  *out = b;
+  return BMF_OK;
+}
+
+namespace {
+
+bmf_status batch_proc_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
+  if (vcap <= b->proc_vcap && icap <= b->proc_icap) return BMF_OK;
+  bmf_ctx* ctx = b->ctx;
+  const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
+  const int64_t np = icap / N;
+  void* ptrs[] = {b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p, b->ps.dual_n, b->ps.tmp,
+                  b->d_idxg, b->d_valence, b->d_boundary};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  b->proc_vcap = b->proc_icap = 0;
+  BMF_CUDA(ctx, cudaMalloc(&b->ps.off, sizeof(uint32_t) * (vcap + 1)));
+  BMF_CUDA(ctx, cudaMalloc(&b->ps.cursor, sizeof(uint32_t) * (vcap + 1)));
+  BMF_CUDA(ctx, cudaMalloc(&b->ps.adj, sizeof(uint32_t) * (np * N + 1)));
+  BMF_CUDA(ctx, cudaMalloc(&b->ps.dual_p, sizeof(float) * (3 * np + 3)));
+  BMF_CUDA(ctx, cudaMalloc(&b->ps.dual_n, sizeof(float) * (3 * np + 3)));
+  BMF_CUDA(ctx, cudaMalloc(&b->ps.tmp, sizeof(uint32_t) * (vcap / 4096 + 2)));
+  BMF_CUDA(ctx, cudaMalloc(&b->d_idxg, sizeof(uint32_t) * (icap + 1)));
+  BMF_CUDA(ctx, cudaMalloc(&b->d_valence, vcap + 1));
+  BMF_CUDA(ctx, cudaMalloc(&b->d_boundary, vcap + 1));
+  b->proc_vcap = vcap;
+  b->proc_icap = icap;
+  return BMF_OK;
+}
+
+// Enqueues one whole update on st (captured into the graph, or run directly).
+bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st, int64_t* kernels) {
+  bmf_ctx* ctx = b->ctx;
+  const bool proc = b->opts.iters > 0;
+  BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
+  launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
+                      b->d_words, b->d_flags, st);
+  launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
+  launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st);
+  launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
+                       b->d_totals, st);
+  MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
+             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap};
+  launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_dens,
+              b->d_flags, b->ws, mo, st);
+  int64_t k = 5;
+  if (proc) {
+    const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
+    launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary, b->d_valence,
+                   b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals, b->ps, st);
+    k += 6 + 2 * b->opts.iters;
+    if (out->d_boundary)
+      BMF_CUDA(ctx, cudaMemcpyAsync(out->d_boundary, b->d_boundary, (size_t)out->vcap, cudaMemcpyDeviceToDevice, st));
+  }
+  BMF_CUDA(ctx, cudaPeekAtLastError());
+  *kernels = k;
+  return BMF_OK;
+}
+
+bool same_out(const bmf_batch_out& a, const bmf_batch_out& b) {
+  return a.d_pos == b.d_pos && a.d_nrm == b.d_nrm && a.d_boundary == b.d_boundary && a.d_idx == b.d_idx &&
+         a.vcap == b.vcap && a.icap == b.icap && a.d_chunk_info == b.d_chunk_info;
+}
+
+}  // namespace
+
+bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, int32_t sync, void* stream) {
+  if (!b) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  if (!out || !out->d_pos || !out->d_idx || out->vcap < 0 || out->icap < 0)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_run: output arena needs d_pos and d_idx");
+  cudaStream_t st = (cudaStream_t)stream;
+  bmf_status s;
+  if (b->opts.iters > 0 && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
+  if (use_graph) {
+    if (!b->exec || !same_out(b->graph_out, *out)) {
+      if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+      }
+      cudaStream_t cap;
+      BMF_CUDA(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+      cudaGraph_t g;
+      BMF_CUDA(ctx, cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+      int64_t k = 0;
+      s = batch_record(b, out, cap, &k);
+      cudaError_t e = cudaStreamEndCapture(cap, &g);
+      cudaStreamDestroy(cap);
+      if (s != BMF_OK) return s;
+      BMF_CUDA(ctx, e);
+      e = cudaGraphInstantiate(&b->exec, g, 0);
+      cudaGraphDestroy(g);
+      BMF_CUDA(ctx, e);
+      b->graph_out = *out;
+      b->graph_kernels = k;
+    }
+    BMF_CUDA(ctx, cudaGraphLaunch(b->exec, st));
+    ctx->launches += b->graph_kernels;
+  } else {
+    int64_t k = 0;
+    if ((s = batch_record(b, out, st, &k)) != BMF_OK) return s;
+    ctx->launches += k;
+  }
+  if (sync) {
+    BMF_CUDA(ctx, cudaMemcpyAsync(b->h_pinned, b->d_totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    BMF_CUDA(ctx, cudaStreamSynchronize(st));
+    out->n_verts = b->h_pinned[0];
+    out->n_idx = b->h_pinned[1];
+    if (out->n_verts > out->vcap || out->n_idx > out->icap)
+      return fail(ctx, BMF_ERR_CAPACITY, "bmf_batch_run: output capacity exceeded (needed totals reported)");
+  }
+  return BMF_OK;
+}
+
+bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_descs, int32_t n_chunks, void* stream) {
+  if (!b) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  if (!h_descs || n_chunks != b->n) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_set_descs: count differs");
+  for (int i = 0; i < n_chunks; ++i)
+    if (h_descs[i].dim != b->h_chunks[i].dim)
+      return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_set_descs: a chunk's dim differs from the plan");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!b->h_stage) {
+    BMF_CUDA(ctx, cudaMallocHost(&b->h_stage, sizeof(ChunkDev) * b->n));
+    BMF_CUDA(ctx, cudaEventCreateWithFlags(&b->stage_done, cudaEventDisableTiming));
+  } else {
+    BMF_CUDA(ctx, cudaEventSynchronize(b->stage_done));
+  }
+  for (int i = 0; i < n_chunks; ++i) {
+    ChunkDev c = b->h_chunks[i];
+    c.ox = h_descs[i].origin[0];
+    c.oy = h_descs[i].origin[1];
+    c.oz = h_descs[i].origin[2];
+    c.scale = h_descs[i].scale;
+    b->h_chunks[i] = c;
+    b->h_stage[i] = c;
+  }
+  BMF_CUDA(ctx, cudaMemcpyAsync(b->d_chunks, b->h_stage, sizeof(ChunkDev) * b->n, cudaMemcpyHostToDevice, st));
+  BMF_CUDA(ctx, cudaEventRecord(b->stage_done, st));
+  return BMF_OK;
+}
+
+bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms, void* stream) {
+  if (!b || !h_stage_ms) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  if (!out || !out->d_pos || !out->d_idx) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_profile: no output");
+  cudaStream_t st = (cudaStream_t)stream;
+  bmf_status s;
+  const bool proc = b->opts.iters > 0;
+  if (proc && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
+  cudaEvent_t ev[7];
+  for (auto& e : ev) BMF_CUDA(ctx, cudaEventCreate(&e));
+  BMF_CUDA(ctx, cudaEventRecord(ev[0], st));
+  BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
+  launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
+                      b->d_words, b->d_flags, st);
+  BMF_CUDA(ctx, cudaEventRecord(ev[1], st));
+  launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
+  BMF_CUDA(ctx, cudaEventRecord(ev[2], st));
+  launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st);
+  BMF_CUDA(ctx, cudaEventRecord(ev[3], st));
+  launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
+                       b->d_totals, st);
+  BMF_CUDA(ctx, cudaEventRecord(ev[4], st));
+  MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
+             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap};
+  launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_dens,
+              b->d_flags, b->ws, mo, st);
+  BMF_CUDA(ctx, cudaEventRecord(ev[5], st));
+  if (proc) {
+    const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
+    launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary, b->d_valence,
+                   b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals, b->ps, st);
+  }
+  BMF_CUDA(ctx, cudaEventRecord(ev[6], st));
+  BMF_CUDA(ctx, cudaEventSynchronize(ev[6]));
+  BMF_CUDA(ctx, cudaPeekAtLastError());
+  for (int k = 0; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
+  for (auto& e : ev) cudaEventDestroy(e);
+  ctx->launches += 5 + (proc ? 6 + 2 * b->opts.iters : 0);
+  return BMF_OK;
+}
+
+bmf_status bmf_batch_destroy(bmf_batch* b) {
+  if (!b) return BMF_ERR_INVALID_ARGUMENT;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
+                  b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
+                  b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (b->h_pinned) cudaFreeHost(b->h_pinned);
+  if (b->h_stage) cudaFreeHost(b->h_stage);
+  if (b->stage_done) cudaEventDestroy(b->stage_done);
+  delete b;
+  return BMF_OK;
+}
+
+}  // extern "C"

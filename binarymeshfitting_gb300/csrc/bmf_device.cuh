@@ -1,0 +1,238 @@
+// Device-side building blocks shared by the sm_103a kernels.
+//
+// Every translation unit is compiled with --fmad=false and IEEE division /
+// square root, so each float expression below is rounded exactly as written:
+// the kernels reproduce the reference's single-precision results bit for bit
+// (DMCChunk.cpp:657-674 lerp, MeshProcessor.cpp:130-306 averages) and this
+// project's own field definitions (bmf_fields.h).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/bmf_fields.h"
+#include "bmf_case_tables.h"
+
+namespace bmf {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------------------
+// Case tables (generated from the reference's MCTable.h / Tables.hpp).
+// ---------------------------------------------------------------------------
+static __constant__ uint64_t c_tri_cases[256] = BMF_TRI_CASES_INIT;
+static __constant__ uint64_t c_group_cases[256] = BMF_GROUP_CASES_INIT;
+static __constant__ uint64_t c_edge_uses[256] = BMF_EDGE_USES_INIT;
+
+__device__ __forceinline__ int tri_count(int mask) { return (int)(c_tri_cases[mask] >> 60); }
+__device__ __forceinline__ int tri_edge(uint64_t w, int i) { return (int)((w >> (4 * i)) & 0xF); }
+__device__ __forceinline__ int group_count(int mask) { return (int)((c_group_cases[mask] >> 48) & 0xF); }
+__device__ __forceinline__ int group_of(int mask, int e) { return (int)((c_group_cases[mask] >> (4 * e)) & 0xF); }
+__device__ __forceinline__ int edge_uses(int mask, int e) { return (int)((c_edge_uses[mask] >> (4 * e)) & 0xF); }
+
+// Corners of edge e (corner c = 4dx + 2dy + dz).
+__device__ __forceinline__ int edge_c0(int e) {
+  // x-edges 0-3: corners e, e+4; y-edges 4-7: 4dx+dz; z-edges 8-11: 4dx+2dy.
+  return e < 4 ? e : (e < 8 ? (((e - 4) >> 1) << 2) | ((e - 4) & 1) : ((e - 8) << 1));
+}
+__device__ __forceinline__ int edge_c1(int e) { return e < 4 ? e + 4 : (e < 8 ? edge_c0(e) + 2 : edge_c0(e) + 1); }
+
+// ---------------------------------------------------------------------------
+// Chunk record used by every kernel (one per chunk in a batch).
+// ---------------------------------------------------------------------------
+struct ChunkDev {
+  float ox, oy, oz, scale;
+  int dim;        // samples per axis
+  int zc;         // 32-bit occupancy words per (x, y) line = ceil(dim / 32)
+  int64_t dens;   // offset of the chunk's density block (floats); -1 = not materialised
+  int64_t words;  // offset of the chunk's occupancy words (u32)
+  int64_t vout;   // offset of the chunk's vertices in the output arena
+  int64_t iout;   // offset of the chunk's indices in the output arena
+};
+
+// Field parameters passed by value.  perm is the noise permutation.
+struct FieldDev {
+  int kind;
+  float p[BMF_FIELD_MAX_PARAMS];
+  uint8_t perm[256];
+};
+
+// ---------------------------------------------------------------------------
+// Deterministic scalar math (same definitions as the CPU oracle, written for
+// the device).
+// ---------------------------------------------------------------------------
+
+// sin: Cody-Waite reduction by pi/2 (two 12-bit pieces + float remainder) and
+// the Taylor series of sin/cos on [-pi/4, pi/4], Horner form.
+__device__ __forceinline__ float det_sin(float x) {
+  const float k = rintf(x * 0x1.45f306p-1f);
+  float r = x - k * 0x1.92p+0f;
+  r = r - k * 0x1.fb4p-12f;
+  r = r - k * 0x1.4442d2p-24f;
+  const int q = ((int)k) & 3;
+  const float r2 = r * r;
+  float s = r2 * 2.7557319e-6f;
+  s = s + -1.9841270e-4f;
+  s = s * r2;
+  s = s + 8.3333333e-3f;
+  s = s * r2;
+  s = s + -1.6666667e-1f;
+  s = s * r2;
+  s = s * r;
+  s = s + r;
+  float c = r2 * 2.4801587e-5f;
+  c = c + -1.3888889e-3f;
+  c = c * r2;
+  c = c + 4.1666667e-2f;
+  c = c * r2;
+  c = c + -0.5f;
+  c = c * r2;
+  c = c + 1.0f;
+  const float v = (q & 1) ? c : s;
+  return (q & 2) ? -v : v;
+}
+
+__device__ __forceinline__ float fade(float t) {
+  float a = t * 6.0f;
+  a = a - 15.0f;
+  a = t * a;
+  a = a + 10.0f;
+  float t3 = t * t;
+  t3 = t3 * t;
+  return t3 * a;
+}
+__device__ __forceinline__ float lerp_t(float t, float a, float b) { return a + t * (b - a); }
+
+// Gradient of K. Perlin's improved noise: +/-u +/-v with u, v picked from
+// (x, y, z) by the low four hash bits.
+__device__ __forceinline__ float grad(int h, float x, float y, float z) {
+  const float u = (h & 8) ? y : x;
+  const float v = (h & 12) == 0 ? y : (((h & 15) == 12 || (h & 15) == 14) ? x : z);
+  const float su = __int_as_float(__float_as_int(u) ^ ((h & 1) << 31));
+  const float sv = __int_as_float(__float_as_int(v) ^ ((h & 2) << 30));
+  return su + sv;
+}
+
+// Improved gradient noise (Perlin, SIGGRAPH 2002); perm lives in shared memory
+// as 32-bit entries.
+__device__ __forceinline__ float perlin(const int* __restrict__ perm, float x, float y, float z) {
+  const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+  const int X = ((int)fx) & 255, Y = ((int)fy) & 255, Z = ((int)fz) & 255;
+  x = x - fx;
+  y = y - fy;
+  z = z - fz;
+  const float u = fade(x), v = fade(y), w = fade(z);
+  const int A = perm[X] + Y, B = perm[(X + 1) & 255] + Y;
+  const int AA = perm[A & 255] + Z, AB = perm[(A + 1) & 255] + Z;
+  const int BA = perm[B & 255] + Z, BB = perm[(B + 1) & 255] + Z;
+  const float x1 = x - 1.0f, y1 = y - 1.0f, z1 = z - 1.0f;
+  const float g000 = grad(perm[AA & 255], x, y, z), g100 = grad(perm[BA & 255], x1, y, z);
+  const float g010 = grad(perm[AB & 255], x, y1, z), g110 = grad(perm[BB & 255], x1, y1, z);
+  const float g001 = grad(perm[(AA + 1) & 255], x, y, z1), g101 = grad(perm[(BA + 1) & 255], x1, y, z1);
+  const float g011 = grad(perm[(AB + 1) & 255], x, y1, z1), g111 = grad(perm[(BB + 1) & 255], x1, y1, z1);
+  const float l00 = lerp_t(u, g000, g100), l10 = lerp_t(u, g010, g110);
+  const float l01 = lerp_t(u, g001, g101), l11 = lerp_t(u, g011, g111);
+  const float l0 = lerp_t(v, l00, l10), l1 = lerp_t(v, l01, l11);
+  return lerp_t(w, l0, l1);
+}
+
+__device__ __forceinline__ float len3(float x, float y, float z) {
+  const float a = x * x, b = y * y, c = z * z;
+  return sqrtf((a + b) + c);
+}
+
+// Evaluates a density field at world position (px, py, pz).
+__device__ __forceinline__ float eval_field(const FieldDev& f, const int* __restrict__ perm, float px, float py,
+                                            float pz) {
+  switch (f.kind) {
+    case BMF_FIELD_SPHERE_WAVE: {
+      const float l = len3(px - f.p[0], py - f.p[1], pz - f.p[2]);
+      float s = det_sin(f.p[5] * px) * det_sin(f.p[5] * py);
+      s = s * det_sin(f.p[5] * pz);
+      return (l - f.p[3]) + f.p[4] * s;
+    }
+    case BMF_FIELD_TERRAIN_FBM: {
+      const int oct = (int)f.p[5];
+      float sum = 0.0f, amp = 1.0f, fr = f.p[2];
+      for (int o = 0; o < oct; ++o) {
+        const float n = perlin(perm, px * fr, py * fr, pz * fr);
+        sum = sum + amp * n;
+        fr = fr * f.p[3];
+        amp = amp * f.p[4];
+      }
+      return (py - f.p[0]) - f.p[1] * sum;
+    }
+    case BMF_FIELD_TORUS_Z: {  // ImplicitSampler.cpp:27-34
+      const float r1 = f.p[0] / 4.0f, r2 = f.p[0] / 10.0f;
+      const float q_x = fabsf(sqrtf(px * px + py * py)) - r1;
+      const float len = sqrtf(q_x * q_x + pz * pz);
+      return -(len - r2);
+    }
+    case BMF_FIELD_SPHERE: {  // ImplicitSampler.cpp:46-50
+      const float r = f.p[0] * 0.25f;
+      return -(len3(px, py, pz) - r);
+    }
+    case BMF_FIELD_CUBOID: {  // ImplicitSampler.cpp:52-60
+      const float r = f.p[0] / 8.0f;
+      const float dx = fabsf(px) - r, dy = fabsf(py) - r, dz = fabsf(pz) - r;
+      const float m = fmaxf(dx, fmaxf(dy, dz));
+      return -fminf(m, len3(dx, dy, dz));
+    }
+    default:  // BMF_FIELD_PLANE_Y, ImplicitSampler.cpp:62-65
+      return -py;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Occupancy-word helpers.  W points at a chunk's words, [x][y][zb] row-major.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t word_at(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int zb) {
+  if (x < 0 || y < 0 || x >= dim || y >= dim || zb < 0 || zb >= zc) return 0u;
+  return __ldg(W + ((int64_t)x * dim + y) * zc + zb);
+}
+// Inside bit of sample (x, y, z); 0 outside the chunk.
+__device__ __forceinline__ int inside_at(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int z) {
+  if (z < 0 || z >= dim) return 0;
+  return (int)((word_at(W, dim, zc, x, y, z >> 5) >> (z & 31)) & 1u);
+}
+// Reference cell mask (DMCChunk.cpp:202-438): corners outside the chunk are 0.
+__device__ __forceinline__ int cell_mask_at(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int z) {
+  int m = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) m |= inside_at(W, dim, zc, x + ((c >> 2) & 1), y + ((c >> 1) & 1), z + (c & 1)) << c;
+  return m;
+}
+
+// Bits of a z-line (x, y) block zb that have a crossing towards +z.
+__device__ __forceinline__ uint32_t zcross_word(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int zb) {
+  const uint32_t w = word_at(W, dim, zc, x, y, zb);
+  const uint32_t wn = word_at(W, dim, zc, x, y, zb + 1);
+  uint32_t Z = w ^ ((w >> 1) | (wn << 31));
+  const int valid = dim - 1 - 32 * zb;  // cells z with z + 1 < dim
+  if (valid < 32) Z &= valid <= 0 ? 0u : ((1u << valid) - 1u);
+  return Z;
+}
+// Bits of line (x, y) block zb that have a crossing towards +x (0 on the far x face).
+__device__ __forceinline__ uint32_t xcross_word(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int zb) {
+  if (x + 1 >= dim) return 0u;
+  return word_at(W, dim, zc, x, y, zb) ^ word_at(W, dim, zc, x + 1, y, zb);
+}
+__device__ __forceinline__ uint32_t ycross_word(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int zb) {
+  if (y + 1 >= dim) return 0u;
+  return word_at(W, dim, zc, x, y, zb) ^ word_at(W, dim, zc, x, y + 1, zb);
+}
+
+__device__ __forceinline__ uint32_t lane_lt(int lane) { return (1u << lane) - 1u; }
+
+// Warp-inclusive scan of an int.
+__device__ __forceinline__ int warp_incl_scan(int v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int n = __shfl_up_sync(kFull, v, o);
+    if (lane >= o) v += n;
+  }
+  return v;
+}
+
+}  // namespace bmf

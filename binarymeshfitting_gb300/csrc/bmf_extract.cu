@@ -1,0 +1,694 @@
+// Stage 3 + 4: surface-cell enumeration, vertex / primitive compaction and
+// emission (DMCChunk::label_edges enumeration + calculate_cell +
+// calculate_isovertex + polygonize, DMCChunk.cpp:440-674), and the DMC quad
+// emitter with mass-point / QEF placement (qef_simd.h).
+//
+// The reference numbers vertices in one sequential scan: cells in linear
+// (x, y, z) order, and inside a cell its x-, y-, z-edge crossings
+// (DMCChunk.cpp:449-474, 599-654).  Here every 32-bit occupancy word W[x][y][zb]
+// stands for the 32 cells (x, y, 32zb..32zb+31), and the crossings those cells
+// own are three bit words:
+//     X = W[x][y] ^ W[x+1][y],  Y = W[x][y] ^ W[x][y+1],  Z = W ^ (W >> 1 | next << 31)
+// so a word hosts popc(X)+popc(Y)+popc(Z) vertices, and the vertex id of cell z's
+// axis-a crossing is   base(word) + popc((X|Y|Z bits of cells < z)) + (own earlier axes).
+// base(word) is an exclusive scan of the per-word counts in (x, y, zb) order,
+// which is exactly the reference's sequential order.  Triangles are counted
+// and placed the same way, so vertex and index buffers come out bit-identical
+// to the reference without any per-cell index volume (IndexesBlock) or cell
+// list (DMC_CellsBlock).
+#include "bmf_device.cuh"
+#include "bmf_internal.h"
+
+namespace bmf {
+
+__device__ __forceinline__ int find_chunk_e(const int* __restrict__ unit_start, int n_chunks, int u) {
+  int lo = 0, hi = n_chunks - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(unit_start + mid) <= u) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ bool contains_mesh(uint32_t f) { return (f & 1u) || ((f & 6u) == 6u); }
+
+// EDGE_V offsets (DMCChunk.cpp:32, 543-565): edge e of a cell is the axis-a
+// crossing owned by the cell at offset (ox, oy, oz).
+static __constant__ int8_t c_edge_owner[12][4] = {{0, 0, 0, 0}, {0, 0, 1, 0}, {0, 1, 0, 0}, {0, 1, 1, 0},
+                                                  {0, 0, 0, 1}, {0, 0, 1, 1}, {1, 0, 0, 1}, {1, 0, 1, 1},
+                                                  {0, 0, 0, 2}, {0, 1, 0, 2}, {1, 0, 0, 2}, {1, 1, 0, 2}};
+
+// Mask of cell (x, y, 32zb + lane) from the four line words around it and the
+// four next-block words (for corner z + 1 of the block's last cell).
+__device__ __forceinline__ int mask_from_lines(uint32_t w00, uint32_t w01, uint32_t w10, uint32_t w11, uint32_t n00,
+                                               uint32_t n01, uint32_t n10, uint32_t n11, int lane) {
+  const uint64_t q00 = ((uint64_t)n00 << 32) | w00, q01 = ((uint64_t)n01 << 32) | w01;
+  const uint64_t q10 = ((uint64_t)n10 << 32) | w10, q11 = ((uint64_t)n11 << 32) | w11;
+  return (int)(((q00 >> lane) & 3u) | (((q01 >> lane) & 3u) << 2) | (((q10 >> lane) & 3u) << 4) |
+               (((q11 >> lane) & 3u) << 6));
+}
+
+struct LineWords {
+  uint32_t w00, w01, w10, w11, n00, n01, n10, n11;
+  __device__ __forceinline__ void load(const uint32_t* W, int dim, int zc, int x, int y, int zb) {
+    w00 = word_at(W, dim, zc, x, y, zb);
+    w01 = word_at(W, dim, zc, x, y + 1, zb);
+    w10 = word_at(W, dim, zc, x + 1, y, zb);
+    w11 = word_at(W, dim, zc, x + 1, y + 1, zb);
+    n00 = word_at(W, dim, zc, x, y, zb + 1);
+    n01 = word_at(W, dim, zc, x, y + 1, zb + 1);
+    n10 = word_at(W, dim, zc, x + 1, y, zb + 1);
+    n11 = word_at(W, dim, zc, x + 1, y + 1, zb + 1);
+  }
+  __device__ __forceinline__ int mask(int lane) const {
+    return mask_from_lines(w00, w01, w10, w11, n00, n01, n10, n11, lane);
+  }
+};
+
+// Interior-edge test of Mode Q: the grid edge from sample s along axis a has
+// all four surrounding cells.
+__device__ __forceinline__ bool q_edge_interior(int dim, int sx, int sy, int sz, int a) {
+  const int s[3] = {sx, sy, sz};
+  const int b = (a + 1) % 3, c = (a + 2) % 3;
+  return s[a] <= dim - 2 && s[b] >= 1 && s[b] <= dim - 2 && s[c] >= 1 && s[c] <= dim - 2;
+}
+
+// Interior crossing words of Mode Q (quads) for line (x, y) block zb.
+__device__ __forceinline__ void q_quad_words(const uint32_t* W, int dim, int zc, int x, int y, int zb, uint32_t& Xi,
+                                             uint32_t& Yi, uint32_t& Zi) {
+  // z in [1, dim-2]
+  uint32_t zint = kFull;
+  const int lo = 1 - 32 * zb, hi = dim - 2 - 32 * zb;  // valid bit range [lo, hi]
+  if (hi < 0 || lo > 31) zint = 0u;
+  else {
+    if (hi < 31) zint &= (2u << hi) - 1u;
+    if (lo > 0) zint &= ~((1u << lo) - 1u);
+  }
+  Xi = (y >= 1 && y <= dim - 2) ? (xcross_word(W, dim, zc, x, y, zb) & zint) : 0u;
+  Yi = (x >= 1 && x <= dim - 2) ? (ycross_word(W, dim, zc, x, y, zb) & zint) : 0u;
+  Zi = (x >= 1 && x <= dim - 2 && y >= 1 && y <= dim - 2) ? zcross_word(W, dim, zc, x, y, zb) : 0u;
+}
+
+// ---------------------------------------------------------------------------
+// K2: per-word counts
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chunks, int n_chunks,
+                                               const int* __restrict__ unit_start, const uint32_t* __restrict__ words,
+                                               const uint32_t* __restrict__ flags, WordScratch ws) {
+  const int u = blockIdx.x;
+  const int c = find_chunk_e(unit_start, n_chunks, u);
+  const ChunkDev ch = chunks[c];
+  const int x = u - __ldg(unit_start + c);
+  const int dim = ch.dim, zc = ch.zc, nw = dim * zc;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t* W = words + ch.words;
+  const bool cm = contains_mesh(__ldg(flags + c));
+  for (int wi = warp; wi < nw; wi += nwarps) {
+    const int y = wi / zc, zb = wi - y * zc;
+    const int64_t o = ch.words + (int64_t)x * nw + wi;
+    if (!cm) {
+      if (lane == 0) {
+        ws.vcnt[o] = 0u;
+        ws.icnt[o] = 0u;
+        if (MODE == 1) { ws.gpl[3 * o] = 0u; ws.gpl[3 * o + 1] = 0u; ws.gpl[3 * o + 2] = 0u; }
+      }
+      continue;
+    }
+    const int z = 32 * zb + lane;
+    LineWords lw;
+    lw.load(W, dim, zc, x, y, zb);
+    uint32_t vc, ic;
+    if (MODE == 0) {
+      const uint32_t X = (x + 1 < dim) ? (lw.w00 ^ lw.w10) : 0u;
+      const uint32_t Y = (y + 1 < dim) ? (lw.w00 ^ lw.w01) : 0u;
+      const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
+      vc = __popc(X) + __popc(Y) + __popc(Z);
+      const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
+      int t = interior ? 3 * tri_count(lw.mask(lane)) : 0;
+      t += __shfl_xor_sync(kFull, t, 16);
+      t += __shfl_xor_sync(kFull, t, 8);
+      t += __shfl_xor_sync(kFull, t, 4);
+      t += __shfl_xor_sync(kFull, t, 2);
+      t += __shfl_xor_sync(kFull, t, 1);
+      ic = (uint32_t)t;
+    } else {
+      const bool interior = x <= dim - 2 && y <= dim - 2 && z <= dim - 2;
+      const int ng = interior ? group_count(lw.mask(lane)) : 0;
+      const uint32_t g0 = __ballot_sync(kFull, ng & 1), g1 = __ballot_sync(kFull, ng & 2),
+                     g2 = __ballot_sync(kFull, ng & 4);
+      vc = __popc(g0) + 2 * __popc(g1) + 4 * __popc(g2);
+      uint32_t Xi, Yi, Zi;
+      q_quad_words(W, dim, zc, x, y, zb, Xi, Yi, Zi);
+      ic = 4u * (__popc(Xi) + __popc(Yi) + __popc(Zi));
+      if (lane == 0) { ws.gpl[3 * o] = g0; ws.gpl[3 * o + 1] = g1; ws.gpl[3 * o + 2] = g2; }
+    }
+    if (lane == 0) {
+      ws.vcnt[o] = vc;
+      ws.icnt[o] = ic;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K3: exclusive scan of each chunk's per-word counts (one CTA per chunk).
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ void block_excl_scan2(uint32_t& a, uint32_t& b, uint32_t& tot_a, uint32_t& tot_b) {
+  __shared__ uint32_t sa[NT / 32], sb[NT / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t na = __shfl_up_sync(kFull, ia, o), nb = __shfl_up_sync(kFull, ib, o);
+    if (lane >= o) { ia += na; ib += nb; }
+  }
+  if (lane == 31) { sa[warp] = ia; sb[warp] = ib; }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t va = lane < NT / 32 ? sa[lane] : 0u, vb = lane < NT / 32 ? sb[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t na = __shfl_up_sync(kFull, va, o), nb = __shfl_up_sync(kFull, vb, o);
+      if (lane >= o) { va += na; vb += nb; }
+    }
+    if (lane < NT / 32) { sa[lane] = va; sb[lane] = vb; }
+  }
+  __syncthreads();
+  const uint32_t wa = warp ? sa[warp - 1] : 0u, wb = warp ? sb[warp - 1] : 0u;
+  tot_a = sa[NT / 32 - 1];
+  tot_b = sb[NT / 32 - 1];
+  a = wa + ia - a;
+  b = wb + ib - b;
+  __syncthreads();
+}
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_chunks(const ChunkDev* __restrict__ chunks, WordScratch ws,
+                                                            uint32_t* __restrict__ tot) {
+  const ChunkDev ch = chunks[blockIdx.x];
+  const int64_t n = (int64_t)ch.dim * ch.dim * ch.zc;
+  uint32_t* v = ws.vcnt + ch.words;
+  uint32_t* ic = ws.icnt + ch.words;
+  uint32_t carry_v = 0, carry_i = 0;
+  for (int64_t base = 0; base < n; base += (int64_t)kScanThreads * kScanItems) {
+    const int64_t i0 = base + (int64_t)threadIdx.x * kScanItems;
+    uint32_t lv[kScanItems], li[kScanItems], sv = 0, si = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      lv[k] = (i0 + k < n) ? v[i0 + k] : 0u;
+      li[k] = (i0 + k < n) ? ic[i0 + k] : 0u;
+      sv += lv[k];
+      si += li[k];
+    }
+    uint32_t ev = sv, ei = si, tv, ti;
+    block_excl_scan2<kScanThreads>(ev, ei, tv, ti);
+    ev += carry_v;
+    ei += carry_i;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      if (i0 + k < n) {
+        v[i0 + k] = ev;
+        ic[i0 + k] = ei;
+      }
+      ev += lv[k];
+      ei += li[k];
+    }
+    carry_v += tv;
+    carry_i += ti;
+  }
+  if (threadIdx.x == 0) {
+    tot[2 * blockIdx.x] = carry_v;
+    tot[2 * blockIdx.x + 1] = carry_i;
+  }
+}
+
+// Chunk offsets in the output arena + per-chunk info (single CTA).
+__global__ void __launch_bounds__(1024) k_chunk_offsets(ChunkDev* __restrict__ chunks, int n, const uint32_t* tot,
+                                                        const uint32_t* flags, int64_t vcap, int64_t icap,
+                                                        int64_t* info, int64_t* totals) {
+  __shared__ int64_t s_v[1024], s_i[1024];
+  int64_t carry_v = 0, carry_i = 0;
+  for (int base = 0; base < n; base += 1024) {
+    const int c = base + threadIdx.x;
+    const int64_t v = c < n ? (int64_t)tot[2 * c] : 0, i = c < n ? (int64_t)tot[2 * c + 1] : 0;
+    s_v[threadIdx.x] = v;
+    s_i[threadIdx.x] = i;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const int64_t av = threadIdx.x >= o ? s_v[threadIdx.x - o] : 0, ai = threadIdx.x >= o ? s_i[threadIdx.x - o] : 0;
+      __syncthreads();
+      s_v[threadIdx.x] += av;
+      s_i[threadIdx.x] += ai;
+      __syncthreads();
+    }
+    if (c < n) {
+      const int64_t vo = carry_v + s_v[threadIdx.x] - v, io = carry_i + s_i[threadIdx.x] - i;
+      chunks[c].vout = vo;
+      chunks[c].iout = io;
+      if (info) {
+        info[6 * c + 0] = vo;
+        info[6 * c + 1] = v;
+        info[6 * c + 2] = io;
+        info[6 * c + 3] = i;
+        info[6 * c + 4] = contains_mesh(flags[c]) ? 1 : 0;
+        info[6 * c + 5] = (vo + v > vcap || io + i > icap) ? 3 : 0;
+      }
+    }
+    carry_v += s_v[1023];
+    carry_i += s_i[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && totals) {
+    totals[0] = carry_v;
+    totals[1] = carry_i;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K4: emission
+// ---------------------------------------------------------------------------
+
+// Vertex id (chunk-local) of the axis-a crossing owned by sample (x, y, z).
+__device__ __forceinline__ uint32_t r_vertex_id(const uint32_t* W, const uint32_t* vbase, int dim, int zc, int x, int y,
+                                                int z, int a) {
+  const int zb = z >> 5, l = z & 31;
+  const uint32_t X = xcross_word(W, dim, zc, x, y, zb), Y = ycross_word(W, dim, zc, x, y, zb);
+  const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
+  const uint32_t lt = lane_lt(l);
+  uint32_t id = __ldg(vbase + ((int64_t)x * dim + y) * zc + zb) + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
+  if (a >= 1) id += (X >> l) & 1u;
+  if (a >= 2) id += (Y >> l) & 1u;
+  return id;
+}
+
+// Mode Q vertex base of cell (x, y, z).
+__device__ __forceinline__ uint32_t q_vertex_base(const uint32_t* vbase, const uint32_t* gpl, int dim, int zc, int x,
+                                                  int y, int z) {
+  const int64_t wi = ((int64_t)x * dim + y) * zc + (z >> 5);
+  const uint32_t lt = lane_lt(z & 31);
+  return __ldg(vbase + wi) + __popc(__ldg(gpl + 3 * wi) & lt) + 2 * __popc(__ldg(gpl + 3 * wi + 1) & lt) +
+         4 * __popc(__ldg(gpl + 3 * wi + 2) & lt);
+}
+
+__device__ __forceinline__ float dens_at(const float* D, int dim, int x, int y, int z) {
+  return __ldg(D + ((int64_t)x * dim + y) * dim + z);
+}
+
+// Central-difference grid gradient, one-sided at the chunk faces.
+__device__ __forceinline__ void grid_gradient(const float* D, int dim, int x, int y, int z, float g[3]) {
+  const int c[3] = {x, y, z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int lo[3] = {x, y, z}, hi[3] = {x, y, z};
+    float h = 0.5f;
+    if (c[a] > 0) lo[a]--; else h = 1.0f;
+    if (c[a] < dim - 1) hi[a]++; else h = 1.0f;
+    g[a] = (dens_at(D, dim, hi[0], hi[1], hi[2]) - dens_at(D, dim, lo[0], lo[1], lo[2])) * h;
+  }
+}
+
+// QEF solve, restating qef_simd.h:150-579 lane by lane in FP32 with the exact
+// 1/sqrt in place of _mm_rsqrt_ps.
+__device__ __forceinline__ float dot4(const float a[4], const float b[4]) {
+  const float m0 = a[0] * b[0], m1 = a[1] * b[1], m2 = a[2] * b[2], m3 = a[3] * b[3];
+  return (m0 + m1) + (m3 + m2);
+}
+__device__ __forceinline__ void vec_mul_m4(const float a[4], const float B[4][4], float out[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float r = a[0] * B[0][k];
+    r = r + a[1] * B[1][k];
+    r = r + a[2] * B[2][k];
+    r = r + a[3] * B[3][k];
+    out[k] = r;
+  }
+}
+
+struct QefAccum {
+  float ata[4][4];
+  float atb[4];
+  float acc[4];
+  int count;
+  __device__ __forceinline__ void init() {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) ata[r][k] = 0.0f;
+      atb[r] = 0.0f;
+      acc[r] = 0.0f;
+    }
+    count = 0;
+  }
+  // qef_simd_add, qef_simd.h:411-430
+  __device__ __forceinline__ void add(const float pp[3], const float nn[3]) {
+    const float p[4] = {pp[0], pp[1], pp[2], 1.0f};
+    const float n[4] = {nn[0], nn[1], nn[2], 0.0f};
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) ata[r][k] = ata[r][k] + n[r] * n[k];
+    }
+    const float d = dot4(p, n);
+    const float dd[4] = {d, d, d, 0.0f};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) atb[k] = atb[k] + dd[k] * n[k];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = acc[k] + p[k];
+    ++count;
+  }
+  // qef_simd_solve + svd_solve_ATA_ATb (qef_simd.h:304-461); returns false
+  // for fewer than 2 or more than 12 inputs (qef_simd.h:556-560).
+  __device__ bool solve(float out[3]) const {
+    if (count < 2 || count > 12) {
+      out[0] = out[1] = out[2] = 0.0f;
+      return false;
+    }
+    float mp[4], pr[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) mp[k] = acc[k] / acc[3];
+    vec_mul_m4(mp, ata, pr);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) pr[k] = atb[k] - pr[k];
+    float V[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 0}};
+    float vt[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) vt[r][k] = ata[r][k];
+    }
+#pragma unroll 1
+    for (int sweep = 0; sweep < 5; ++sweep) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int a = q == 2 ? 1 : 0, b = q == 0 ? 1 : 2;
+        if (vt[a][b] != 0.0f) {
+          // givens_coeffs_sym
+          const float pp = vt[a][a], pq = vt[a][b], qq = vt[b][b];
+          const float tau = (qq - pp) / (pq * 2.0f);
+          const float stt = sqrtf(tau * tau + 1.0f);
+          const float tn = 1.0f / ((tau >= 0.0f) ? (tau + stt) : (tau - stt));
+          float cc = 1.0f / sqrtf(1.0f + tn * tn);
+          float ss = tn * cc;
+          if (pq == 0.0f) { cc = 1.0f; ss = 0.0f; }
+          // rotateq_xy
+          const float c2 = cc * cc, s2 = ss * ss;
+          const float mx = ((2.0f * cc) * ss) * pq;
+          const float nx = (c2 * pp - mx) + s2 * qq;
+          const float ny = (s2 * pp + mx) + c2 * qq;
+          vt[a][a] = nx;
+          vt[b][b] = ny;
+          // rotate_xy
+          const float u3 = vt[0][3 - b], v3 = vt[1 - a][2];
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            const float uu = V[r][a], vv = V[r][b];
+            V[r][a] = cc * uu - ss * vv;
+            V[r][b] = ss * uu + cc * vv;
+          }
+          vt[0][3 - b] = cc * u3 - ss * v3;
+          vt[1 - a][2] = ss * u3 + cc * v3;
+          vt[a][b] = 0.0f;
+        }
+      }
+    }
+    const float sigma[4] = {vt[0][0], vt[1][1], vt[2][2], 0.0f};
+    float invdet[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {  // svd_invdet
+      const float oo = 1.0f / sigma[k];
+      const float a1 = fabsf(sigma[k]), a2 = fabsf(oo);
+      const float mn = (a1 < a2) ? a1 : a2;
+      invdet[k] = (mn >= 0.001f) ? oo : 0.0f;
+    }
+    float mm[3][4], o[4][4];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) mm[r][k] = V[r][k] * invdet[k];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) o[r][k] = (r < 3 && k < 3) ? dot4(mm[k], V[r]) : 0.0f;
+    }
+    float xq[4];
+    vec_mul_m4(pr, o, xq);
+    out[0] = xq[0] + mp[0];
+    out[1] = xq[1] + mp[1];
+    out[2] = xq[2] + mp[2];
+    return true;
+  }
+};
+
+// Crossing point (and hermite normal) of edge e of cell (x, y, z).
+__device__ __forceinline__ void hermite(const float* D, int dim, int x, int y, int z, int e, bool want_n, float p[3],
+                                        float n[3]) {
+  const int ca = edge_c0(e), cb = edge_c1(e);
+  const int a0[3] = {x + ((ca >> 2) & 1), y + ((ca >> 1) & 1), z + (ca & 1)};
+  const int a1[3] = {x + ((cb >> 2) & 1), y + ((cb >> 1) & 1), z + (cb & 1)};
+  const float s0 = dens_at(D, dim, a0[0], a0[1], a0[2]), s1 = dens_at(D, dim, a1[0], a1[1], a1[2]);
+  const float mu = (0.0f - s0) / (s1 - s0);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float dv = ((float)a1[k] - (float)a0[k]) * mu;
+    p[k] = dv + (float)a0[k];
+  }
+  if (want_n) {
+    float g0[3], g1[3], g[3];
+    grid_gradient(D, dim, a0[0], a0[1], a0[2], g0);
+    grid_gradient(D, dim, a1[0], a1[1], a1[2], g1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) g[k] = g0[k] + (g1[k] - g0[k]) * mu;
+    const float l2 = (g[0] * g[0] + g[1] * g[1]) + g[2] * g[2];
+    const float inv = 1.0f / sqrtf(l2);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) n[k] = g[k] * inv;
+  }
+}
+
+template <int PLACE>
+__device__ __forceinline__ void q_place(const float* D, int dim, int x, int y, int z, int mask, int g, float out[3]) {
+  if (PLACE == 0) {
+    out[0] = (float)x + 0.5f;
+    out[1] = (float)y + 0.5f;
+    out[2] = (float)z + 0.5f;
+    return;
+  }
+  float mp[3] = {0.0f, 0.0f, 0.0f};
+  int cnt = 0;
+  QefAccum q;
+  if (PLACE == 2) q.init();
+  for (int e = 0; e < 12; ++e) {
+    if (group_of(mask, e) != g) continue;
+    float p[3], n[3];
+    hermite(D, dim, x, y, z, e, PLACE == 2, p, n);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) mp[k] = mp[k] + p[k];
+    ++cnt;
+    if (PLACE == 2) q.add(p, n);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) mp[k] = mp[k] / (float)cnt;
+  if (PLACE == 2) {
+    float s[3];
+    q.solve(s);
+    const bool ok = s[0] >= (float)x && s[0] <= (float)(x + 1) && s[1] >= (float)y && s[1] <= (float)(y + 1) &&
+                    s[2] >= (float)z && s[2] <= (float)(z + 1);
+    if (ok) {
+      out[0] = s[0]; out[1] = s[1]; out[2] = s[2];
+      return;
+    }
+  }
+  out[0] = mp[0]; out[1] = mp[1]; out[2] = mp[2];
+}
+
+template <int MODE, int PLACE>
+__global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunks, int n_chunks,
+                                              const int* __restrict__ unit_start, const uint32_t* __restrict__ words,
+                                              const float* __restrict__ dens, const uint32_t* __restrict__ flags,
+                                              WordScratch ws, MeshOut out) {
+  const int u = blockIdx.x;
+  const int c = find_chunk_e(unit_start, n_chunks, u);
+  if (!contains_mesh(__ldg(flags + c))) return;
+  const ChunkDev ch = chunks[c];
+  const int x = u - __ldg(unit_start + c);
+  const int dim = ch.dim, zc = ch.zc, nw = dim * zc;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t* W = words + ch.words;
+  const uint32_t* vbase = ws.vcnt + ch.words;
+  const uint32_t* ibase = ws.icnt + ch.words;
+  const float* D = dens + ch.dens;
+  const uint32_t lt = lane_lt(lane);
+  for (int wi = warp; wi < nw; wi += nwarps) {
+    const int y = wi / zc, zb = wi - y * zc;
+    const int z = 32 * zb + lane;
+    const int64_t wo = (int64_t)x * nw + wi;
+    LineWords lw;
+    lw.load(W, dim, zc, x, y, zb);
+    if (MODE == 0) {
+      // ---- vertices: calculate_cell / calculate_isovertex order ----
+      const uint32_t X = (x + 1 < dim) ? (lw.w00 ^ lw.w10) : 0u;
+      const uint32_t Y = (y + 1 < dim) ? (lw.w00 ^ lw.w01) : 0u;
+      const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
+      if ((X | Y | Z) != 0u) {
+        uint32_t vid = __ldg(vbase + wo) + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
+        const uint32_t own = ((X >> lane) & 1u) | (((Y >> lane) & 1u) << 1) | (((Z >> lane) & 1u) << 2);
+        for (int a = 0; a < 3; ++a) {
+          if (!((own >> a) & 1u)) continue;
+          const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+          const int64_t gv = ch.vout + vid;
+          ++vid;
+          if (gv >= out.vcap) continue;
+          const float s0 = dens_at(D, dim, x, y, z), s1 = dens_at(D, dim, x1, y1, z1);
+          const float mu = (0.0f - s0) / (s1 - s0);
+          const float q0[3] = {(float)x, (float)y, (float)z};
+          const float dl[3] = {(float)(x1 - x), (float)(y1 - y), (float)(z1 - z)};
+          float* P = out.pos + 3 * gv;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const float dv = dl[k] * mu;
+            P[k] = dv + q0[k];
+          }
+          if (out.boundary)
+            out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
+                                x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
+          if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
+          if (out.valence) {
+            // init_valence: uses of this edge by the (up to) four interior
+            // cells around it (polygonize skips far-face cells, DMCChunk.cpp:528).
+            int val = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int d1 = k >> 1, d2 = k & 1;
+              int cx = x, cy = y, cz = z, e;
+              if (a == 0) { cy -= d1; cz -= d2; e = 2 * d1 + d2; }
+              else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
+              else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
+              if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
+              val += edge_uses(cell_mask_at(W, dim, zc, cx, cy, cz), e);
+            }
+            out.valence[gv] = (uint8_t)val;
+          }
+        }
+      }
+      // ---- triangles: polygonize_cell order ----
+      const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
+      const int mask = interior ? lw.mask(lane) : 0;
+      const uint64_t tw = c_tri_cases[mask];
+      const int t3 = 3 * (int)(tw >> 60);
+      if (__ballot_sync(kFull, t3 != 0) == 0u) continue;
+      const int incl = warp_incl_scan(t3);
+      int64_t gi = ch.iout + (int64_t)__ldg(ibase + wo) + (incl - t3);
+      for (int i = 0; i < t3; ++i, ++gi) {
+        const int e = tri_edge(tw, i);
+        const uint32_t vid = r_vertex_id(W, vbase, dim, zc, x + c_edge_owner[e][0], y + c_edge_owner[e][1],
+                                         z + c_edge_owner[e][2], c_edge_owner[e][3]);
+        if (gi < out.icap) out.idx[gi] = vid;
+      }
+    } else {
+      // ---- Mode Q vertices: one per vertex group of each interior surface cell ----
+      const bool interior = x <= dim - 2 && y <= dim - 2 && z <= dim - 2;
+      const int mask = interior ? lw.mask(lane) : 0;
+      const int ng = group_count(mask);
+      const int64_t gpo = 3 * (ch.words + wo);
+      if (ng) {
+        uint32_t vid = __ldg(vbase + wo) + __popc(__ldg(ws.gpl + gpo) & lt) +
+                       2 * __popc(__ldg(ws.gpl + gpo + 1) & lt) + 4 * __popc(__ldg(ws.gpl + gpo + 2) & lt);
+        const int nc = dim - 1;
+        const uint8_t bnd = (x == 0 || y == 0 || z == 0 || x == nc - 1 || y == nc - 1 || z == nc - 1);
+        for (int g = 0; g < ng; ++g, ++vid) {
+          const int64_t gv = ch.vout + vid;
+          if (gv >= out.vcap) continue;
+          float P[3];
+          q_place<PLACE>(D, dim, x, y, z, mask, g, P);
+          out.pos[3 * gv] = P[0];
+          out.pos[3 * gv + 1] = P[1];
+          out.pos[3 * gv + 2] = P[2];
+          if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
+          if (out.boundary) out.boundary[gv] = bnd;
+          if (out.valence) {
+            int val = 0;
+            for (int e = 0; e < 12; ++e) {
+              if (group_of(mask, e) != g) continue;
+              const int c0 = edge_c0(e);
+              val += q_edge_interior(dim, x + ((c0 >> 2) & 1), y + ((c0 >> 1) & 1), z + (c0 & 1), e >> 2);
+            }
+            out.valence[gv] = (uint8_t)val;
+          }
+        }
+      }
+      // ---- quads: one per interior sign-changing grid edge ----
+      uint32_t Xi, Yi, Zi;
+      q_quad_words(W, dim, zc, x, y, zb, Xi, Yi, Zi);
+      const int own = (int)(((Xi >> lane) & 1u) | (((Yi >> lane) & 1u) << 1) | (((Zi >> lane) & 1u) << 2));
+      const int nq = __popc(own);
+      if (__ballot_sync(kFull, nq != 0) == 0u) continue;
+      const int incl = warp_incl_scan(4 * nq);
+      int64_t gi = ch.iout + (int64_t)__ldg(ibase + wo) + (incl - 4 * nq);
+      const bool in0 = ((lw.w00 >> lane) & 1u) != 0u;
+      for (int a = 0; a < 3; ++a) {
+        if (!((own >> a) & 1)) continue;
+        const int b = (a + 1) % 3, cax = (a + 2) % 3;
+        uint32_t q[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int ob = (k == 0 || k == 3) ? -1 : 0, oc = (k < 2) ? -1 : 0;
+          int cc[3] = {x, y, z};
+          cc[b] += ob;
+          cc[cax] += oc;
+          int lo[3] = {0, 0, 0};
+          lo[b] = -ob;
+          lo[cax] = -oc;
+          const int e = a == 0 ? 2 * lo[1] + lo[2] : (a == 1 ? 4 + 2 * lo[0] + lo[2] : 8 + 2 * lo[0] + lo[1]);
+          const int cm = cell_mask_at(W, dim, zc, cc[0], cc[1], cc[2]);
+          q[k] = q_vertex_base(vbase, ws.gpl + 3 * ch.words, dim, zc, cc[0], cc[1], cc[2]) + (uint32_t)group_of(cm, e);
+        }
+        if (!in0) {
+          const uint32_t t = q[1];
+          q[1] = q[3];
+          q[3] = t;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k, ++gi)
+          if (gi < out.icap) {
+            out.idx[gi] = q[k];
+            if (out.idx_global) out.idx_global[gi] = (uint32_t)(ch.vout + q[k]);
+          }
+      }
+    }
+  }
+}
+
+void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
+                  const uint32_t* words, const uint32_t* flags, WordScratch ws, cudaStream_t st) {
+  if (mode == 0) k_count<0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
+  else k_count<1><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
+}
+
+void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, uint32_t* d_tot, cudaStream_t st) {
+  k_scan_chunks<<<n_chunks, kScanThreads, 0, st>>>(d_chunks, ws, d_tot);
+}
+
+void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_tot, const uint32_t* flags,
+                          int64_t vcap, int64_t icap, int64_t* d_info, int64_t* d_totals, cudaStream_t st) {
+  k_chunk_offsets<<<1, 1024, 0, st>>>(d_chunks, n_chunks, d_tot, flags, vcap, icap, d_info, d_totals);
+}
+
+void launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start,
+                 int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
+                 MeshOut out, cudaStream_t st) {
+  if (mode == 0) {
+    k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
+  } else if (placement == 0) {
+    k_emit<1, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
+  } else if (placement == 1) {
+    k_emit<1, 1><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
+  } else {
+    k_emit<1, 2><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
+  }
+}
+
+}  // namespace bmf

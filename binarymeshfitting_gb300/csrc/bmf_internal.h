@@ -1,0 +1,72 @@
+// Host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bmf {
+
+struct ChunkDev;
+struct FieldDev;
+
+// Output arena for one launch of the emit kernels (single chunk or batch).
+struct MeshOut {
+  float* pos;
+  float* nrm;
+  uint8_t* boundary;
+  uint8_t* valence;
+  uint32_t* idx;          // chunk-local vertex ids (one VerticesIndicesBlock per chunk)
+  uint32_t* idx_global;   // optional: the same indices offset by the chunk's vertex base
+  int64_t vcap, icap;
+};
+
+// Per-word scratch of the extraction kernels, indexed like the occupancy
+// words (chunk.words + (x*dim + y)*zc + zb).
+struct WordScratch {
+  uint32_t* vcnt;   // vertices hosted by the word's 32 cells; scanned in place to the chunk-local base
+  uint32_t* icnt;   // indices emitted by the word's cells; scanned in place
+  uint32_t* gpl;    // Mode Q: 3 bit-planes of the per-cell vertex-group count
+};
+
+void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units, int max_dim,
+                         const FieldDev& field, const float* dens_in, float* dens_out, uint32_t* words,
+                         uint32_t* flags, cudaStream_t st);
+void launch_cell_masks(int dim, const uint32_t* W, uint8_t* masks, cudaStream_t st);
+// contains_mesh flags of chunks whose words were produced elsewhere.
+void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, uint32_t* flags,
+                       cudaStream_t st);
+
+// Extraction: count -> per-chunk scan -> (chunk offsets) -> emit.
+void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
+                  const uint32_t* words, const uint32_t* flags, WordScratch ws, cudaStream_t st);
+// Scans each chunk's word counts; writes chunk totals (vertices, indices) to d_tot[2c].
+void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, uint32_t* d_tot, cudaStream_t st);
+// Exclusive scan of the chunk totals into chunk.vout / chunk.iout, and the
+// per-chunk info table {voff, vcount, ioff, icount, contains_mesh, status}.
+void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_tot, const uint32_t* flags,
+                          int64_t vcap, int64_t icap, int64_t* d_info, int64_t* d_totals, cudaStream_t st);
+void launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start,
+                 int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
+                 MeshOut out, cudaStream_t st);
+
+// MeshProcessor: operates on one flat mesh (vertices [0, nv), prims of N).
+struct ProcessScratch {
+  uint32_t* off;      // nv + 1 CSR offsets
+  uint32_t* cursor;   // nv fill cursors
+  uint32_t* adj;      // sum of valences
+  float* dual_p;      // 3 * n_prims
+  float* dual_n;      // 3 * n_prims
+  uint32_t* tmp;      // scan scratch (block totals)
+};
+// nv / n_prims size the grids; when d_counts is given the actual vertex and
+// index counts are read from d_counts[0] / d_counts[1] on the device (so the
+// sequence can be captured in a CUDA graph before the counts are known).
+// Scratch sizes: off nv+1, cursor nv, adj N*n_prims, dual_p/dual_n 3*n_prims,
+// tmp ceil(nv / 4096) + 1.
+void launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
+                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
+                    int process_boundary, int smooth_normals, ProcessScratch s, cudaStream_t st);
+void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n, const int64_t* d_n,
+                                     uint32_t* block_tmp, cudaStream_t st);
+
+}  // namespace bmf

@@ -1,0 +1,293 @@
+// Stage 5: MeshProcessor<N> dual / primal smoothing and normals
+// (MeshProcessor.cpp:26-306), in the order ChunkGenerator::extract_chunk runs
+// it (ChunkGenerator.cpp:112-124): iters dual steps, a primal step after each
+// but the last inside optimize_dual_grid, then one more primal step.
+//
+// The reference's sweeps are Jacobi-style (a dual step reads only vertex
+// positions, a primal step reads only dual points), so every primitive and
+// every vertex is independent: one thread each.  The one order that matters
+// for bit-exact sums is the adjacency order: init_primitives appends prims to
+// each vertex in ascending prim id (MeshProcessor.cpp:114-127).  The CSR
+// fill uses atomic cursors and then sorts each (short) list.
+#include "bmf_device.cuh"
+#include "bmf_internal.h"
+
+namespace bmf {
+
+constexpr int kScanBlock = 1024;
+constexpr int kScanPer = 4;
+
+// Block-level exclusive scan of u8 counts -> u32 offsets; writes block totals.
+__global__ void __launch_bounds__(kScanBlock) k_scan_u8_local(const uint8_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                             int64_t n, const int64_t* __restrict__ d_n,
+                                                             uint32_t* __restrict__ block_tot) {
+  __shared__ uint32_t warp_tot[kScanBlock / 32];
+  const int64_t n_valid = d_n ? min(n, *d_n) : n;
+  const int64_t i0 = ((int64_t)blockIdx.x * kScanBlock + threadIdx.x) * kScanPer;
+  uint32_t v[kScanPer], s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    v[k] = (i0 + k < n_valid) ? in[i0 + k] : 0u;
+    s += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(kFull, w, o);
+      if (lane >= o) w += t;
+    }
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  uint32_t e = (warp ? warp_tot[warp - 1] : 0u) + inc - s;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    if (i0 + k < n) out[i0 + k] = e;
+    e += v[k];
+  }
+  if (threadIdx.x == kScanBlock - 1) block_tot[blockIdx.x] = warp_tot[31];
+}
+
+// Scans the block totals in place (single CTA) and stores the grand total at [nb].
+__global__ void __launch_bounds__(1024) k_scan_totals(uint32_t* __restrict__ t, int nb) {
+  __shared__ uint32_t s[1024];
+  uint32_t carry = 0;
+  for (int base = 0; base < nb; base += 1024) {
+    const int i = base + threadIdx.x;
+    const uint32_t v = i < nb ? t[i] : 0u;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      const uint32_t a = threadIdx.x >= o ? s[threadIdx.x - o] : 0u;
+      __syncthreads();
+      s[threadIdx.x] += a;
+      __syncthreads();
+    }
+    if (i < nb) t[i] = carry + s[threadIdx.x] - v;
+    carry += s[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) t[nb] = carry;
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, int64_t n, const uint32_t* __restrict__ block_off) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += block_off[i / ((int64_t)kScanBlock * kScanPer)];
+}
+
+void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n, const int64_t* d_n,
+                                     uint32_t* block_tmp, cudaStream_t st) {
+  const int64_t per = (int64_t)kScanBlock * kScanPer;
+  const int nb = (int)((n + per - 1) / per);
+  if (nb == 0) return;
+  k_scan_u8_local<<<nb, kScanBlock, 0, st>>>(in, out, n, d_n, block_tmp);
+  k_scan_totals<<<1, 1024, 0, st>>>(block_tmp, nb);
+  k_scan_add<<<(int)((n + 255) / 256), 256, 0, st>>>(out, n, block_tmp);
+  // off[n] = total
+  cudaMemcpyAsync(out + n, block_tmp + nb, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+}
+
+// set_adj (MeshRecursion.hpp:173-190): adj[off[v] + k] = prim.
+__global__ void k_fill_adj(int N, int64_t n_slots, const int64_t* __restrict__ d_counts,
+                           const uint32_t* __restrict__ idx, const uint32_t* __restrict__ off,
+                           const uint8_t* __restrict__ valence, uint32_t* __restrict__ cursor,
+                           uint32_t* __restrict__ adj) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= (d_counts ? min(n_slots, d_counts[1] / N * N) : n_slots)) return;
+  const uint32_t v = idx[j];
+  const uint32_t k = atomicAdd(cursor + v, 1u);
+  if (k < valence[v]) adj[off[v] + k] = (uint32_t)(j / N);
+}
+
+// Restores ascending prim order in each vertex's list (insertion sort; the
+// lists hold at most a few dozen entries).
+__global__ void k_sort_adj(int64_t nv, const int64_t* __restrict__ d_counts, const uint32_t* __restrict__ off,
+                           const uint32_t* __restrict__ cursor, const uint8_t* __restrict__ valence,
+                           uint32_t* __restrict__ adj) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
+  const uint32_t n = min(cursor[v], (uint32_t)valence[v]);
+  uint32_t* a = adj + off[v];
+  for (uint32_t i = 1; i < n; ++i) {
+    const uint32_t key = a[i];
+    int j = (int)i - 1;
+    while (j >= 0 && a[j] > key) {
+      a[j + 1] = a[j];
+      --j;
+    }
+    a[j + 1] = key;
+  }
+}
+
+__device__ __forceinline__ void nrm3(const float v[3], float o[3]) {
+  const float l2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+  const float inv = 1.0f / sqrtf(l2);
+  o[0] = v[0] * inv;
+  o[1] = v[1] * inv;
+  o[2] = v[2] * inv;
+}
+__device__ __forceinline__ void cross3(const float a[3], const float b[3], float o[3]) {
+  o[0] = a[1] * b[2] - b[1] * a[2];
+  o[1] = a[2] * b[0] - b[2] * a[0];
+  o[2] = a[0] * b[1] - b[0] * a[1];
+}
+
+// optimize_dual_grid body (MeshProcessor.cpp:142-227).  normal_mode: 0 none,
+// 1 face normal, 2 sum of vertex normals.
+template <int N>
+__global__ void k_dual(int64_t n_prims, const int64_t* __restrict__ d_counts, const uint32_t* __restrict__ idx,
+                       const float* __restrict__ pos, const float* __restrict__ nrm, float* __restrict__ dual_p,
+                       float* __restrict__ dual_n, int normal_mode) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (d_counts ? min(n_prims, d_counts[1] / N) : n_prims)) return;
+  uint32_t v[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) v[k] = __ldg(idx + N * t + k);
+  float p[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p[c] = p[c] + __ldg(pos + 3 * v[k] + c);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) dual_p[3 * t + c] = p[c] / (float)N;
+  if (normal_mode == 0) return;
+  float o[3];
+  if (normal_mode == 1) {
+    if (N == 3) {
+      float a[3] = {0.0f, 0.0f, 0.0f}, b[3] = {0.0f, 0.0f, 0.0f}, na[3], nb[3];
+      if (v[0] != v[1] && v[1] != v[2] && v[0] != v[2]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          a[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[1] + c);
+          b[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[2] + c);
+        }
+      }
+      nrm3(a, na);
+      nrm3(b, nb);
+      cross3(na, nb, o);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c] = -o[c];
+    } else {
+      float a[3], b[3], na[3], nb[3], n1[3], n2[3];
+      const uint32_t v3 = v[N - 1];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[1] + c);
+        b[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[2] + c);
+      }
+      nrm3(a, na);
+      nrm3(b, nb);
+      cross3(na, nb, n1);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a[c] = __ldg(pos + 3 * v[2] + c) - __ldg(pos + 3 * v3 + c);
+        b[c] = __ldg(pos + 3 * v[2] + c) - __ldg(pos + 3 * v[0] + c);
+      }
+      nrm3(a, na);
+      nrm3(b, nb);
+      cross3(na, nb, n2);
+      if (isnan(n1[0])) {
+        n1[0] = n2[0]; n1[1] = n2[1]; n1[2] = n2[2];
+        if (isnan(n1[0])) { n1[0] = 0.0f; n1[1] = 1.0f; n1[2] = 0.0f; }
+      }
+      if (isnan(n2[0])) { n2[0] = n1[0]; n2[1] = n1[1]; n2[2] = n1[2]; }
+      const float h[3] = {(n1[0] + n2[0]) * 0.5f, (n1[1] + n2[1]) * 0.5f, (n1[2] + n2[2]) * 0.5f};
+      nrm3(h, o);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c] = -o[c];
+    }
+  } else {
+    o[0] = o[1] = o[2] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c] = o[c] + __ldg(nrm + 3 * v[k] + c);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) dual_n[3 * t + c] = o[c];
+}
+
+// optimize_primal_grid (MeshProcessor.cpp:238-306).
+__global__ void k_primal(int64_t nv, const int64_t* __restrict__ d_counts, const uint32_t* __restrict__ off,
+                         const uint32_t* __restrict__ cursor,
+                         const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
+                         const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
+                         const float* __restrict__ dual_n, float* __restrict__ pos, float* __restrict__ nrm,
+                         int process_boundary, int smooth_normals, int set_colors) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
+  const uint32_t n = min(cursor[v], (uint32_t)valence[v]);
+  if (n == 0 || (!process_boundary && boundary[v])) return;
+  const uint32_t* a = adj + off[v];
+  float p[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint32_t t = __ldg(a + k);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p[c] = p[c] + __ldg(dual_p + 3 * t + c);
+    if (smooth_normals) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) nn[c] = nn[c] + __ldg(dual_n + 3 * t + c);
+    }
+  }
+  const float cnt = (float)n;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) p[c] = p[c] / cnt;
+  if (smooth_normals) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nn[c] = nn[c] / cnt;
+  }
+  if (set_colors) {
+    float o[3];
+    nrm3(nn, o);
+    nn[0] = o[0]; nn[1] = o[1]; nn[2] = o[2];
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) pos[3 * v + c] = p[c];
+  if (nrm && nn[1] != 0.0f) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nrm[3 * v + c] = nn[c];
+  }
+}
+
+void launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
+                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
+                    int process_boundary, int smooth_normals, ProcessScratch s, cudaStream_t st) {
+  if (nv == 0 || n_prims == 0 || iters <= 0) return;
+  const int64_t n_slots = n_prims * N;
+  // CSR offsets: exclusive scan of init_valence (MeshProcessor.cpp:32-40)
+  launch_exclusive_scan_u8_to_u32(valence, s.off, nv, d_counts, s.tmp, st);
+  cudaMemsetAsync(s.cursor, 0, (size_t)nv * sizeof(uint32_t), st);
+  k_fill_adj<<<(int)((n_slots + 255) / 256), 256, 0, st>>>(N, n_slots, d_counts, idx, s.off, valence, s.cursor,
+                                                           s.adj);
+  const int vb = (int)((nv + 255) / 256), pb = (int)((n_prims + 255) / 256);
+  k_sort_adj<<<vb, 256, 0, st>>>(nv, d_counts, s.off, s.cursor, valence, s.adj);
+  const int hard_norm_max = 10;
+  const int max_norms = (iters / 2 - 3 < hard_norm_max ? iters / 2 - 3 : hard_norm_max);
+  const bool sn = smooth_normals != 0 && nrm != nullptr;
+  for (int m = 0; m < iters; ++m) {
+    const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
+    if (N == 3)
+      k_dual<3><<<pb, 256, 0, st>>>(n_prims, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
+    else
+      k_dual<4><<<pb, 256, 0, st>>>(n_prims, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
+    // primal after every dual step but the last (MeshProcessor.cpp:229-232),
+    // and once more after the loop with set_colors false (ChunkGenerator.cpp:120)
+    const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
+    k_primal<<<vb, 256, 0, st>>>(nv, d_counts, s.off, s.cursor, valence, s.adj, boundary, s.dual_p, s.dual_n, pos,
+                                 nrm, process_boundary, sn ? 1 : 0, set_colors);
+  }
+}
+
+}  // namespace bmf

@@ -1,0 +1,197 @@
+/* bmf.h -- C ABI of the GB300-native chunk-extraction library (libbmf_gb300.so).
+ *
+ * The reference (BinaryMeshFitting) has no C ABI: its extraction surface is the
+ * C++ Sampler functor triple, DMCChunk's stage methods, MeshProcessor<N> and
+ * ChunkGenerator::process_queue.  Each entry point below replaces one of
+ * those, as cited beside it.  Conventions:
+ *   - every call returns a bmf_status; bmf_last_error() gives a message;
+ *   - pointers named d_* are device pointers owned by the caller; h_* are host
+ *     pointers; nothing is freed across the ABI;
+ *   - `stream` is a cudaStream_t (0 = the legacy default stream);
+ *   - outputs carry counts, and a capacity overflow is reported as
+ *     BMF_ERR_CAPACITY with the needed counts filled in (nothing is written
+ *     out of bounds);
+ *   - a context is not thread-safe: use one per host thread (the reference
+ *     gives each OpenMP worker its own chunk, ChunkGenerator.cpp:91).
+ *
+ * Grid conventions (as in the reference): a chunk has dim samples per axis and
+ * dim-1 cells per axis; sample (x,y,z) sits at index x*dim*dim + y*dim + z
+ * (z fastest) and at world position origin + (x,y,z)*scale; positions in the
+ * output mesh are in sample-index units (the reference's shader applies
+ * world = p*scale + origin, shaders/main_vs.glsl:34).
+ */
+#ifndef BMF_H
+#define BMF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "bmf_fields.h"
+
+#if defined(__GNUC__)
+#define BMF_API __attribute__((visibility("default")))
+#else
+#define BMF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bmf_status {
+  BMF_OK = 0,
+  BMF_ERR_INVALID_ARGUMENT = 1,
+  BMF_ERR_CUDA = 2,
+  BMF_ERR_CAPACITY = 3,      /* output capacity too small; needed counts reported */
+  BMF_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+  BMF_ERR_OUT_OF_MEMORY = 5,
+  BMF_ERR_NOT_SUPPORTED = 6
+} bmf_status;
+
+typedef struct bmf_ctx bmf_ctx;
+
+typedef struct bmf_config {
+  int32_t device;          /* CUDA device ordinal */
+  int32_t flags;           /* reserved, 0 */
+  size_t scratch_bytes;    /* initial scratch arena size (0 = grow on demand) */
+} bmf_config;
+
+/* One density source: the Sampler plugin (Sampler.hpp:20-34). */
+typedef struct bmf_field {
+  int32_t kind;                          /* BMF_FIELD_* (bmf_fields.h) */
+  float params[BMF_FIELD_MAX_PARAMS];
+} bmf_field;
+
+/* One chunk: DMCChunk's pos/overlap/scale after label_grid set them
+ * (DMCChunk.cpp:94-98): origin = overlap_pos, scale = delta. */
+typedef struct bmf_chunk_desc {
+  float origin[3];
+  float scale;
+  int32_t dim;             /* samples per axis, 2..1024 */
+  int32_t level;           /* LOD level (informational) */
+} bmf_chunk_desc;
+
+/* Topology modes. */
+#define BMF_MODE_R 0   /* reference: Marching-Cubes triangles on edge crossings (DMCChunk::polygonize) */
+#define BMF_MODE_Q 1   /* dual marching cubes quads, one vertex per Tables::EdgeTable group */
+
+/* Mode Q vertex placement. */
+#define BMF_PLACE_CENTER 0
+#define BMF_PLACE_MASSPOINT 1
+#define BMF_PLACE_QEF 2       /* qef_simd.h solve on hermite data (grid-gradient normals) */
+
+typedef struct bmf_extract_opts {
+  int32_t mode;             /* BMF_MODE_* */
+  int32_t placement;        /* BMF_PLACE_* (Mode Q) */
+  int32_t iters;            /* MeshProcessor iterations (0 = none), WorldProperties::process_iters */
+  int32_t process_boundary; /* WorldProperties::boundary_processing */
+  int32_t smooth_normals;   /* MeshProcessor smooth_normals (SMOOTH_NORMALS) */
+  int32_t reserved;
+} bmf_extract_opts;
+
+/* A chunk mesh in caller-owned device buffers (VerticesIndicesBlock,
+ * ChunkBlocks.hpp:161-179, as structure-of-arrays). */
+typedef struct bmf_mesh {
+  float* d_pos;        /* vcap * 3 */
+  float* d_nrm;        /* vcap * 3, may be NULL (then normals are not produced) */
+  uint8_t* d_boundary; /* vcap, may be NULL */
+  uint8_t* d_valence;  /* vcap, may be NULL (init_valence) */
+  uint32_t* d_idx;     /* icap */
+  int64_t vcap, icap;
+  /* outputs */
+  int64_t n_verts, n_idx;
+  int32_t contains_mesh;
+  int32_t prim_size;   /* 3 (Mode R) or 4 (Mode Q) */
+} bmf_mesh;
+
+/* ---- context ---- */
+BMF_API bmf_status bmf_create(const bmf_config* cfg, bmf_ctx** out);
+BMF_API bmf_status bmf_destroy(bmf_ctx* ctx);
+BMF_API const char* bmf_status_string(bmf_status s);
+BMF_API const char* bmf_last_error(const bmf_ctx* ctx);
+/* Number of kernels this context has launched (instrumentation). */
+BMF_API int64_t bmf_launch_count(const bmf_ctx* ctx);
+
+/* ---- stage entry points (per chunk) ---- */
+
+/* Sampler::block (Sampler.hpp:21; ImplicitSampler.hpp:14-36,
+ * NoiseSampler.cpp:148-263): fill d_density[dim^3] for the chunk. */
+BMF_API bmf_status bmf_sample_block(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
+                            void* stream);
+
+/* DMCChunk::label_grid binarisation (DMCChunk.cpp:113-162): d_words gets
+ * dim*dim*ceil(dim/32) occupancy words (bit z%32 of word [x][y][z/32] set
+ * when density < 0); *h_contains_mesh (may be NULL) gets the reference's
+ * contains_mesh flag (synchronises the stream when non-NULL). */
+BMF_API bmf_status bmf_label_grid(bmf_ctx* ctx, int32_t dim, const float* d_density, uint32_t* d_words,
+                          int32_t* h_contains_mesh, void* stream);
+
+/* Fused Sampler::block + label_grid: density (d_density may be NULL when only
+ * the occupancy words are wanted) and words in one pass. */
+BMF_API bmf_status bmf_sample_label(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
+                            uint32_t* d_words, int32_t* h_contains_mesh, void* stream);
+
+/* DMCChunk::label_edges mask passes (DMCChunk.cpp:202-438): one byte per cell,
+ * d_masks[(x*dim + y)*zpad + z], zpad = 32*ceil(dim/32); bit (4dx+2dy+dz) set
+ * when corner (x+dx,y+dy,z+dz) exists and is inside.  For dim % 32 == 0 this
+ * is byte-for-byte the reference's uint64 MasksBlock. */
+BMF_API bmf_status bmf_cell_masks(bmf_ctx* ctx, int32_t dim, const uint32_t* d_words, uint8_t* d_masks, void* stream);
+
+/* DMCChunk::label_edges enumeration + polygonize (DMCChunk.cpp:440-576) for
+ * Mode R, or the DMC quad emitter for Mode Q.  Synchronises the stream to
+ * report counts in *out. */
+BMF_API bmf_status bmf_polygonize(bmf_ctx* ctx, int32_t dim, const float* d_density, const uint32_t* d_words,
+                          int32_t mode, int32_t placement, bmf_mesh* out, void* stream);
+
+/* MeshProcessor<N>::init/optimize_dual_grid/optimize_primal_grid/flush
+ * (MeshProcessor.cpp:26-306) in the order ChunkGenerator::extract_chunk uses
+ * (ChunkGenerator.cpp:112-124).  Updates d_pos (and d_nrm when non-NULL) in
+ * place; N = mesh->prim_size. */
+BMF_API bmf_status bmf_process(bmf_ctx* ctx, bmf_mesh* mesh, int32_t iters, int32_t process_boundary,
+                       int32_t smooth_normals, void* stream);
+
+/* ChunkGenerator::extract_chunk for one chunk (ChunkGenerator.cpp:98-124):
+ * sample -> label -> polygonize -> process.  d_density_scratch may be NULL
+ * (the context then uses its own scratch). */
+BMF_API bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field,
+                             const bmf_extract_opts* opts, bmf_mesh* out, void* stream);
+
+/* ---- batched form: ChunkGenerator::process_queue (ChunkGenerator.hpp:23) ----
+ * A plan owns the device descriptor queue and the scratch for one batch shape
+ * and records the whole update as a CUDA graph. */
+typedef struct bmf_batch bmf_batch;
+
+typedef struct bmf_batch_out {
+  float* d_pos;          /* vcap * 3 */
+  float* d_nrm;          /* vcap * 3 or NULL */
+  uint8_t* d_boundary;   /* vcap or NULL */
+  uint32_t* d_idx;       /* icap; indices are chunk-local (as each VerticesIndicesBlock) */
+  int64_t vcap, icap;
+  /* d_chunk_info[6*i + k], k: 0 vertex offset, 1 vertex count, 2 index
+   * offset, 3 index count, 4 contains_mesh, 5 status (0 ok, 3 capacity) */
+  int64_t* d_chunk_info;
+  /* outputs (host) */
+  int64_t n_verts, n_idx;
+} bmf_batch_out;
+
+BMF_API bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t n_chunks, const bmf_field* field,
+                            const bmf_extract_opts* opts, bmf_batch** out);
+/* Runs the update.  use_graph != 0 replays the captured CUDA graph.
+ * sync != 0 waits and fills out->n_verts / n_idx. */
+BMF_API bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, int32_t sync, void* stream);
+BMF_API bmf_status bmf_batch_destroy(bmf_batch* b);
+/* Replaces the plan's chunk descriptors with those of the next update (same
+ * count and the same dim per slot, e.g. the next frame of a streaming world):
+ * an asynchronous pinned host->device copy on `stream`, so the captured graph
+ * replays on the new chunks.  The caller's array may be reused on return. */
+BMF_API bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_descs, int32_t n_chunks, void* stream);
+/* Runs one update stage by stage (no graph) with CUDA events between the
+ * stages on `stream` and returns the stage times in ms:
+ * h_stage_ms[0] fill+label, [1] count, [2] scan, [3] offsets, [4] emit,
+ * [5] mesh processing. */
+BMF_API bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,152 @@
+"""ctypes wrapper of the C restatement (oracle/bmf_oracle.c) -- test infrastructure only."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libbmf_oracle.so")
+_lib = None
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+
+
+def build():
+    """Compiles the restatement with its Makefile (gcc, -ffp-contract=off)."""
+    subprocess.check_call(["make", "-s", "-C", _HERE], stdout=subprocess.DEVNULL)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        vp, i64, c_int, c_float = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_float
+        L.bmfo_sin.restype = c_float
+        L.bmfo_sin.argtypes = [c_float]
+        L.bmfo_fill_field.argtypes = [c_int, vp, c_int, vp, c_float, vp]
+        L.bmfo_label_grid.restype = c_int
+        L.bmfo_label_grid.argtypes = [c_int, vp, vp]
+        L.bmfo_cell_masks.argtypes = [c_int, vp, vp]
+        L.bmfo_extract_r.restype = c_int
+        L.bmfo_extract_r.argtypes = [c_int, vp, vp, i64, i64, i64, vp, vp, vp, vp, vp, vp, vp]
+        L.bmfo_extract_q.restype = c_int
+        L.bmfo_extract_q.argtypes = [c_int, vp, vp, c_int, i64, i64, vp, vp, vp, vp, vp]
+        L.bmfo_process.argtypes = [c_int, i64, vp, vp, vp, vp, i64, vp, c_int, c_int, c_int]
+        L.bmfo_qef_f32.restype = c_float
+        L.bmfo_qef_f32.argtypes = [vp, vp, c_int, vp]
+        L.bmfo_qef_f64.restype = ctypes.c_double
+        L.bmfo_qef_f64.argtypes = [vp, vp, c_int, vp]
+        L.bmfo_extract_batch.restype = i64
+        L.bmfo_extract_batch.argtypes = [c_int, vp, c_int, vp, c_int, c_int, c_int, c_int, vp, c_int]
+        _lib = L
+    return _lib
+
+
+class Counts(ctypes.Structure):
+    _fields_ = [("n_cells", ctypes.c_int64), ("n_verts", ctypes.c_int64), ("n_idx", ctypes.c_int64)]
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def fill_field(kind, params, dim, origin=(0.0, 0.0, 0.0), scale=1.0):
+    out = np.empty(dim ** 3, np.float32)
+    prm = np.zeros(8, np.float32)
+    prm[: len(params)] = params
+    org = np.asarray(origin, np.float32)
+    lib().bmfo_fill_field(kind, _p(prm), dim, _p(org), scale, _p(out))
+    return out
+
+
+def label_grid(dim, density):
+    zc = (dim + 31) // 32
+    words = np.empty(dim * dim * zc, np.uint32)
+    cm = lib().bmfo_label_grid(dim, _p(np.ascontiguousarray(density, np.float32)), _p(words))
+    return words, int(cm)
+
+
+def cell_masks(dim, words):
+    zc = (dim + 31) // 32
+    masks = np.zeros(dim * dim * 4 * zc, np.uint64)
+    lib().bmfo_cell_masks(dim, _p(np.ascontiguousarray(words, np.uint32)), _p(masks))
+    return masks
+
+
+def extract_r(dim, density, masks, with_cells=False):
+    """Mode R: returns dict(pos, boundary, valence, idx[, cell_lin, cell_mask])."""
+    d = np.ascontiguousarray(density, np.float32)
+    c = Counts()
+    lib().bmfo_extract_r(dim, _p(d), _p(masks), 0, 0, 0, None, None, None, None, None, None, ctypes.byref(c))
+    nv, ni, nc = c.n_verts, c.n_idx, c.n_cells
+    pos = np.empty(nv * 3, np.float32)
+    bnd = np.empty(nv, np.uint8)
+    val = np.empty(nv, np.uint8)
+    idx = np.empty(ni, np.uint32)
+    cl = np.empty(nc, np.uint32) if with_cells else None
+    cm = np.empty(nc, np.uint16) if with_cells else None
+    rc = lib().bmfo_extract_r(dim, _p(d), _p(masks), nv, ni, nc if with_cells else 0, _p(pos), _p(bnd), _p(val),
+                              _p(idx), _p(cl), _p(cm), ctypes.byref(c))
+    assert rc == 0
+    out = dict(pos=pos.reshape(-1, 3), boundary=bnd, valence=val, idx=idx, n_cells=nc)
+    if with_cells:
+        out.update(cell_lin=cl, cell_mask=cm)
+    return out
+
+
+def extract_q(dim, density, words, placement=0):
+    d = np.ascontiguousarray(density, np.float32)
+    w = np.ascontiguousarray(words, np.uint32)
+    c = Counts()
+    lib().bmfo_extract_q(dim, _p(d), _p(w), placement, 0, 0, None, None, None, None, ctypes.byref(c))
+    nv, ni = c.n_verts, c.n_idx
+    pos = np.empty(nv * 3, np.float32)
+    bnd = np.empty(nv, np.uint8)
+    val = np.empty(nv, np.uint8)
+    idx = np.empty(ni, np.uint32)
+    rc = lib().bmfo_extract_q(dim, _p(d), _p(w), placement, nv, ni, _p(pos), _p(bnd), _p(val), _p(idx),
+                              ctypes.byref(c))
+    assert rc == 0
+    return dict(pos=pos.reshape(-1, 3), boundary=bnd, valence=val, idx=idx, n_cells=c.n_cells)
+
+
+def process(N, pos, boundary, valence, idx, iters, process_boundary=False, smooth_normals=False, nrm=None):
+    p = np.ascontiguousarray(pos, np.float32).reshape(-1).copy()
+    n = np.zeros_like(p) if nrm is None else np.ascontiguousarray(nrm, np.float32).reshape(-1).copy()
+    b = np.ascontiguousarray(boundary, np.uint8)
+    v = np.ascontiguousarray(valence, np.uint8)
+    ix = np.ascontiguousarray(idx, np.uint32)
+    lib().bmfo_process(N, len(b), _p(p), _p(n), _p(b), _p(v), len(ix), _p(ix), iters, int(process_boundary),
+                       int(smooth_normals))
+    return p.reshape(-1, 3), n.reshape(-1, 3)
+
+
+def qef_f32(pos, nrm):
+    pos = np.ascontiguousarray(pos, np.float32)
+    nrm = np.ascontiguousarray(nrm, np.float32)
+    out = np.zeros(3, np.float32)
+    e = lib().bmfo_qef_f32(_p(pos), _p(nrm), len(pos), _p(out))
+    return out, e
+
+
+def qef_f64(pos, nrm):
+    pos = np.ascontiguousarray(pos, np.float64)
+    nrm = np.ascontiguousarray(nrm, np.float64)
+    out = np.zeros(3, np.float64)
+    e = lib().bmfo_qef_f64(_p(pos), _p(nrm), len(pos), _p(out))
+    return out, e
+
+
+def extract_batch(desc, field, params, mode=0, placement=0, iters=0, smooth_normals=False, n_threads=0):
+    """Whole CPU path over a batch of chunks (OpenMP over chunks).  desc: (n, 5)
+    float32 rows {origin xyz, scale, dim}.  Returns (total vertices, counts (n, 3))."""
+    desc = np.ascontiguousarray(desc, np.float32)
+    prm = np.zeros(8, np.float32)
+    prm[: len(params)] = params
+    counts = np.zeros((len(desc), 3), np.int64)
+    tot = lib().bmfo_extract_batch(len(desc), _p(desc), field, _p(prm), mode, placement, iters,
+                                   int(smooth_normals), _p(counts), n_threads)
+    return int(tot), counts

@@ -1,0 +1,39 @@
+"""Host-side logic: workloads, descriptor sharding, C-ABI struct layouts (CPU only)."""
+import ctypes
+
+import numpy as np
+
+from binarymeshfitting_gb300 import _lib, workloads
+
+
+def test_lod_update_matches_spec():
+    descs, rows = workloads.lod_update()
+    assert len(descs) == 4096
+    dims, counts = np.unique(rows[:, 4], return_counts=True)
+    assert dims.tolist() == [33, 65, 129] and counts.tolist() == [2048, 1434, 614]
+    assert int((rows[:, 4] ** 3).sum()) == 1785478272
+    assert set(np.unique(rows[:, 3]).tolist()) == {1.0, 2.0, 4.0, 8.0}
+    ext = (rows[:, 4] - 1) * rows[:, 3]
+    assert np.all(rows[:, :3] >= 0) and np.all(rows[:, :3] + ext[:, None] <= workloads.WORLD)
+    assert np.all(np.mod(rows[:, :3], ext[:, None]) == 0), "origins snap to the chunk extent"
+    _, rows2 = workloads.lod_update()
+    np.testing.assert_array_equal(rows, rows2)
+
+
+def test_shard_partitions_chunks():
+    _, rows = workloads.lod_update(n=512)
+    for ws in (1, 2, 3, 8):
+        parts = [workloads.shard(rows, r, ws) for r in range(ws)]
+        allidx = np.concatenate(parts)
+        np.testing.assert_array_equal(np.sort(allidx), np.arange(len(rows)))
+        w = [(rows[p, 4] ** 3).sum() for p in parts]
+        assert max(w) <= (rows[:, 4] ** 3).sum() / ws + 129 ** 3
+
+
+def test_struct_layouts_match_header():
+    # include/bmf.h: bmf_chunk_desc is 24 bytes, bmf_field 36, bmf_mesh 80, bmf_batch_out 72
+    assert ctypes.sizeof(_lib.ChunkDesc) == 24
+    assert ctypes.sizeof(_lib.Field) == 36
+    assert ctypes.sizeof(_lib.ExtractOpts) == 24
+    assert ctypes.sizeof(_lib.Mesh) == 80
+    assert ctypes.sizeof(_lib.BatchOut) == 72
