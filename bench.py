@@ -1,0 +1,351 @@
+"""Benchmark of the chunk-extraction hot path on one GB300 (or N, one process each).
+
+One step = one batched WorldOctree-style update: 4096 chunks of the FBM terrain
+field y - 64 - 40 FBM(p) at mixed LOD (2048 x 33^3, 1434 x 65^3, 614 x 129^3
+samples, cell size 1/2/4/8), each chunk going through density filling ->
+occupancy words -> cell masks -> compaction + emission (reference Marching-Cubes
+topology by default) -> 4 MeshProcessor iterations with smoothed normals,
+replayed as one captured CUDA graph.  Inputs are seeded synthetic chunk
+descriptors; every step writes 7.1 GB of density, far more than the 129 MB L2.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU implementation of the same path (the oracle
+restatement of the reference's DMCChunk / MeshProcessor code, OpenMP over
+chunks like ChunkGenerator::extract_chunk) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "chunks/s (mixed-LOD batch vs per-chunk, same GB300, exact topology)"
+FP32_OPS_PER_SAMPLE = 337  # terrain FBM, 5 octaves, counted from the kernel source
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--mode", default="R", choices=["R", "Q"])
+    p.add_argument("--placement", type=int, default=1)
+    p.add_argument("--iters", type=int, default=4)
+    p.add_argument("--no-normals", action="store_true")
+    p.add_argument("--chunks", type=int, default=4096)
+    p.add_argument("--cpu-sample", type=int, default=128, help="chunks per CPU sample")
+    p.add_argument("--skip-per-chunk", action="store_true")
+    p.add_argument("--skip-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(5)
+        self.t.join(2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), d.get("sm_max_mhz", 2070.0), "measured"
+    return 6800.0, 2070.0, "fallback"
+
+
+def cpu_sample_rows(rows, n, seed):
+    """A bounded, tier-stratified random sample of an update's chunks."""
+    rng = np.random.default_rng(seed)
+    pick = []
+    for dim in np.unique(rows[:, 4]):
+        idx = np.flatnonzero(rows[:, 4] == dim)
+        k = max(1, int(round(n * len(idx) / len(rows))))
+        pick.append(rng.choice(idx, size=min(k, len(idx)), replace=False))
+    return np.sort(np.concatenate(pick))
+
+
+def cpu_run(rows, args, threads):
+    from binarymeshfitting_gb300 import workloads
+    from oracle import cpu
+    mode = 0 if args.mode == "R" else 1
+    t0 = time.perf_counter()
+    tot, counts = cpu.extract_batch(rows[:, :5].astype(np.float32), 2, list(workloads.TERRAIN_PARAMS), mode,
+                                    args.placement, args.iters, not args.no_normals, n_threads=threads)
+    return time.perf_counter() - t0, tot
+
+
+def run_reference(args):
+    """CPU implementation of the path (the oracle port), all host threads."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from binarymeshfitting_gb300 import workloads
+    from oracle import cpu
+    cpu.build()
+    threads = os.cpu_count() or 1
+    _, rows = workloads.lod_update(n=args.chunks)
+    for w in range(args.warmup):
+        cpu_run(rows[cpu_sample_rows(rows, args.cpu_sample, 100 + w)], args, threads)
+    times, chunks = [], 0
+    for k in range(args.steps):
+        sub = rows[cpu_sample_rows(rows, args.cpu_sample, 1000 + k)]
+        t, _ = cpu_run(sub, args, threads)
+        times.append(t)
+        chunks += len(sub)
+    total = sum(times)
+    value = chunks / total
+    sample = "%d steps x ~%d tier-stratified chunks of the %d-chunk update" % (args.steps, args.cpu_sample,
+                                                                                 args.chunks)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "chunks/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config(args),
+            "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "chunks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config(args):
+    return {"workload": "lod_update_%d" % args.chunks,
+            "chunks": args.chunks, "chunk_samples": "2048x33^3 + 1434x65^3 + 614x129^3",
+            "field": "terrain y-64-40*FBM(p), 5 octaves perlin, freq 0.01, lacunarity 2, gain 0.5, seed 1337",
+            "topology": "mode R (reference Marching-Cubes triangles)" if args.mode == "R" else
+            "mode Q (DMC quads, placement %d)" % args.placement,
+            "smoothing_iters": args.iters, "smoothed_normals": not args.no_normals,
+            "l2": "inputs larger than L2: 7.1 GB density written per step", "parallelism": "replicas" if
+            args.gpus == 1 else "weak: one independent update per GPU"}
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    from binarymeshfitting_gb300 import _lib as L
+    from binarymeshfitting_gb300 import workloads
+    from binarymeshfitting_gb300.engine import Batch, Context
+
+    world, rank, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = Context(local)
+    mode = L.MODE_R if args.mode == "R" else L.MODE_Q
+    normals = not args.no_normals
+    descs, rows = workloads.lod_update(n=args.chunks, seed=2024 + rank)
+    field = workloads.terrain_field()
+    b = Batch(ctx, descs, field, mode=mode, placement=args.placement, iters=args.iters, smooth_normals=normals)
+    # size the output arena from one sizing pass (counts are exact), then keep it
+    vcap, icap = 40_000_000, 240_000_000
+    for _ in range(3):
+        b.allocate(vcap, icap, normals=normals)
+        try:
+            nv, ni = b.run(use_graph=False, sync=True)
+            break
+        except L.BmfError as e:
+            if e.status != L.ERR_CAPACITY:
+                raise
+            vcap, icap = int(b.out.n_verts * 1.05) + 1024, int(b.out.n_idx * 1.05) + 1024
+    bufs = b.allocate(nv + 1024, ni + 1024, normals=normals)
+    stream = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 1)):
+        nv, ni = b.run(use_graph=True, sync=True)
+    # ---- timed region: K graph replays ----
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = ctx.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.run(use_graph=True, sync=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    if world > 1:
+        dist.barrier()
+    ms_t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = args.chunks * world / (ms / 1000.0)
+    nv, ni = b.run(use_graph=True, sync=True)
+
+    # ---- per-stage profile (outside the timed region) ----
+    stages = [b.profile() for _ in range(3)]
+    st_ms = [statistics.median(s[k] for s in stages) for k in range(6)]
+    samples = int((rows[:, 4] ** 3).sum())
+    words = int((rows[:, 4] ** 2 * np.ceil(rows[:, 4] / 32)).sum())
+    hbm_peak, sm_max, peak_kind = measured_peaks()
+    clock_mhz = clk["sm_mhz"] or sm_max
+    fp32_peak = 152 * 128 * sm_max * 1e6 / 1e12  # nominal FP32 instruction rate at max clock, Tops/s
+    fill_achieved = FP32_OPS_PER_SAMPLE * samples / (st_ms[0] / 1000.0) / 1e12
+    # algorithmic HBM bytes of the extraction kernels (count + scan + offsets + emit)
+    per_vertex = 12 + 1 + 1 + 8 + (12 if normals else 0)
+    ext_bytes = words * (4 + 8 + 8 + 4) + nv * per_vertex + ni * 4
+    ext_ms = st_ms[1] + st_ms[2] + st_ms[3] + st_ms[4]
+    ext_gbs = ext_bytes / (ext_ms / 1000.0) / 1e9
+    roofline = {"kernel": "k_sample_label (density FBM + occupancy words)", "bound": "fp32",
+                "achieved": fill_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fill_achieved / fp32_peak,
+                "peak_kind": "nominal 152 SM x 128 FP32 lanes x %.0f MHz (no measured FP32 peak exists)" % sm_max,
+                "traffic": None, "ms_per_launch": st_ms[0],
+                "flops_per_launch": FP32_OPS_PER_SAMPLE * samples,
+                "extraction_hbm": {"kernels": "count+scan+offsets+emit", "achieved": ext_gbs, "peak": hbm_peak,
+                                   "unit": "GB/s", "frac": ext_gbs / hbm_peak, "bytes": ext_bytes,
+                                   "ms": ext_ms, "peak_kind": peak_kind},
+                "stage_ms": {"fill_label": st_ms[0], "count": st_ms[1], "scan": st_ms[2], "offsets": st_ms[3],
+                             "emit": st_ms[4], "process": st_ms[5]}}
+
+    # ---- end to end through the public API with host buffers ----
+    h_desc_list = descs
+    vbytes = nv * 12
+    ibytes = ni * 4
+    h_pos = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True)
+    h_idx = torch.empty(ni, dtype=torch.int32, pin_memory=True)
+    h_info = torch.empty((args.chunks, 6), dtype=torch.int64, pin_memory=True)
+    h2d = args.chunks * 56
+    d2h = vbytes + ibytes + args.chunks * 48
+    for _ in range(2):
+        b.set_descs(h_desc_list)
+        b.run(use_graph=True, sync=False)
+        h_pos.copy_(bufs["pos"][:nv], non_blocking=True)
+        h_idx.copy_(bufs["idx"][:ni], non_blocking=True)
+        h_info.copy_(bufs["info"], non_blocking=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.set_descs(h_desc_list)
+        b.run(use_graph=True, sync=False)
+        h_pos.copy_(bufs["pos"][:nv], non_blocking=True)
+        h_idx.copy_(bufs["idx"][:ni], non_blocking=True)
+        h_info.copy_(bufs["info"], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1000.0) / args.steps
+    e2e = {"value": args.chunks * world / (e2e_ms / 1000.0), "unit": "chunks/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}
+
+    # ---- the plain per-chunk path (the drop-in), same chunks ----
+    per_chunk = None
+    if not args.skip_per_chunk and rank == 0:
+        for dsc in descs[:16]:
+            ctx.extract_chunk(dsc, field, mode=mode, placement=args.placement, iters=args.iters,
+                              smooth_normals=normals)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pv = 0
+        for dsc in descs:
+            m = ctx.extract_chunk(dsc, field, mode=mode, placement=args.placement, iters=args.iters,
+                                  smooth_normals=normals)
+            pv += m.n_verts
+        torch.cuda.synchronize()
+        pc_s = time.perf_counter() - t0
+        per_chunk = {"value": args.chunks / pc_s, "unit": "chunks/s", "launches": "one bmf_extract_chunk per chunk",
+                     "vertices_match_batch": pv == nv, "batch_speedup": (args.chunks / (ms / 1000.0)) /
+                     (args.chunks / pc_s)}
+
+    # ---- CPU baseline (rank 0): bounded sample of the same update, all host threads ----
+    cpu_baseline = None
+    if not args.skip_cpu and rank == 0:
+        from oracle import cpu
+        cpu.build()
+        threads = os.cpu_count() or 1
+        sub = rows[cpu_sample_rows(rows, args.cpu_sample, 7)]
+        cpu_run(sub[:8], args, threads)
+        t, _ = cpu_run(sub, args, threads)
+        cpu_baseline = {"value": len(sub) / t, "unit": "chunks/s", "cores": threads, "kind": "port",
+                        "sample": "%d tier-stratified chunks of the %d-chunk update, OpenMP over chunks" %
+                                  (len(sub), args.chunks)}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "chunks/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(args),
+                "samples_per_s": samples * world / (ms / 1000.0),
+                "vertices_per_s": nv * world / (ms / 1000.0), "vertices_per_step": nv, "indices_per_step": ni,
+                "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e, "per_chunk": per_chunk,
+                "gpu_launches": launches, "clocks": clk, "bwd_fwd": None}
+        print(json.dumps(line), flush=True)
+    b.close()
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -15,7 +15,7 @@ namespace {
 
 enum Slot {
   S_CHUNKS, S_UNITS, S_FLAGS, S_TOT, S_INFO, S_TOTALS, S_WORDS, S_DENS, S_VCNT, S_ICNT, S_GPL,
-  S_OFF, S_CURSOR, S_ADJ, S_DUALP, S_DUALN, S_SCANTMP, S_NUM
+  S_OFF, S_CURSOR, S_ADJ, S_DUALP, S_DUALN, S_SCANTMP, S_VKEY, S_NUM
 };
 
 constexpr int kMaxDim = 512;
@@ -55,6 +55,7 @@ struct bmf_batch {
   uint32_t* d_idxg = nullptr;
   uint8_t* d_valence = nullptr;
   uint8_t* d_boundary = nullptr;
+  uint32_t* d_vkey = nullptr;
   // captured graph and the output it was captured for
   cudaGraphExec_t exec = nullptr;
   bmf_batch_out graph_out{};
@@ -165,14 +166,15 @@ bmf_status upload_single(bmf_ctx* ctx, const ChunkDev& c, cudaStream_t st, Chunk
 bmf_status extract_core(bmf_ctx* ctx, int mode, int placement, ChunkDev* d_chunks, int n_chunks, const int* d_units,
                         int n_units, const uint32_t* d_words, const float* d_dens, const uint32_t* d_flags,
                         int64_t words_total, const MeshOut& mo, int64_t* d_info, int64_t* d_totals,
-                        cudaStream_t st) {
+                        cudaStream_t st, WordScratch* ws_out = nullptr) {
   WordScratch ws{};
   uint32_t* tot = nullptr;
   bmf_status s;
   if ((s = scratch(ctx, S_VCNT, (size_t)words_total, &ws.vcnt)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_ICNT, (size_t)words_total, &ws.icnt)) != BMF_OK) return s;
-  if (mode == BMF_MODE_Q && (s = scratch(ctx, S_GPL, (size_t)words_total * 3, &ws.gpl)) != BMF_OK) return s;
+  if ((s = scratch(ctx, S_GPL, (size_t)words_total * 3, &ws.gpl)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_TOT, (size_t)n_chunks * 2, &tot)) != BMF_OK) return s;
+  if (ws_out) *ws_out = ws;
   launch_count(mode, d_chunks, n_chunks, d_units, n_units, d_words, d_flags, ws, st);
   BMF_LAUNCHED(ctx, 1);
   launch_scan_chunks(d_chunks, n_chunks, ws, tot, st);
@@ -190,7 +192,8 @@ bmf_status mesh_valid(bmf_ctx* ctx, const bmf_mesh* m) {
   return BMF_OK;
 }
 
-bmf_status process_mesh(bmf_ctx* ctx, bmf_mesh* mesh, int iters, int pb, int sn, cudaStream_t st) {
+bmf_status process_mesh(bmf_ctx* ctx, bmf_mesh* mesh, int iters, int pb, int sn, cudaStream_t st,
+                        const StructuredAdj* sa = nullptr) {
   const int N = mesh->prim_size;
   if (N != 3 && N != 4) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "prim_size must be 3 or 4");
   if (!mesh->d_valence || !mesh->d_boundary)
@@ -206,9 +209,9 @@ bmf_status process_mesh(bmf_ctx* ctx, bmf_mesh* mesh, int iters, int pb, int sn,
   if ((s = scratch(ctx, S_DUALP, (size_t)n_prims * 3, &ps.dual_p)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_DUALN, (size_t)n_prims * 3, &ps.dual_n)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_SCANTMP, (size_t)(nv / 4096 + 2), &ps.tmp)) != BMF_OK) return s;
-  launch_process(N, nv, n_prims, nullptr, mesh->d_pos, mesh->d_nrm, mesh->d_boundary, mesh->d_valence, mesh->d_idx,
-                 iters, pb, sn, ps, st);
-  BMF_LAUNCHED(ctx, 4 + 2 * iters);
+  const int k = launch_process(N, nv, n_prims, nullptr, mesh->d_pos, mesh->d_nrm, mesh->d_boundary,
+                               mesh->d_valence, mesh->d_idx, iters, pb, sn, ps, sa, st);
+  BMF_LAUNCHED(ctx, k);
   return BMF_OK;
 }
 
@@ -401,8 +404,10 @@ bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf
   launch_sample_label(d_c, 1, d_u, dim, dim, fd, nullptr, d_dens, d_words, d_flags, st);
   BMF_LAUNCHED(ctx, 1);
   MeshOut mo{out->d_pos, out->d_nrm, out->d_boundary, out->d_valence, out->d_idx, nullptr, out->vcap, out->icap};
+  if (opts->iters > 0 && (s = scratch(ctx, S_VKEY, (size_t)out->vcap + 1, &mo.vkey)) != BMF_OK) return s;
+  WordScratch ws{};
   if ((s = extract_core(ctx, opts->mode, opts->placement, d_c, 1, d_u, dim, d_words, d_dens, d_flags,
-                        (int64_t)dim * dim * c.zc, mo, nullptr, d_totals, st)) != BMF_OK)
+                        (int64_t)dim * dim * c.zc, mo, nullptr, d_totals, st, &ws)) != BMF_OK)
     return s;
   BMF_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, d_totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   BMF_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned + 2, d_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -416,7 +421,8 @@ bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf
     return fail(ctx, BMF_ERR_CAPACITY, "bmf_extract_chunk: output capacity exceeded (needed counts reported)");
   // ChunkGenerator.cpp:112: processing only when the chunk has a mesh
   if (opts->iters > 0 && out->contains_mesh && out->n_verts && out->n_idx) {
-    if ((s = process_mesh(ctx, out, opts->iters, opts->process_boundary, opts->smooth_normals, st)) != BMF_OK)
+    const StructuredAdj sa{opts->mode, d_c, 1, d_words, ws, mo.vkey};
+    if ((s = process_mesh(ctx, out, opts->iters, opts->process_boundary, opts->smooth_normals, st, &sa)) != BMF_OK)
       return s;
     BMF_CUDA(ctx, cudaStreamSynchronize(st));
   }
@@ -476,9 +482,7 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
   if ((s = bail(cudaMalloc(&b->d_words, sizeof(uint32_t) * words), "words")) != BMF_OK) return s;
   if ((s = bail(cudaMalloc(&b->ws.vcnt, sizeof(uint32_t) * words), "vcnt")) != BMF_OK) return s;
   if ((s = bail(cudaMalloc(&b->ws.icnt, sizeof(uint32_t) * words), "icnt")) != BMF_OK) return s;
-  if (opts->mode == BMF_MODE_Q &&
-      (s = bail(cudaMalloc(&b->ws.gpl, sizeof(uint32_t) * 3 * words), "gpl")) != BMF_OK)
-    return s;
+  if ((s = bail(cudaMalloc(&b->ws.gpl, sizeof(uint32_t) * 3 * words), "gpl")) != BMF_OK) return s;
   if ((s = bail(cudaMallocHost(&b->h_pinned, sizeof(int64_t) * 4), "pinned")) != BMF_OK) return s;
   if ((s = bail(cudaMemcpy(b->d_chunks, b->h_chunks.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice),
                 "upload chunks")) != BMF_OK)
@@ -498,7 +502,7 @@ bmf_status batch_proc_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
   const int64_t np = icap / N;
   void* ptrs[] = {b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p, b->ps.dual_n, b->ps.tmp,
-                  b->d_idxg, b->d_valence, b->d_boundary};
+                  b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   b->proc_vcap = b->proc_icap = 0;
@@ -511,6 +515,7 @@ bmf_status batch_proc_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   BMF_CUDA(ctx, cudaMalloc(&b->d_idxg, sizeof(uint32_t) * (icap + 1)));
   BMF_CUDA(ctx, cudaMalloc(&b->d_valence, vcap + 1));
   BMF_CUDA(ctx, cudaMalloc(&b->d_boundary, vcap + 1));
+  BMF_CUDA(ctx, cudaMalloc(&b->d_vkey, sizeof(uint32_t) * (vcap + 1)));
   b->proc_vcap = vcap;
   b->proc_icap = icap;
   return BMF_OK;
@@ -528,15 +533,16 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
-             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap};
+             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, proc ? b->d_vkey : nullptr};
   launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_dens,
               b->d_flags, b->ws, mo, st);
   int64_t k = 5;
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
-    launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary, b->d_valence,
-                   b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals, b->ps, st);
-    k += 6 + 2 * b->opts.iters;
+    const StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
+    k += launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary,
+                        b->d_valence, b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals,
+                        b->ps, &sa, st);
     if (out->d_boundary)
       BMF_CUDA(ctx, cudaMemcpyAsync(out->d_boundary, b->d_boundary, (size_t)out->vcap, cudaMemcpyDeviceToDevice, st));
   }
@@ -651,21 +657,24 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
                        b->d_totals, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[4], st));
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
-             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap};
+             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, proc ? b->d_vkey : nullptr};
   launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_dens,
               b->d_flags, b->ws, mo, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[5], st));
+  int pk = 0;
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
-    launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary, b->d_valence,
-                   b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals, b->ps, st);
+    const StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
+    pk = launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary,
+                        b->d_valence, b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals,
+                        b->ps, &sa, st);
   }
   BMF_CUDA(ctx, cudaEventRecord(ev[6], st));
   BMF_CUDA(ctx, cudaEventSynchronize(ev[6]));
   BMF_CUDA(ctx, cudaPeekAtLastError());
   for (int k = 0; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
-  ctx->launches += 5 + (proc ? 6 + 2 * b->opts.iters : 0);
+  ctx->launches += 5 + pk;
   return BMF_OK;
 }
 
@@ -674,7 +683,7 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
                   b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
-                  b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary};
+                  b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);

@@ -65,6 +65,25 @@ struct LineWords {
   }
 };
 
+constexpr int kWordBlock = 256;  // threads per CTA of the count / emit kernels
+
+// A word is quiet when its 32 cells can neither own a crossing nor have a
+// mixed corner mask: the four line words around it are identical, so are the
+// four next-block words, and the line has no z-crossing.  Then X = Y = Z = 0
+// and every cell with all corners inside the chunk has mask 0 or 255, so the
+// word contributes no vertex, triangle or quad in either mode.
+__device__ __forceinline__ bool word_is_quiet(const uint32_t* W, int dim, int zc, int x, int y, int zb) {
+  const uint32_t w = word_at(W, dim, zc, x, y, zb);
+  if (word_at(W, dim, zc, x, y + 1, zb) != w || word_at(W, dim, zc, x + 1, y, zb) != w ||
+      word_at(W, dim, zc, x + 1, y + 1, zb) != w)
+    return false;
+  const uint32_t n = word_at(W, dim, zc, x, y, zb + 1);
+  if (word_at(W, dim, zc, x, y + 1, zb + 1) != n || word_at(W, dim, zc, x + 1, y, zb + 1) != n ||
+      word_at(W, dim, zc, x + 1, y + 1, zb + 1) != n)
+    return false;
+  return zcross_word(W, dim, zc, x, y, zb) == 0u;
+}
+
 // Interior-edge test of Mode Q: the grid edge from sample s along axis a has
 // all four surrounding cells.
 __device__ __forceinline__ bool q_edge_interior(int dim, int sx, int sy, int sz, int a) {
@@ -104,17 +123,31 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t* W = words + ch.words;
   const bool cm = contains_mesh(__ldg(flags + c));
-  for (int wi = warp; wi < nw; wi += nwarps) {
-    const int y = wi / zc, zb = wi - y * zc;
-    const int64_t o = ch.words + (int64_t)x * nw + wi;
-    if (!cm) {
-      if (lane == 0) {
+  __shared__ int s_busy[kWordBlock];
+  __shared__ int s_nbusy;
+  for (int base = 0; base < nw; base += kWordBlock) {
+    // level 1: one thread per word; quiet words get zero counts right away
+    if (threadIdx.x == 0) s_nbusy = 0;
+    __syncthreads();
+    if (base + (int)threadIdx.x < nw) {
+      const int wi = base + threadIdx.x;
+      const int y = wi / zc, zb = wi - y * zc;
+      if (cm && !word_is_quiet(W, dim, zc, x, y, zb)) {
+        s_busy[atomicAdd(&s_nbusy, 1)] = wi;
+      } else {
+        const int64_t o = ch.words + (int64_t)x * nw + wi;
         ws.vcnt[o] = 0u;
         ws.icnt[o] = 0u;
-        if (MODE == 1) { ws.gpl[3 * o] = 0u; ws.gpl[3 * o + 1] = 0u; ws.gpl[3 * o + 2] = 0u; }
+        if (ws.gpl) { ws.gpl[3 * o] = 0u; ws.gpl[3 * o + 1] = 0u; ws.gpl[3 * o + 2] = 0u; }
       }
-      continue;
     }
+    __syncthreads();
+    // level 2: one warp per busy word, one lane per cell
+    const int nbusy = s_nbusy;
+    for (int li = warp; li < nbusy; li += nwarps) {
+    const int wi = s_busy[li];
+    const int y = wi / zc, zb = wi - y * zc;
+    const int64_t o = ch.words + (int64_t)x * nw + wi;
     const int z = 32 * zb + lane;
     LineWords lw;
     lw.load(W, dim, zc, x, y, zb);
@@ -125,7 +158,13 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
       const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
       vc = __popc(X) + __popc(Y) + __popc(Z);
       const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
-      int t = interior ? 3 * tri_count(lw.mask(lane)) : 0;
+      const int nt = interior ? tri_count(lw.mask(lane)) : 0;
+      int t = 3 * nt;
+      // bit-planes of the per-cell triangle count (0..5): a cell's first
+      // primitive is ibase + 3 * (popc(p0 & lt) + 2 popc(p1 & lt) + 4 popc(p2 & lt))
+      const uint32_t p0 = __ballot_sync(kFull, nt & 1), p1 = __ballot_sync(kFull, nt & 2),
+                     p2 = __ballot_sync(kFull, nt & 4);
+      if (lane == 0 && ws.gpl) { ws.gpl[3 * o] = p0; ws.gpl[3 * o + 1] = p1; ws.gpl[3 * o + 2] = p2; }
       t += __shfl_xor_sync(kFull, t, 16);
       t += __shfl_xor_sync(kFull, t, 8);
       t += __shfl_xor_sync(kFull, t, 4);
@@ -147,6 +186,8 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
       ws.vcnt[o] = vc;
       ws.icnt[o] = ic;
     }
+    }
+    __syncthreads();
   }
 }
 
@@ -522,7 +563,22 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
   const uint32_t* ibase = ws.icnt + ch.words;
   const float* D = dens + ch.dens;
   const uint32_t lt = lane_lt(lane);
-  for (int wi = warp; wi < nw; wi += nwarps) {
+  __shared__ int s_busy[kWordBlock];
+  __shared__ int s_nbusy;
+  for (int base = 0; base < nw; base += kWordBlock) {
+    // level 1: one thread per word; quiet words emit nothing
+    if (threadIdx.x == 0) s_nbusy = 0;
+    __syncthreads();
+    if (base + (int)threadIdx.x < nw) {
+      const int wi = base + threadIdx.x;
+      const int y = wi / zc, zb = wi - y * zc;
+      if (!word_is_quiet(W, dim, zc, x, y, zb)) s_busy[atomicAdd(&s_nbusy, 1)] = wi;
+    }
+    __syncthreads();
+    // level 2: one warp per busy word, one lane per cell
+    const int nbusy = s_nbusy;
+    for (int li = warp; li < nbusy; li += nwarps) {
+    const int wi = s_busy[li];
     const int y = wi / zc, zb = wi - y * zc;
     const int z = 32 * zb + lane;
     const int64_t wo = (int64_t)x * nw + wi;
@@ -556,6 +612,7 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
             out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
                                 x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
           if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
+          if (out.vkey) out.vkey[gv] = ((uint32_t)(((int64_t)x * dim + y) * dim + z) << 2) | (uint32_t)a;
           if (out.valence) {
             // init_valence: uses of this edge by the (up to) four interior
             // cells around it (polygonize skips far-face cells, DMCChunk.cpp:528).
@@ -586,7 +643,10 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
         const int e = tri_edge(tw, i);
         const uint32_t vid = r_vertex_id(W, vbase, dim, zc, x + c_edge_owner[e][0], y + c_edge_owner[e][1],
                                          z + c_edge_owner[e][2], c_edge_owner[e][3]);
-        if (gi < out.icap) out.idx[gi] = vid;
+        if (gi < out.icap) {
+          out.idx[gi] = vid;
+          if (out.idx_global) out.idx_global[gi] = (uint32_t)(ch.vout + vid);
+        }
       }
     } else {
       // ---- Mode Q vertices: one per vertex group of each interior surface cell ----
@@ -609,6 +669,7 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
           out.pos[3 * gv + 2] = P[2];
           if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
           if (out.boundary) out.boundary[gv] = bnd;
+          if (out.vkey) out.vkey[gv] = ((uint32_t)(((int64_t)x * dim + y) * dim + z) << 2) | (uint32_t)g;
           if (out.valence) {
             int val = 0;
             for (int e = 0; e < 12; ++e) {
@@ -659,7 +720,110 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
           }
       }
     }
+    }
+    __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// K5: vertex -> primitive adjacency (the CSR of MeshProcessor::init /
+// init_primitives, MeshProcessor.cpp:26-128), built per vertex from the grid
+// structure instead of by scattering primitives: a Mode R vertex on the axis-a
+// edge of sample s is used by the (up to) four interior cells around that
+// edge, whose primitive ids are ascending in linear cell order and, inside a
+// cell, in triangle-list order -- exactly the ascending-prim order
+// init_primitives produces.  A Mode Q vertex is used by one quad per interior
+// crossing edge of its group; those quad ids are sorted.  No atomics, no sort
+// pass, deterministic.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_chunk_by_vertex(const ChunkDev* __restrict__ chunks, int n, int64_t v) {
+  int lo = 0, hi = n - 1;  // last chunk whose vout <= v (empty chunks share the next one's offset)
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (chunks[mid].vout <= v) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ chunks, int n_chunks,
+                                                   const uint32_t* __restrict__ words, WordScratch ws,
+                                                   const uint32_t* __restrict__ vkey, const uint32_t* __restrict__ off,
+                                                   const int64_t* __restrict__ d_counts, int64_t vcap,
+                                                   uint32_t* __restrict__ adj) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
+  const int c = find_chunk_by_vertex(chunks, n_chunks, v);
+  const ChunkDev ch = chunks[c];
+  const int dim = ch.dim, zc = ch.zc;
+  const uint32_t* W = words + ch.words;
+  const uint32_t* vbase = ws.vcnt + ch.words;
+  const uint32_t* ibase = ws.icnt + ch.words;
+  const uint32_t* pl = ws.gpl + 3 * ch.words;
+  const uint32_t key = vkey[v];
+  const int lin = (int)(key >> 2), k = (int)(key & 3u);
+  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+  uint32_t* out = adj + off[v];
+  // the vertex's CSR range (the exclusive scan of init_valence): never write past it
+  const int room = (int)(off[v + 1] - off[v]);
+  int n = 0;
+  if (MODE == 0) {
+    const int a = k;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {  // cells around the edge, ascending linear order
+      const int d1 = (q >> 1) ^ 1, d2 = (q & 1) ^ 1;
+      int cx = x, cy = y, cz = z, e;
+      if (a == 0) { cy -= d1; cz -= d2; e = 2 * d1 + d2; }
+      else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
+      else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
+      if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
+      const int m = cell_mask_at(W, dim, zc, cx, cy, cz);
+      if (!edge_uses(m, e)) continue;
+      const uint64_t tw = c_tri_cases[m];
+      const int nt = (int)(tw >> 60);
+      const int64_t wi = ((int64_t)cx * dim + cy) * zc + (cz >> 5);
+      const uint32_t lt = lane_lt(cz & 31);
+      const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
+                           4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
+      const int64_t first = (ch.iout + (int64_t)__ldg(ibase + wi)) / 3 + pre;
+      for (int t = 0; t < nt; ++t)
+        if ((tri_edge(tw, 3 * t) == e || tri_edge(tw, 3 * t + 1) == e || tri_edge(tw, 3 * t + 2) == e) && n < room)
+          out[n++] = (uint32_t)(first + t);
+    }
+  } else {
+    const int g = k;
+    const int m = cell_mask_at(W, dim, zc, x, y, z);
+    uint32_t ids[12];
+    for (int e = 0; e < 12; ++e) {
+      if (group_of(m, e) != g) continue;
+      const int c0 = edge_c0(e), a = e >> 2;
+      const int sx = x + ((c0 >> 2) & 1), sy = y + ((c0 >> 1) & 1), sz = z + (c0 & 1);
+      if (!q_edge_interior(dim, sx, sy, sz, a)) continue;
+      uint32_t Xi, Yi, Zi;
+      q_quad_words(W, dim, zc, sx, sy, sz >> 5, Xi, Yi, Zi);
+      const int l = sz & 31;
+      const uint32_t lt = lane_lt(l);
+      uint32_t pre = __popc(Xi & lt) + __popc(Yi & lt) + __popc(Zi & lt);
+      if (a >= 1) pre += (Xi >> l) & 1u;
+      if (a >= 2) pre += (Yi >> l) & 1u;
+      const int64_t wi = ((int64_t)sx * dim + sy) * zc + (sz >> 5);
+      uint32_t id = (uint32_t)((ch.iout + (int64_t)__ldg(ibase + wi)) / 4 + pre);
+      int j = n++;  // insertion into the sorted prefix
+      while (j > 0 && ids[j - 1] > id) { ids[j] = ids[j - 1]; --j; }
+      ids[j] = id;
+    }
+    for (int i = 0; i < n && i < room; ++i) out[i] = ids[i];
+  }
+  (void)vbase;
+}
+
+void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
+                      const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,
+                      uint32_t* adj, cudaStream_t st) {
+  const int blocks = (int)((vcap + 255) / 256);
+  if (blocks == 0) return;
+  if (mode == 0) k_adj_build<0><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
+  else k_adj_build<1><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
 }
 
 void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,

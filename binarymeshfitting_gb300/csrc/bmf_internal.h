@@ -18,6 +18,10 @@ struct MeshOut {
   uint32_t* idx;          // chunk-local vertex ids (one VerticesIndicesBlock per chunk)
   uint32_t* idx_global;   // optional: the same indices offset by the chunk's vertex base
   int64_t vcap, icap;
+  // optional: where each vertex came from, (chunk-local linear sample index << 2) | k,
+  // k = crossing axis (Mode R) or vertex group (Mode Q); the key the analytic
+  // adjacency build starts from.
+  uint32_t* vkey = nullptr;
 };
 
 // Per-word scratch of the extraction kernels, indexed like the occupancy
@@ -63,9 +67,25 @@ struct ProcessScratch {
 // sequence can be captured in a CUDA graph before the counts are known).
 // Scratch sizes: off nv+1, cursor nv, adj N*n_prims, dual_p/dual_n 3*n_prims,
 // tmp ceil(nv / 4096) + 1.
-void launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
-                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
-                    int process_boundary, int smooth_normals, ProcessScratch s, cudaStream_t st);
+// Where the vertex->primitive lists come from: a mesh this library extracted
+// (grid structure known: built analytically per vertex) or any mesh (atomic
+// scatter + per-vertex sort).
+struct StructuredAdj {
+  int mode;                  // BMF_MODE_R / BMF_MODE_Q
+  const ChunkDev* chunks;    // with vout / iout set
+  int n_chunks;
+  const uint32_t* words;
+  WordScratch ws;            // scanned counts + per-word bit-planes
+  const uint32_t* vkey;      // per-vertex keys written by the emit kernel
+};
+void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
+                      const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,
+                      uint32_t* adj, cudaStream_t st);
+// Returns the number of kernels launched.
+int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
+                   const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
+                   int process_boundary, int smooth_normals, ProcessScratch s, const StructuredAdj* sa,
+                   cudaStream_t st);
 void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n, const int64_t* d_n,
                                      uint32_t* block_tmp, cudaStream_t st);
 

@@ -98,25 +98,28 @@ void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n
 }
 
 // set_adj (MeshRecursion.hpp:173-190): adj[off[v] + k] = prim.
-__global__ void k_fill_adj(int N, int64_t n_slots, const int64_t* __restrict__ d_counts,
+__global__ void k_fill_adj(int N, int64_t n_slots, int64_t nv, const int64_t* __restrict__ d_counts,
                            const uint32_t* __restrict__ idx, const uint32_t* __restrict__ off,
                            const uint8_t* __restrict__ valence, uint32_t* __restrict__ cursor,
                            uint32_t* __restrict__ adj) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= (d_counts ? min(n_slots, d_counts[1] / N * N) : n_slots)) return;
   const uint32_t v = idx[j];
+  if ((int64_t)v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;  // an index outside the mesh is ignored
   const uint32_t k = atomicAdd(cursor + v, 1u);
-  if (k < valence[v]) adj[off[v] + k] = (uint32_t)(j / N);
+  // a caller's valence may not sum to more than the index slots: stay inside adj
+  if (k < valence[v] && (int64_t)off[v] + k < n_slots) adj[off[v] + k] = (uint32_t)(j / N);
 }
 
 // Restores ascending prim order in each vertex's list (insertion sort; the
 // lists hold at most a few dozen entries).
-__global__ void k_sort_adj(int64_t nv, const int64_t* __restrict__ d_counts, const uint32_t* __restrict__ off,
-                           const uint32_t* __restrict__ cursor, const uint8_t* __restrict__ valence,
-                           uint32_t* __restrict__ adj) {
+__global__ void k_sort_adj(int64_t nv, int64_t adj_cap, const int64_t* __restrict__ d_counts,
+                           const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
+                           const uint8_t* __restrict__ valence, uint32_t* __restrict__ adj) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
-  const uint32_t n = min(cursor[v], (uint32_t)valence[v]);
+  const int64_t room = adj_cap - (int64_t)off[v];
+  const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)min(cursor[v], (uint32_t)valence[v]), room));
   uint32_t* a = adj + off[v];
   for (uint32_t i = 1; i < n; ++i) {
     const uint32_t key = a[i];
@@ -145,14 +148,18 @@ __device__ __forceinline__ void cross3(const float a[3], const float b[3], float
 // optimize_dual_grid body (MeshProcessor.cpp:142-227).  normal_mode: 0 none,
 // 1 face normal, 2 sum of vertex normals.
 template <int N>
-__global__ void k_dual(int64_t n_prims, const int64_t* __restrict__ d_counts, const uint32_t* __restrict__ idx,
-                       const float* __restrict__ pos, const float* __restrict__ nrm, float* __restrict__ dual_p,
-                       float* __restrict__ dual_n, int normal_mode) {
+__global__ void k_dual(int64_t n_prims, int64_t nv, const int64_t* __restrict__ d_counts,
+                       const uint32_t* __restrict__ idx, const float* __restrict__ pos, const float* __restrict__ nrm,
+                       float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (d_counts ? min(n_prims, d_counts[1] / N) : n_prims)) return;
+  const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
   uint32_t v[N];
 #pragma unroll
-  for (int k = 0; k < N; ++k) v[k] = __ldg(idx + N * t + k);
+  for (int k = 0; k < N; ++k) {
+    v[k] = __ldg(idx + N * t + k);
+    if ((int64_t)v[k] >= nvb) v[k] = 0;  // an index outside the mesh reads vertex 0 instead of faulting
+  }
   float p[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
   for (int k = 0; k < N; ++k) {
@@ -220,20 +227,24 @@ __global__ void k_dual(int64_t n_prims, const int64_t* __restrict__ d_counts, co
 }
 
 // optimize_primal_grid (MeshProcessor.cpp:238-306).
-__global__ void k_primal(int64_t nv, const int64_t* __restrict__ d_counts, const uint32_t* __restrict__ off,
-                         const uint32_t* __restrict__ cursor,
+__global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int64_t* __restrict__ d_counts,
+                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
                          const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
                          const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
                          const float* __restrict__ dual_n, float* __restrict__ pos, float* __restrict__ nrm,
                          int process_boundary, int smooth_normals, int set_colors) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
-  const uint32_t n = min(cursor[v], (uint32_t)valence[v]);
+  // list length: adj_next (MeshProcessor.cpp:247); with a prebuilt adjacency it equals init_valence
+  const int64_t room = adj_cap - (int64_t)off[v];
+  const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)(cursor ? min(cursor[v], (uint32_t)valence[v])
+                                                                    : (uint32_t)valence[v]), room));
   if (n == 0 || (!process_boundary && boundary[v])) return;
   const uint32_t* a = adj + off[v];
   float p[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
   for (uint32_t k = 0; k < n; ++k) {
     const uint32_t t = __ldg(a + k);
+    if ((int64_t)t >= np_lim) continue;  // never read past the dual points
 #pragma unroll
     for (int c = 0; c < 3; ++c) p[c] = p[c] + __ldg(dual_p + 3 * t + c);
     if (smooth_normals) {
@@ -261,33 +272,45 @@ __global__ void k_primal(int64_t nv, const int64_t* __restrict__ d_counts, const
   }
 }
 
-void launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
-                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
-                    int process_boundary, int smooth_normals, ProcessScratch s, cudaStream_t st) {
-  if (nv == 0 || n_prims == 0 || iters <= 0) return;
+int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
+                   const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
+                   int process_boundary, int smooth_normals, ProcessScratch s, const StructuredAdj* sa,
+                   cudaStream_t st) {
+  if (nv == 0 || n_prims == 0 || iters <= 0) return 0;
   const int64_t n_slots = n_prims * N;
+  int launched = 3;
   // CSR offsets: exclusive scan of init_valence (MeshProcessor.cpp:32-40)
   launch_exclusive_scan_u8_to_u32(valence, s.off, nv, d_counts, s.tmp, st);
-  cudaMemsetAsync(s.cursor, 0, (size_t)nv * sizeof(uint32_t), st);
-  k_fill_adj<<<(int)((n_slots + 255) / 256), 256, 0, st>>>(N, n_slots, d_counts, idx, s.off, valence, s.cursor,
-                                                           s.adj);
   const int vb = (int)((nv + 255) / 256), pb = (int)((n_prims + 255) / 256);
-  k_sort_adj<<<vb, 256, 0, st>>>(nv, d_counts, s.off, s.cursor, valence, s.adj);
+  const uint32_t* cursor = nullptr;
+  if (sa) {
+    launch_adj_build(sa->mode, sa->chunks, sa->n_chunks, sa->words, sa->ws, sa->vkey, s.off, d_counts, nv, s.adj, st);
+    launched += 1;
+  } else {
+    cudaMemsetAsync(s.cursor, 0, (size_t)nv * sizeof(uint32_t), st);
+    k_fill_adj<<<(int)((n_slots + 255) / 256), 256, 0, st>>>(N, n_slots, nv, d_counts, idx, s.off, valence,
+                                                             s.cursor, s.adj);
+    k_sort_adj<<<vb, 256, 0, st>>>(nv, n_slots, d_counts, s.off, s.cursor, valence, s.adj);
+    cursor = s.cursor;
+    launched += 2;
+  }
   const int hard_norm_max = 10;
   const int max_norms = (iters / 2 - 3 < hard_norm_max ? iters / 2 - 3 : hard_norm_max);
   const bool sn = smooth_normals != 0 && nrm != nullptr;
   for (int m = 0; m < iters; ++m) {
     const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
     if (N == 3)
-      k_dual<3><<<pb, 256, 0, st>>>(n_prims, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
+      k_dual<3><<<pb, 256, 0, st>>>(n_prims, nv, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
     else
-      k_dual<4><<<pb, 256, 0, st>>>(n_prims, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
+      k_dual<4><<<pb, 256, 0, st>>>(n_prims, nv, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
     // primal after every dual step but the last (MeshProcessor.cpp:229-232),
     // and once more after the loop with set_colors false (ChunkGenerator.cpp:120)
     const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
-    k_primal<<<vb, 256, 0, st>>>(nv, d_counts, s.off, s.cursor, valence, s.adj, boundary, s.dual_p, s.dual_n, pos,
-                                 nrm, process_boundary, sn ? 1 : 0, set_colors);
+    k_primal<<<vb, 256, 0, st>>>(nv, n_prims, n_slots, d_counts, s.off, cursor, valence, s.adj, boundary, s.dual_p,
+                                 s.dual_n, pos, nrm, process_boundary, sn ? 1 : 0, set_colors);
+    launched += 2;
   }
+  return launched;
 }
 
 }  // namespace bmf
