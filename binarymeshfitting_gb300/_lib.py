@@ -88,6 +88,8 @@ SIGNATURES = {
     "bmf_cell_masks": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_void_p]),
     "bmf_polygonize": (c_int32, [c_void_p, c_int32, c_void_p, c_void_p, c_int32, c_int32, ctypes.POINTER(Mesh),
                                  c_void_p]),
+    "bmf_polygonize_noalloc": (c_int32, [c_int32, c_void_p, c_void_p, c_int32, c_int32, ctypes.POINTER(Mesh),
+                                         c_void_p]),
     "bmf_process": (c_int32, [c_void_p, ctypes.POINTER(Mesh), c_int32, c_int32, c_int32, c_void_p]),
     "bmf_extract_chunk": (c_int32, [c_void_p, ctypes.POINTER(ChunkDesc), ctypes.POINTER(Field),
                                     ctypes.POINTER(ExtractOpts), ctypes.POINTER(Mesh), c_void_p]),

@@ -143,6 +143,23 @@ BMF_API bmf_status bmf_cell_masks(bmf_ctx* ctx, int32_t dim, const uint32_t* d_w
 BMF_API bmf_status bmf_polygonize(bmf_ctx* ctx, int32_t dim, const float* d_density, const uint32_t* d_words,
                           int32_t mode, int32_t placement, bmf_mesh* out, void* stream);
 
+/* Largest chunk (samples per axis) bmf_polygonize_noalloc accepts. */
+#define BMF_NOALLOC_MAX_DIM 129
+
+/* bmf_polygonize for callers that cannot allocate device memory.  No
+ * counterpart in the reference (its extraction always takes blocks from its
+ * allocator pools).  Meant for hosts that own all device memory through their
+ * own pool or may not block on the driver's allocator (engines, real-time
+ * threads): it needs no bmf_ctx and calls no cudaMalloc / cudaFree; its
+ * scratch is a fixed ~1.7 MB device array that every GPU loading the library
+ * holds until exit.  dim > BMF_NOALLOC_MAX_DIM returns BMF_ERR_NOT_SUPPORTED.
+ * All calls share that array: calls that overlap on the GPU race, so
+ * serialise them.  The first call on a device resolves the array's address
+ * for that device; make it before any stream capture.  Inputs, outputs and
+ * results are those of bmf_polygonize; synchronises the stream. */
+BMF_API bmf_status bmf_polygonize_noalloc(int32_t dim, const float* d_density, const uint32_t* d_words,
+                                          int32_t mode, int32_t placement, bmf_mesh* out, void* stream);
+
 /* MeshProcessor<N>::init/optimize_dual_grid/optimize_primal_grid/flush
  * (MeshProcessor.cpp:26-306) in the order ChunkGenerator::extract_chunk uses
  * (ChunkGenerator.cpp:112-124).  Updates d_pos (and d_nrm when non-NULL) in
