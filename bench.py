@@ -46,6 +46,9 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=128, help="chunks per CPU sample")
     p.add_argument("--skip-per-chunk", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--fit-chunks", type=int, default=512)
+    p.add_argument("--fit-steps", type=int, default=200)
+    p.add_argument("--skip-fit", action="store_true")
     return p.parse_args()
 
 
@@ -175,6 +178,87 @@ def config(args):
             "smoothing_iters": args.iters, "smoothed_normals": not args.no_normals,
             "l2": "inputs larger than L2: 7.1 GB density written per step", "parallelism": "replicas" if
             args.gpus == 1 else "weak: one independent update per GPU"}
+
+
+def run_fit(ctx, args, stream):
+    """Batched fitting: forward / backward kernel times (bwd/fwd) and an Adam
+    loop on fit_chunks learnable 65^3 grids with sphere-union targets."""
+    import torch
+
+    from binarymeshfitting_gb300 import _lib as L
+    from binarymeshfitting_gb300 import workloads
+    from binarymeshfitting_gb300.fitting import ExtractFit, FitPlan, sphere_union_loss
+
+    n, dim, iters = args.fit_chunks, 65, 8
+    dens0, spheres = workloads.fit_batch(n, dim=dim, seed=77)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    plan = FitPlan(ctx, n, dim, L.PLACE_QEF, iters)
+    plan_bytes = free0 - torch.cuda.mem_get_info()[0]
+    pos, _, info = plan.forward(dens0)
+    leaf = pos.detach().clone().requires_grad_(True)
+    (gpos,) = torch.autograd.grad(sphere_union_loss(leaf, info, spheres), leaf)
+    gden = torch.empty_like(dens0)
+    nv = plan.n_verts
+    for _ in range(3):
+        plan.forward(dens0, sync=False)
+        plan.backward(gpos, out=gden)
+    torch.cuda.synchronize()
+    k = max(args.steps, 5)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    e[0].record(stream)
+    for _ in range(k):
+        plan.forward(dens0, sync=False)
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    e[2].record(stream)
+    for _ in range(k):
+        plan.backward(gpos, out=gden)
+    e[3].record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = e[0].elapsed_time(e[1]) / k
+    bwd_ms = e[2].elapsed_time(e[3]) / k
+    # the same backward with the FP32 QEF adjoint, for comparison
+    plan32 = FitPlan(ctx, n, dim, L.PLACE_QEF, iters, adjoint_f64=False)
+    plan32.forward(dens0)
+    for _ in range(3):
+        plan32.backward(gpos, out=gden)
+    torch.cuda.synchronize()
+    e[2].record(stream)
+    for _ in range(k):
+        plan32.backward(gpos, out=gden)
+    e[3].record(stream)
+    torch.cuda.synchronize()
+    bwd32_ms = e[2].elapsed_time(e[3]) / k
+    plan32.close()
+    del plan32
+    # the fitting loop: topology recomputed every forward, smoothing adjoint
+    # applied without stored iterates (the sweeps are linear in positions)
+    dens = dens0.clone().requires_grad_(True)
+    opt = torch.optim.Adam([dens], lr=1e-2)
+    torch.cuda.reset_peak_memory_stats()
+    losses = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.fit_steps):
+        opt.zero_grad(set_to_none=False)
+        p = ExtractFit.apply(dens, plan)
+        loss = sphere_union_loss(p, plan.info, spheres)
+        loss.backward()
+        opt.step()
+        losses.append(loss.detach())
+    torch.cuda.synchronize()
+    step_ms = (time.perf_counter() - t0) * 1000.0 / max(args.fit_steps, 1)
+    peak = torch.cuda.max_memory_allocated() + plan_bytes
+    out = {"workload": "fit_%dx65^3" % n, "fwd_ms": fwd_ms, "bwd_ms": bwd_ms, "ratio": bwd_ms / fwd_ms,
+           "adjoint": "QEF adjoint from an FP64 re-solve (default)", "bwd_ms_fp32_adjoint": bwd32_ms,
+           "vertices": nv, "fit_steps": args.fit_steps, "step_ms": step_ms, "peak_mem_bytes": int(peak),
+           "loss_first": float(losses[0]) if losses else None, "loss_last": float(losses[-1]) if losses else None,
+           "note": "fwd = bmf_fit_forward (label, count, scan, offsets, emit with QEF, 8 sweeps); bwd = "
+                   "bmf_fit_backward (sweep adjoint + QEF/hermite adjoint); Adam step timed on the host "
+                   "clock incl. the totals read-back, torch loss and optimizer"}
+    plan.close()
+    return out
 
 
 def run_gb300(args):
@@ -311,6 +395,15 @@ def run_gb300(args):
                      "vertices_match_batch": pv == nv, "batch_speedup": (args.chunks / (ms / 1000.0)) /
                      (args.chunks / pc_s)}
 
+    # ---- batched fitting: backward vs forward ----
+    bwd_fwd = None
+    if not args.skip_fit and rank == 0:
+        b.close()
+        b = None
+        del bufs
+        torch.cuda.empty_cache()
+        bwd_fwd = run_fit(ctx, args, stream)
+
     # ---- CPU baseline (rank 0): bounded sample of the same update, all host threads ----
     cpu_baseline = None
     if not args.skip_cpu and rank == 0:
@@ -331,9 +424,10 @@ def run_gb300(args):
                 "samples_per_s": samples * world / (ms / 1000.0),
                 "vertices_per_s": nv * world / (ms / 1000.0), "vertices_per_step": nv, "indices_per_step": ni,
                 "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e, "per_chunk": per_chunk,
-                "gpu_launches": launches, "clocks": clk, "bwd_fwd": None}
+                "gpu_launches": launches, "clocks": clk, "bwd_fwd": bwd_fwd}
         print(json.dumps(line), flush=True)
-    b.close()
+    if b is not None:
+        b.close()
     ctx.close()
     if world > 1:
         dist.destroy_process_group()

@@ -15,6 +15,7 @@ FIELD_GRID, FIELD_SPHERE_WAVE, FIELD_TERRAIN_FBM = 0, 1, 2
 FIELD_TORUS_Z, FIELD_SPHERE, FIELD_CUBOID, FIELD_PLANE_Y = 3, 4, 5, 6
 MODE_R, MODE_Q = 0, 1
 PLACE_CENTER, PLACE_MASSPOINT, PLACE_QEF = 0, 1, 2
+FIT_ADJOINT_F64 = 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "output capacity exceeded", 4: "device wait timed out",
           5: "out of device memory", 6: "not supported"}
@@ -99,6 +100,12 @@ SIGNATURES = {
     "bmf_batch_destroy": (c_int32, [c_void_p]),
     "bmf_batch_set_descs": (c_int32, [c_void_p, ctypes.POINTER(ChunkDesc), c_int32, c_void_p]),
     "bmf_batch_profile": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), ctypes.POINTER(c_float), c_void_p]),
+    "bmf_fit_create": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_int64, c_int64, c_int32,
+                                 ctypes.POINTER(c_void_p)]),
+    "bmf_fit_forward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_int64),
+                                  c_void_p]),
+    "bmf_fit_backward": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "bmf_fit_destroy": (c_int32, [c_void_p]),
 }
 
 _lib = None

@@ -678,6 +678,159 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   return BMF_OK;
 }
 
+// ---------------------------------------------------------------------------
+// differentiable extraction (fitting)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct bmf_fit {
+  bmf_ctx* ctx = nullptr;
+  int n = 0, dim = 0, placement = 0, iters = 0, flags = 0;
+  int64_t vcap = 0, icap = 0;
+  ChunkDev* d_chunks = nullptr;
+  int* d_units = nullptr;
+  uint32_t *d_flags = nullptr, *d_tot = nullptr, *d_words = nullptr;
+  int64_t* d_totals = nullptr;
+  WordScratch ws{};
+  ProcessScratch ps{};
+  uint32_t *d_idxg = nullptr, *d_vkey = nullptr;
+  uint8_t *d_valence = nullptr, *d_boundary = nullptr;
+  float* d_g = nullptr;           // position-gradient work buffer
+  const float* last_density = nullptr;
+  int64_t* h_pinned = nullptr;
+};
+
+extern "C" {
+
+bmf_status bmf_fit_destroy(bmf_fit* f) {
+  if (!f) return BMF_ERR_INVALID_ARGUMENT;
+  void* ptrs[] = {f->d_chunks, f->d_units, f->d_flags, f->d_tot, f->d_words, f->d_totals, f->ws.vcnt, f->ws.icnt,
+                  f->ws.gpl, f->ps.off, f->ps.cursor, f->ps.adj, f->ps.dual_p, f->ps.dual_n, f->ps.tmp, f->d_idxg,
+                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (f->h_pinned) cudaFreeHost(f->h_pinned);
+  delete f;
+  return BMF_OK;
+}
+
+bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t placement, int32_t iters,
+                          int64_t vcap, int64_t icap, int32_t flags, bmf_fit** out) {
+  if (!ctx || !out) return BMF_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (n_chunks <= 0 || !dim_ok(dim) || (placement != BMF_PLACE_MASSPOINT && placement != BMF_PLACE_QEF) ||
+      iters < 0 || vcap <= 0 || icap <= 0 || (flags & ~BMF_FIT_ADJOINT_F64))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
+                "bmf_fit_create: bad count, dim, placement, iters, capacity or flags");
+  bmf_fit* f = new bmf_fit();
+  f->ctx = ctx;
+  f->n = n_chunks;
+  f->dim = dim;
+  f->placement = placement;
+  f->iters = iters;
+  f->flags = flags;
+  f->vcap = vcap;
+  f->icap = icap;
+  const int zc = (dim + 31) / 32;
+  const int64_t words = (int64_t)n_chunks * dim * dim * zc;
+  std::vector<ChunkDev> hc(n_chunks);
+  std::vector<int> units(n_chunks + 1);
+  for (int i = 0; i < n_chunks; ++i) {
+    ChunkDev c{};
+    c.scale = 1.0f;
+    c.dim = dim;
+    c.zc = zc;
+    c.dens = (int64_t)i * dim * dim * dim;
+    c.words = (int64_t)i * dim * dim * zc;
+    hc[i] = c;
+    units[i] = i * dim;
+  }
+  units[n_chunks] = n_chunks * dim;
+  const int64_t np = icap / 4;
+  bool ok = cudaMalloc(&f->d_chunks, sizeof(ChunkDev) * n_chunks) == cudaSuccess &&
+            cudaMalloc(&f->d_units, sizeof(int) * (n_chunks + 1)) == cudaSuccess &&
+            cudaMalloc(&f->d_flags, sizeof(uint32_t) * n_chunks) == cudaSuccess &&
+            cudaMalloc(&f->d_tot, sizeof(uint32_t) * 2 * n_chunks) == cudaSuccess &&
+            cudaMalloc(&f->d_words, sizeof(uint32_t) * words) == cudaSuccess &&
+            cudaMalloc(&f->d_totals, sizeof(int64_t) * 2) == cudaSuccess &&
+            cudaMalloc(&f->ws.vcnt, sizeof(uint32_t) * words) == cudaSuccess &&
+            cudaMalloc(&f->ws.icnt, sizeof(uint32_t) * words) == cudaSuccess &&
+            cudaMalloc(&f->ws.gpl, sizeof(uint32_t) * 3 * words) == cudaSuccess &&
+            cudaMalloc(&f->ps.off, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
+            cudaMalloc(&f->ps.adj, sizeof(uint32_t) * (np * 4 + 1)) == cudaSuccess &&
+            cudaMalloc(&f->ps.dual_p, sizeof(float) * (3 * np + 3)) == cudaSuccess &&
+            cudaMalloc(&f->ps.tmp, sizeof(uint32_t) * (vcap / 4096 + 2)) == cudaSuccess &&
+            cudaMalloc(&f->d_idxg, sizeof(uint32_t) * (icap + 1)) == cudaSuccess &&
+            cudaMalloc(&f->d_vkey, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
+            cudaMalloc(&f->d_valence, vcap + 1) == cudaSuccess && cudaMalloc(&f->d_boundary, vcap + 1) == cudaSuccess &&
+            cudaMalloc(&f->d_g, sizeof(float) * 3 * (vcap + 1)) == cudaSuccess &&
+            cudaMallocHost(&f->h_pinned, sizeof(int64_t) * 4) == cudaSuccess &&
+            cudaMemcpy(f->d_chunks, hc.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(f->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    bmf_fit_destroy(f);
+    return fail(ctx, BMF_ERR_OUT_OF_MEMORY, "bmf_fit_create: device allocation failed");
+  }
+  *out = f;
+  return BMF_OK;
+}
+
+bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uint32_t* d_idx, int64_t* d_chunk_info,
+                           int64_t* h_counts, void* stream) {
+  if (!f) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = f->ctx;
+  if (!d_density || !d_pos || !d_idx) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_fit_forward: null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  FieldDev fd{};
+  fd.kind = BMF_FIELD_GRID;
+  BMF_CUDA(ctx, cudaMemsetAsync(f->d_flags, 0, sizeof(uint32_t) * f->n, st));
+  launch_sample_label(f->d_chunks, f->n, f->d_units, f->n * f->dim, f->dim, fd, d_density, nullptr, f->d_words,
+                      f->d_flags, st);
+  launch_count(BMF_MODE_Q, f->d_chunks, f->n, f->d_units, f->n * f->dim, f->d_words, f->d_flags, f->ws, st);
+  launch_scan_chunks(f->d_chunks, f->n, f->ws, f->d_tot, st);
+  launch_chunk_offsets(f->d_chunks, f->n, f->d_tot, f->d_flags, f->vcap, f->icap, d_chunk_info, f->d_totals, st);
+  MeshOut mo{d_pos, nullptr, f->d_boundary, f->d_valence, d_idx, f->d_idxg, f->vcap, f->icap, f->d_vkey};
+  launch_emit(BMF_MODE_Q, f->placement, f->d_chunks, f->n, f->d_units, f->n * f->dim, f->d_words, d_density,
+              f->d_flags, f->ws, mo, st);
+  int k = 5;
+  if (f->iters > 0) {
+    const StructuredAdj sa{BMF_MODE_Q, f->d_chunks, f->n, f->d_words, f->ws, f->d_vkey};
+    k += launch_process(4, f->vcap, f->icap / 4, f->d_totals, d_pos, nullptr, f->d_boundary, f->d_valence, f->d_idxg,
+                        f->iters, 0, 0, f->ps, &sa, st);
+  }
+  BMF_LAUNCHED(ctx, k);
+  f->last_density = d_density;
+  if (h_counts) {
+    BMF_CUDA(ctx, cudaMemcpyAsync(f->h_pinned, f->d_totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    BMF_CUDA(ctx, cudaStreamSynchronize(st));
+    h_counts[0] = f->h_pinned[0];
+    h_counts[1] = f->h_pinned[1];
+    if (h_counts[0] > f->vcap || h_counts[1] > f->icap)
+      return fail(ctx, BMF_ERR_CAPACITY, "bmf_fit_forward: output capacity exceeded (needed totals reported)");
+  }
+  return BMF_OK;
+}
+
+bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_verts, float* d_grad_density,
+                            void* stream) {
+  if (!f) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = f->ctx;
+  if (!d_grad_pos || !d_grad_density || !f->last_density || n_grad_verts < 0)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_fit_backward: null buffer or no forward yet");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t ng = n_grad_verts < f->vcap ? n_grad_verts : f->vcap;
+  BMF_CUDA(ctx, cudaMemsetAsync(f->d_g, 0, sizeof(float) * 3 * f->vcap, st));
+  if (ng > 0)
+    BMF_CUDA(ctx, cudaMemcpyAsync(f->d_g, d_grad_pos, sizeof(float) * 3 * ng, cudaMemcpyDeviceToDevice, st));
+  int k = launch_process_bwd(4, f->vcap, f->icap / 4, f->d_totals, f->d_boundary, f->d_valence, f->d_idxg, f->iters,
+                             0, f->ps, f->d_g, st);
+  BMF_CUDA(ctx, cudaMemsetAsync(d_grad_density, 0, sizeof(float) * (size_t)f->n * f->dim * f->dim * f->dim, st));
+  launch_place_bwd(f->placement, (f->flags & BMF_FIT_ADJOINT_F64) != 0, f->d_chunks, f->n, f->d_words,
+                   f->last_density, f->d_vkey, f->d_totals, f->vcap, f->d_g, d_grad_density, st);
+  BMF_LAUNCHED(ctx, k + 1);
+  return BMF_OK;
+}
+
 bmf_status bmf_batch_destroy(bmf_batch* b) {
   if (!b) return BMF_ERR_INVALID_ARGUMENT;
   if (b->exec) cudaGraphExecDestroy(b->exec);

@@ -136,6 +136,88 @@ __device__ __forceinline__ float perlin(const int* __restrict__ perm, float x, f
   return lerp_t(w, l0, l1);
 }
 
+// ---------------------------------------------------------------------------
+// Run evaluation of the terrain FBM: R consecutive z-samples of one (x, y)
+// line, with every x/y-dependent term computed once per octave.  Results are
+// bit-identical to perlin() per sample: the same float operations in the same
+// order; only the integer bookkeeping is reorganised:
+//  * perm2 is the permutation duplicated to 512 entries, so the hash chain
+//    A = P[X]+Y, AA = P[A]+Z, P[AA+1] indexes it without "& 255" masks;
+//  * gcode[i] encodes grad() for hash perm2[i]: .x low 16 bits = byte-permute
+//    selector picking u from (x, y), high 16 = selector picking t from (y, z);
+//    .y low 16 = selector picking v from (t, x), bit 31 = negate u, bit 30 =
+//    negate v.  grad = (+/-u) + (+/-v) exactly as in perlin().
+// ---------------------------------------------------------------------------
+constexpr int kRun = 4;
+
+__host__ __device__ inline uint2 grad_code(int h) {
+  h &= 15;
+  const uint32_t sel_u = (h & 8) ? 0x7654u : 0x3210u;  // y : x
+  const uint32_t sel_t = (h & 12) == 0 ? 0x3210u : 0x7654u;  // y : z
+  const uint32_t sel_v = (h & 13) == 12 ? 0x7654u : 0x3210u;  // x : t
+  uint2 c;
+  c.x = sel_u | (sel_t << 16);
+  c.y = sel_v | ((uint32_t)(h & 1) << 31) | ((uint32_t)((h >> 1) & 1) << 30);
+  return c;
+}
+
+__device__ __forceinline__ float grad_coded(uint2 c, float x, float y, float z) {
+  const uint32_t xb = __float_as_uint(x), yb = __float_as_uint(y), zb = __float_as_uint(z);
+  uint32_t u = __byte_perm(xb, yb, c.x);
+  const uint32_t t = __byte_perm(yb, zb, c.x >> 16);
+  uint32_t v = __byte_perm(t, xb, c.y);
+  u ^= c.y & 0x80000000u;
+  v ^= (c.y << 1) & 0x80000000u;
+  return __uint_as_float(u) + __uint_as_float(v);
+}
+
+// Terrain field (y - h) - a * FBM over a run of n <= kRun samples at
+// z-coordinates pz[k]; px, py are the line's world x, y.
+__device__ __forceinline__ void terrain_run(const FieldDev& f, const int* __restrict__ perm2,
+                                            const uint2* __restrict__ gcode, float px, float py, const float* pz,
+                                            int n, float* out) {
+  float sum[kRun];
+#pragma unroll
+  for (int k = 0; k < kRun; ++k) sum[k] = 0.0f;
+  const int oct = (int)f.p[5];
+  float amp = 1.0f, fr = f.p[2];
+  for (int o = 0; o < oct; ++o) {
+    const float xs = px * fr, ys = py * fr;
+    const float fx = floorf(xs), fy = floorf(ys);
+    const int X = ((int)fx) & 255, Y = ((int)fy) & 255;
+    const float xf = xs - fx, yf = ys - fy;
+    const float u = fade(xf), v = fade(yf);
+    const float x1 = xf - 1.0f, y1 = yf - 1.0f;
+    const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
+    const int pA = perm2[A], pA1 = perm2[A + 1], pB = perm2[B], pB1 = perm2[B + 1];
+#pragma unroll
+    for (int k = 0; k < kRun; ++k) {
+      if (k >= n) break;
+      const float zs = pz[k] * fr;
+      const float fz = floorf(zs);
+      const int Z = ((int)fz) & 255;
+      const float zf = zs - fz;
+      const float w = fade(zf);
+      const float z1 = zf - 1.0f;
+      const int AA = pA + Z, AB = pA1 + Z, BA = pB + Z, BB = pB1 + Z;
+      const float g000 = grad_coded(gcode[AA], xf, yf, zf), g100 = grad_coded(gcode[BA], x1, yf, zf);
+      const float g010 = grad_coded(gcode[AB], xf, y1, zf), g110 = grad_coded(gcode[BB], x1, y1, zf);
+      const float g001 = grad_coded(gcode[AA + 1], xf, yf, z1), g101 = grad_coded(gcode[BA + 1], x1, yf, z1);
+      const float g011 = grad_coded(gcode[AB + 1], xf, y1, z1), g111 = grad_coded(gcode[BB + 1], x1, y1, z1);
+      const float l00 = lerp_t(u, g000, g100), l10 = lerp_t(u, g010, g110);
+      const float l01 = lerp_t(u, g001, g101), l11 = lerp_t(u, g011, g111);
+      const float l0 = lerp_t(v, l00, l10), l1 = lerp_t(v, l01, l11);
+      const float nv = lerp_t(w, l0, l1);
+      sum[k] = sum[k] + amp * nv;
+    }
+    fr = fr * f.p[3];
+    amp = amp * f.p[4];
+  }
+#pragma unroll
+  for (int k = 0; k < kRun; ++k)
+    if (k < n) out[k] = (py - f.p[0]) - f.p[1] * sum[k];
+}
+
 __device__ __forceinline__ float len3(float x, float y, float z) {
   const float a = x * x, b = y * y, c = z * z;
   return sqrtf((a + b) + c);

@@ -86,6 +86,18 @@ int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, 
                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
                    int process_boundary, int smooth_normals, ProcessScratch s, const StructuredAdj* sa,
                    cudaStream_t st);
+// Adjoint of the position sweeps of launch_process (needs its CSR in s.off /
+// s.adj; uses s.dual_p as scratch).  g holds dL/d(final positions) on entry and
+// dL/d(initial positions) on return.  Returns the number of kernels launched.
+int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, const uint8_t* boundary,
+                       const uint8_t* valence, const uint32_t* idx, int iters, int process_boundary,
+                       const ProcessScratch& s, float* g, cudaStream_t st);
+// Adjoint of Mode Q placement (placement 1 mass point, 2 QEF; f64: the QEF
+// derivative from an FP64 re-solve); accumulates into grad_dens (the caller
+// clears it).
+void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
+                      const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
+                      const float* grad_pos, float* grad_dens, cudaStream_t st);
 void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n, const int64_t* d_n,
                                      uint32_t* block_tmp, cudaStream_t st);
 

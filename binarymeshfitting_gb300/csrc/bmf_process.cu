@@ -272,6 +272,83 @@ __global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int6
   }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of the position sweeps.  A dual step averages each primitive's N
+// vertices; a primal step replaces every updated vertex (adjacency non-empty,
+// not a frozen boundary vertex) by the mean of its primitives' dual points and
+// leaves the others unchanged.  Both are linear in the positions and do not
+// depend on them, so the backward needs no stored iterates: it applies the
+// transposes, last sweep first.  Both transposes are gathers (per primitive /
+// per vertex through the CSR), so they need no atomics.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool primal_updates(const uint8_t* valence, const uint8_t* boundary, int64_t v,
+                                               int process_boundary) {
+  return valence[v] != 0 && (process_boundary || !boundary[v]);
+}
+
+// g_dual[t] = sum over the primitive's slots of g[v] / count(v), updated v only.
+template <int N>
+__global__ void k_primal_bwd(int64_t n_prims, int64_t nv, const int64_t* __restrict__ d_counts,
+                             const uint32_t* __restrict__ idx, const uint8_t* __restrict__ valence,
+                             const uint8_t* __restrict__ boundary, int process_boundary, const float* __restrict__ g,
+                             float* __restrict__ g_dual) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (d_counts ? min(n_prims, d_counts[1] / N) : n_prims)) return;
+  const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
+  float s[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const uint32_t v = __ldg(idx + N * t + k);
+    if ((int64_t)v >= nvb || !primal_updates(valence, boundary, v, process_boundary)) continue;
+    const float inv = 1.0f / (float)valence[v];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s[c] += __ldg(g + 3 * v + c) * inv;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) g_dual[3 * t + c] = s[c];
+}
+
+// g[v] <- (updated(v) ? 0 : g[v]) + sum over t in adj(v) of g_dual[t] / N (in place).
+__global__ void k_dual_bwd(int N, int64_t nv, int64_t n_prims, int64_t adj_cap, const int64_t* __restrict__ d_counts,
+                           const uint32_t* __restrict__ off, const uint8_t* __restrict__ valence,
+                           const uint32_t* __restrict__ adj, const uint8_t* __restrict__ boundary, int process_boundary,
+                           const float* __restrict__ g_dual, float* __restrict__ g) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
+  const int64_t room = adj_cap - (int64_t)off[v];
+  const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)valence[v], room));
+  float s[3] = {0.0f, 0.0f, 0.0f};
+  if (!primal_updates(valence, boundary, v, process_boundary)) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s[c] = g[3 * v + c];
+  }
+  const float invN = 1.0f / (float)N;
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint32_t t = __ldg(adj + off[v] + k);
+    if ((int64_t)t >= n_prims) continue;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s[c] += __ldg(g_dual + 3 * t + c) * invN;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) g[3 * v + c] = s[c];
+}
+
+int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, const uint8_t* boundary,
+                       const uint8_t* valence, const uint32_t* idx, int iters, int process_boundary,
+                       const ProcessScratch& s, float* g, cudaStream_t st) {
+  if (nv == 0 || n_prims == 0 || iters <= 0) return 0;
+  const int vb = (int)((nv + 255) / 256), pb = (int)((n_prims + 255) / 256);
+  for (int m = iters - 1; m >= 0; --m) {
+    if (N == 3)
+      k_primal_bwd<3><<<pb, 256, 0, st>>>(n_prims, nv, d_counts, idx, valence, boundary, process_boundary, g, s.dual_p);
+    else
+      k_primal_bwd<4><<<pb, 256, 0, st>>>(n_prims, nv, d_counts, idx, valence, boundary, process_boundary, g, s.dual_p);
+    k_dual_bwd<<<vb, 256, 0, st>>>(N, nv, n_prims, n_prims * N, d_counts, s.off, valence, s.adj, boundary,
+                                   process_boundary, s.dual_p, g);
+  }
+  return 2 * iters;
+}
+
 int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
                    int process_boundary, int smooth_normals, ProcessScratch s, const StructuredAdj* sa,

@@ -30,53 +30,64 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
                                                       const float* __restrict__ dens_in, float* __restrict__ dens_out,
                                                       uint32_t* __restrict__ words, uint32_t* __restrict__ flags) {
   extern __shared__ uint32_t sw[];
-  __shared__ int perm[256];
+  __shared__ int perm2[512];
+  __shared__ uint2 gcode[512];
   const int u = blockIdx.x;
   const int c = find_chunk(unit_start, n_chunks, u);
   const ChunkDev ch = chunks[c];
   const int x = u - __ldg(unit_start + c);
   const int dim = ch.dim, zc = ch.zc;
   const int nw = dim * zc;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) perm[i] = field.perm[i];
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+    perm2[i] = field.perm[i & 255];
+    gcode[i] = grad_code(field.perm[i & 255]);
+  }
   for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = 0u;
   __syncthreads();
 
+  // Work item = a run of kRun consecutive z-samples of one (x, y) line; runs
+  // start at multiples of kRun (which divides 32), so a run's inside bits land
+  // in a single occupancy word.
   const int plane = dim * dim;
-  const int lane = threadIdx.x & 31;
+  const int nruns = (dim + kRun - 1) / kRun;
   const float px = ch.ox + (float)x * ch.scale;
   const int64_t dbase = ch.dens + (int64_t)x * plane;
-  const int step = blockDim.x, step_y = step / dim, step_z = step % dim;
-  int y = threadIdx.x / dim, z = threadIdx.x % dim;
-  for (int s0 = threadIdx.x - lane; s0 < plane; s0 += step) {
-    const int s = s0 + lane;
-    const bool valid = s < plane;
-    float v = 0.0f;
-    if (valid) {
-      if (field.kind == BMF_FIELD_GRID) {
-        v = __ldg(dens_in + dbase + s);
+  for (int item = threadIdx.x; item < dim * nruns; item += blockDim.x) {
+    const int y = item / nruns;
+    const int z0 = (item - y * nruns) * kRun;
+    const int n = min(kRun, dim - z0);
+    const int64_t o = dbase + (int64_t)y * dim + z0;
+    float v[kRun];
+    if (field.kind == BMF_FIELD_GRID) {
+#pragma unroll
+      for (int k = 0; k < kRun; ++k)
+        if (k < n) v[k] = __ldg(dens_in + o + k);
+    } else {
+      const float py = ch.oy + (float)y * ch.scale;
+      float pz[kRun];
+#pragma unroll
+      for (int k = 0; k < kRun; ++k) pz[k] = ch.oz + (float)(z0 + k) * ch.scale;
+      if (field.kind == BMF_FIELD_TERRAIN_FBM) {
+        terrain_run(field, perm2, gcode, px, py, pz, n, v);
       } else {
-        const float py = ch.oy + (float)y * ch.scale;
-        const float pz = ch.oz + (float)z * ch.scale;
-        v = eval_field(field, perm, px, py, pz);
-        if (dens_out) dens_out[dbase + s] = v;
+#pragma unroll
+        for (int k = 0; k < kRun; ++k)
+          if (k < n) v[k] = eval_field(field, perm2, px, py, pz[k]);
+      }
+      if (dens_out) {
+#pragma unroll
+        for (int k = 0; k < kRun; ++k)
+          if (k < n) dens_out[o + k] = v[k];
       }
     }
-    const uint32_t in_bits = __ballot_sync(kFull, valid && v < 0.0f);
-    const bool start = valid && (lane == 0 || (z & 31) == 0);
-    const uint32_t starts = __ballot_sync(kFull, start);
-    if (start && in_bits) {
-      // run = this lane up to (not including) the next run start or warp end
-      const uint32_t later = starts & ~((2u << lane) - 1u);
-      const int end = later ? (__ffs(later) - 1) : 32;
-      const int len = end - lane;
-      const uint32_t run = (in_bits >> lane) & (len >= 32 ? kFull : ((1u << len) - 1u));
-      if (run) atomicOr(&sw[y * zc + (z >> 5)], run << (z & 31));
-    }
-    y += step_y;
-    z += step_z;
-    if (z >= dim) { z -= dim; ++y; }
+    uint32_t bits = 0u;
+#pragma unroll
+    for (int k = 0; k < kRun; ++k)
+      if (k < n && v[k] < 0.0f) bits |= 1u << k;
+    if (bits) atomicOr(&sw[y * zc + (z0 >> 5)], bits << (z0 & 31));
   }
   __syncthreads();
+  const int lane = threadIdx.x & 31;
   uint32_t f = 0;
   uint32_t* wout = words + ch.words + (int64_t)x * nw;
   for (int i = threadIdx.x; i < nw; i += blockDim.x) {

@@ -1,0 +1,120 @@
+"""torch.autograd binding of the differentiable extraction (bmf_fit_* in bmf.h).
+
+Density grids in, mesh vertex positions out; gradients flow back into the
+density through the library's adjoint kernels (QEF placement and position
+sweeps).  Topology and index buffers never carry gradients.  This module is the
+thin test/fitting binding; the compute is in libbmf_gb300.so.
+"""
+import ctypes
+
+import torch
+
+from . import _lib as L
+from .engine import Context, _stream
+
+
+class FitPlan:
+    """n_chunks learnable grids of dim^3 samples (bmf_fit).  adjoint_f64: the
+    QEF adjoint from an FP64 re-solve (the derivative of the exact-arithmetic
+    placement); False differentiates the forward's own FP32 eigen pairs."""
+
+    def __init__(self, ctx: Context, n_chunks, dim, placement=L.PLACE_QEF, iters=8, vcap=None, icap=None,
+                 adjoint_f64=True):
+        self.ctx = ctx
+        self.n, self.dim, self.iters = n_chunks, dim, iters
+        self.vcap = vcap or n_chunks * dim * dim * 4
+        self.icap = icap or 4 * self.vcap
+        h = ctypes.c_void_p()
+        flags = L.FIT_ADJOINT_F64 if adjoint_f64 else 0
+        ctx._check(ctx.lib.bmf_fit_create(ctx.h, n_chunks, dim, placement, iters, self.vcap, self.icap, flags,
+                                          ctypes.byref(h)))
+        self.h = h
+        dev = ctx.device
+        self.pos = torch.empty((self.vcap, 3), dtype=torch.float32, device=dev)
+        self.idx = torch.empty(self.icap, dtype=torch.int32, device=dev)
+        self.info = torch.zeros((n_chunks, 6), dtype=torch.int64, device=dev)
+        self.n_verts = self.n_idx = 0
+
+    def forward(self, density: torch.Tensor, sync=True):
+        """Extracts all chunks.  sync=True reads the totals back and returns views
+        of exactly the output; sync=False only enqueues (whole buffers returned)."""
+        assert density.is_cuda and density.dtype == torch.float32 and density.is_contiguous()
+        assert density.numel() == self.n * self.dim ** 3
+        counts = (ctypes.c_int64 * 2)()
+        self.ctx._check(self.ctx.lib.bmf_fit_forward(self.h, ctypes.c_void_p(density.data_ptr()),
+                                                     ctypes.c_void_p(self.pos.data_ptr()),
+                                                     ctypes.c_void_p(self.idx.data_ptr()),
+                                                     ctypes.c_void_p(self.info.data_ptr()),
+                                                     counts if sync else None, _stream()))
+        if not sync:
+            return self.pos, self.idx, self.info
+        self.n_verts, self.n_idx = int(counts[0]), int(counts[1])
+        return self.pos[: self.n_verts], self.idx[: self.n_idx], self.info
+
+    def backward(self, grad_pos: torch.Tensor, out: torch.Tensor = None):
+        g = grad_pos.contiguous()
+        out = out if out is not None else torch.empty(self.n * self.dim ** 3, dtype=torch.float32,
+                                                      device=self.ctx.device)
+        self.ctx._check(self.ctx.lib.bmf_fit_backward(self.h, ctypes.c_void_p(g.data_ptr()), g.shape[0],
+                                                      ctypes.c_void_p(out.data_ptr()), _stream()))
+        return out
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.bmf_fit_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ExtractFit(torch.autograd.Function):
+    """positions = extract(density) with the topology held fixed."""
+
+    @staticmethod
+    def forward(ctx, density, plan: FitPlan):
+        pos, _, _ = plan.forward(density.detach().contiguous())
+        ctx.plan = plan
+        ctx.shape = density.shape
+        return pos.clone()
+
+    @staticmethod
+    def backward(ctx, grad_pos):
+        g = ctx.plan.backward(grad_pos)
+        return g.view(ctx.shape), None
+
+
+def rounded_box_sdf(p, centre, half, radius):
+    """Signed distance to a box with rounded edges (half extents, corner radius)."""
+    q = (p - centre).abs() - half + radius
+    outside = torch.clamp(q, min=0.0).norm(dim=-1)
+    inside = torch.clamp(q.max(dim=-1).values, max=0.0)
+    return outside + inside - radius
+
+
+def sphere_union_sdf(p, centres, radii):
+    """Signed distance to a union of spheres (centres (k, 3), radii (k,))."""
+    d = (p[:, None, :] - centres[None]).norm(dim=-1) - radii[None]
+    return d.min(dim=1).values
+
+
+def vertex_chunk_ids(info, n_verts):
+    """Chunk of each output vertex, from the per-chunk table (column 0: vertex
+    offset, ascending; an empty chunk shares its offset with the next one)."""
+    v = torch.arange(n_verts, device=info.device, dtype=info.dtype)
+    return torch.searchsorted(info[:, 0].contiguous(), v, right=True) - 1
+
+
+def sphere_union_loss(pos, info, spheres):
+    """Sum over chunks of the mean squared sphere-union SDF of each chunk's
+    vertices.  spheres: (n_chunks, k, 4) rows of centre xyz, radius (unused rows
+    are placed far away)."""
+    cid = vertex_chunk_ids(info, pos.shape[0])
+    sp = spheres[cid]
+    d = ((pos[:, None, :] - sp[..., :3]).norm(dim=-1) - sp[..., 3]).min(dim=1).values
+    cnt = info[:, 1].clamp(min=1).to(pos.dtype)
+    per_chunk = torch.zeros(info.shape[0], dtype=pos.dtype, device=pos.device).index_add_(0, cid, d * d)
+    return (per_chunk / cnt).sum()

@@ -68,3 +68,28 @@ def shard(rows, rank, world_size):
     if rank == world_size - 1:
         hi = len(rows)
     return np.arange(lo, hi)
+
+
+def fit_batch(n, dim=65, seed=0, device="cuda"):
+    """Learnable density grids and targets for batched fitting: chunk i holds the
+    sphere |p - c| - 20 (c = chunk centre) plus N(0, 0.1) noise on dim^3 samples;
+    its target is a union of 1-4 spheres, radii U[6, 20], centres U[4, dim - 5]
+    per axis.  Returns (density (n * dim^3,) float32, spheres (n, 4, 4) float32);
+    unused sphere rows sit at 1e6 with radius 0."""
+    import torch
+
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    g = torch.arange(dim, dtype=torch.float32, device=device)
+    c = (dim - 1) / 2.0
+    r = ((g[:, None, None] - c) ** 2 + (g[None, :, None] - c) ** 2 + (g[None, None, :] - c) ** 2).sqrt() - 20.0
+    dens = r.reshape(1, -1).repeat(n, 1)
+    dens += 0.1 * torch.randn(dens.shape, generator=gen, device=device)
+    rng = np.random.default_rng(seed)
+    sph = np.zeros((n, 4, 4), np.float32)
+    sph[:, :, :3] = 1e6
+    for i in range(n):
+        k = int(rng.integers(1, 5))
+        sph[i, :k, :3] = rng.uniform(4.0, dim - 5.0, (k, 3))
+        sph[i, :k, 3] = rng.uniform(6.0, 20.0, k)
+    return dens.reshape(-1).contiguous(), torch.from_numpy(sph).to(device)

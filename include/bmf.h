@@ -208,6 +208,31 @@ BMF_API bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_des
  * [5] mesh processing. */
 BMF_API bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms, void* stream);
 
+/* ---- differentiable extraction (no counterpart in the reference) ----
+ * With the topology fixed by the signs, Mode Q vertex placement (mass point or
+ * QEF on hermite data with grid-gradient normals, qef_simd.h:411-461) and the
+ * MeshProcessor<4> position sweeps (MeshProcessor.cpp:130-306) are smooth
+ * functions of the density samples.  A fit plan runs them for n_chunks
+ * learnable dim^3 grids packed back to back and gives the exact adjoint
+ * (discrete choices -- topology, QEF truncation pattern, mass-point fallback --
+ * held fixed).  Boundary vertices stay frozen, as in the reference. */
+typedef struct bmf_fit bmf_fit;
+/* flags of bmf_fit_create */
+#define BMF_FIT_ADJOINT_F64 1 /* QEF adjoint from an FP64 re-solve of the hermite data and eigen pairs */
+BMF_API bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t placement, int32_t iters,
+                                  int64_t vcap, int64_t icap, int32_t flags, bmf_fit** out);
+/* Positions (vcap*3) and chunk-local quad indices (icap) of all chunks, with
+ * the per-chunk table of bmf_batch_out.  h_counts (nullable) gets the totals
+ * {vertices, indices} (synchronises).  Keeps d_density's address for the
+ * backward: do not change the density between forward and backward. */
+BMF_API bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uint32_t* d_idx,
+                                   int64_t* d_chunk_info, int64_t* h_counts, void* stream);
+/* dL/d(density) (n_chunks*dim^3, overwritten) from dL/d(positions) of the
+ * last forward; d_grad_pos holds n_grad_verts * 3 floats. */
+BMF_API bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_verts, float* d_grad_density,
+                                    void* stream);
+BMF_API bmf_status bmf_fit_destroy(bmf_fit* f);
+
 #ifdef __cplusplus
 }
 #endif

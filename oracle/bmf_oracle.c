@@ -674,7 +674,8 @@ static void hermite(const float* d, int dim, int x, int y, int z, int e, float p
 }
 
 static void place_group(const float* d, int dim, int x, int y, int z, int mask, int group, int placement,
-                        float out[3]) {
+                        float out[3], int* used_qef) {
+  if (used_qef) *used_qef = 0;
   if (placement == 0) {
     out[0] = (float)x + 0.5f;
     out[1] = (float)y + 0.5f;
@@ -713,6 +714,13 @@ static void place_group(const float* d, int dim, int x, int y, int z, int mask, 
   int ok = q[0] >= (float)x && q[0] <= (float)(x + 1) && q[1] >= (float)y && q[1] <= (float)(y + 1) &&
            q[2] >= (float)z && q[2] <= (float)(z + 1);
   memcpy(out, ok ? q : mp, sizeof(q));
+  if (used_qef) *used_qef = ok;
+}
+
+int bmfo_place_q_f32(int dim, const float* density, int x, int y, int z, int mask, int group, float out[3]) {
+  int used = 0;
+  place_group(density, dim, x, y, z, mask, group, 2, out, &used);
+  return used;
 }
 
 int bmfo_extract_q(int dim, const float* density, const uint32_t* words, int placement, int64_t vcap, int64_t icap,
@@ -739,7 +747,7 @@ int bmfo_extract_q(int dim, const float* density, const uint32_t* words, int pla
             overflow = 1;
             continue;
           }
-          if (vpos) place_group(density, dim, x, y, z, m, g, placement, vpos + 3 * nv);
+          if (vpos) place_group(density, dim, x, y, z, m, g, placement, vpos + 3 * nv, NULL);
           if (vboundary) vboundary[nv] = (x == 0 || y == 0 || z == 0 || x == nc - 1 || y == nc - 1 || z == nc - 1);
           if (vvalence) vvalence[nv] = 0;
         }

@@ -75,6 +75,27 @@ void bmfo_process(int N, int64_t nverts, float* pos, float* nrm, const uint8_t* 
 float bmfo_qef_f32(const float* pos, const float* nrm, int count, float* out);
 double bmfo_qef_f64(const double* pos, const double* nrm, int count, double* out);
 
+/* Mode Q QEF placement (placement 2) of group `group` of cell (x, y, z) with
+ * cell mask `mask`, in float as bmfo_extract_q places it; returns 1 when the
+ * QEF solution was used, 0 for the mass-point fallback. */
+int bmfo_place_q_f32(int dim, const float* density, int x, int y, int z, int mask, int group, float out[3]);
+
+/* ---- FP64 differentiable path (oracle/bmf_oracle_fit.c): Mode Q + QEF
+ * placement + `iters` position sweeps + mean squared rounded-box SDF.  box =
+ * {centre xyz, half extents xyz, corner radius}.  grad_density (nullable,
+ * dim^3) receives dL/d(density) with the discrete choices held fixed;
+ * out_counts (nullable) = {vertices, quads, vertices placed by QEF};
+ * state_hash (nullable) fingerprints those discrete choices; near_branch
+ * (nullable, dim^3) flags the samples read by vertices whose branch (QEF or
+ * mass point, truncation pattern) a float32 forward may take differently. */
+double bmfo_fit_loss_f64(int dim, const double* density, int iters, const double* box, double* grad_density,
+                         int64_t* out_counts, uint64_t* state_hash, unsigned char* near_branch);
+/* The same with the loss' target a union of n_spheres spheres (rows of centre
+ * xyz, radius); the state hash also covers each vertex's nearest sphere. */
+double bmfo_fit_loss_spheres_f64(int dim, const double* density, int iters, const double* spheres, int n_spheres,
+                                 double* grad_density, int64_t* out_counts, uint64_t* state_hash,
+                                 unsigned char* near_branch);
+
 /* ---- CPU baseline driver: the whole per-chunk path for a batch of chunks,
  * OpenMP over chunks like ChunkGenerator::extract_chunk.  desc: per chunk
  * {origin.x, origin.y, origin.z, scale, dim(as float)}.  Returns total

@@ -39,6 +39,10 @@ def lib():
         L.bmfo_qef_f32.argtypes = [vp, vp, c_int, vp]
         L.bmfo_qef_f64.restype = ctypes.c_double
         L.bmfo_qef_f64.argtypes = [vp, vp, c_int, vp]
+        L.bmfo_fit_loss_f64.restype = ctypes.c_double
+        L.bmfo_fit_loss_f64.argtypes = [c_int, vp, c_int, vp, vp, vp, vp, vp]
+        L.bmfo_fit_loss_spheres_f64.restype = ctypes.c_double
+        L.bmfo_fit_loss_spheres_f64.argtypes = [c_int, vp, c_int, vp, c_int, vp, vp, vp, vp]
         L.bmfo_extract_batch.restype = i64
         L.bmfo_extract_batch.argtypes = [c_int, vp, c_int, vp, c_int, c_int, c_int, c_int, vp, c_int]
         _lib = L
@@ -150,3 +154,30 @@ def extract_batch(desc, field, params, mode=0, placement=0, iters=0, smooth_norm
     tot = lib().bmfo_extract_batch(len(desc), _p(desc), field, _p(prm), mode, placement, iters,
                                    int(smooth_normals), _p(counts), n_threads)
     return int(tot), counts
+
+
+def fit_loss_f64(dim, density, iters, box, want_grad=False, near_branch=None):
+    """FP64 differentiable path: returns (loss, grad or None, counts, state_hash).
+    near_branch (uint8 array of dim^3, optional) receives the mask of samples
+    read by vertices whose placement branch a float32 forward may take
+    differently."""
+    d = np.ascontiguousarray(density, np.float64)
+    b = np.ascontiguousarray(box, np.float64)
+    g = np.zeros(dim ** 3, np.float64) if want_grad else None
+    counts = np.zeros(3, np.int64)
+    h = ctypes.c_uint64(0)
+    loss = lib().bmfo_fit_loss_f64(dim, _p(d), iters, _p(b), _p(g), _p(counts), ctypes.byref(h), _p(near_branch))
+    return loss, g, counts, int(h.value)
+
+
+def fit_loss_spheres_f64(dim, density, iters, spheres, want_grad=False, near_branch=None):
+    """FP64 differentiable path with a sphere-union target (spheres: (k, 4) rows
+    of centre xyz, radius): returns (loss, grad or None, counts, state_hash)."""
+    d = np.ascontiguousarray(density, np.float64)
+    sp = np.ascontiguousarray(spheres, np.float64).reshape(-1, 4)
+    g = np.zeros(dim ** 3, np.float64) if want_grad else None
+    counts = np.zeros(3, np.int64)
+    h = ctypes.c_uint64(0)
+    loss = lib().bmfo_fit_loss_spheres_f64(dim, _p(d), iters, _p(sp), len(sp), _p(g), _p(counts), ctypes.byref(h),
+                                           _p(near_branch))
+    return loss, g, counts, int(h.value)

@@ -1,0 +1,187 @@
+"""The differentiable extraction on the GPU (bmf_fit_* through the C ABI and its
+torch.autograd binding) against the oracles.
+
+* forward: Mode Q topology, QEF placement and 8 boundary-frozen MeshProcessor<4>
+  sweeps -- positions and quad indices bit-identical to the float oracle
+  (bmf_oracle.c: extract_q + process);
+* backward: dL/d(density) of L = mean_v sdf_box(p_v)^2 against the FP64 adjoint
+  of oracle/bmf_oracle_fit.c (itself checked against central differences).
+  The forward is float32 (the reference's QEF).  At a vertex where it takes a
+  different branch than the FP64 forward (QEF vs mass point, an eigenvalue at
+  the 1e-3 truncation threshold) the two functions are different pieces of a
+  discontinuous map and their gradients differ by O(1): the oracle flags the
+  samples such vertices read (near_branch) and the comparison runs on the
+  rest.  Bars there: with the FP64 QEF adjoint (the default) 2e-4 relative L2
+  (the float forward's positions feed dL/dp) and 99.9% of the support's
+  entries within 1e-3 relative + 1e-4 max|g|; the FP32 adjoint, whose error is
+  1/s^2 times the ~1e-6 FP32 error of small kept eigenvalues, 1e-2 relative L2.
+  Loss within 1e-4 relative.
+* batching: a chunk's gradient in a 3-chunk batch equals its single-chunk
+  gradient up to float32 reordering of the atomics (1e-5 of max|g|);
+* batched fitting (per-chunk sphere-union targets, loss = sum of per-chunk
+  means): the loss and spot-checked chunks' gradients against the FP64 oracle
+  with the same bars;
+* fitting: 40 Adam steps on the density move the mesh towards the target.
+"""
+import numpy as np
+import pytest
+import torch
+
+from binarymeshfitting_gb300 import _lib as L
+from binarymeshfitting_gb300 import workloads
+from binarymeshfitting_gb300.engine import Context
+from binarymeshfitting_gb300.fitting import ExtractFit, FitPlan, rounded_box_sdf, sphere_union_loss
+from oracle import cpu
+
+pytestmark = pytest.mark.gpu
+
+DIM = 65
+ITERS = 8
+BOX = [32.0, 32.0, 32.0, 18.0, 14.0, 10.0, 4.0]
+
+
+def sphere_noise(seed=3, radius=20.0, sigma=0.1):
+    g = np.arange(DIM, dtype=np.float64)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    rng = np.random.default_rng(seed)
+    d = np.sqrt((X - 32) ** 2 + (Y - 32) ** 2 + (Z - 32) ** 2) - radius + rng.normal(0, sigma, X.shape)
+    return d.reshape(-1).astype(np.float32)
+
+
+def box_loss(pos, reduce="mean"):
+    b = torch.tensor(BOX, dtype=torch.float32, device=pos.device)
+    d = rounded_box_sdf(pos, b[:3], b[3:6], b[6])
+    return (d * d).mean() if reduce == "mean" else (d * d).sum()
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def test_fit_forward_bit_exact(ctx):
+    d = sphere_noise()
+    plan = FitPlan(ctx, 1, DIM, L.PLACE_QEF, ITERS)
+    pos, idx, info = plan.forward(torch.from_numpy(d).cuda())
+    words, _ = cpu.label_grid(DIM, d)
+    ref = cpu.extract_q(DIM, d, words, placement=2)
+    rpos, _ = cpu.process(4, ref["pos"], ref["boundary"], ref["valence"], ref["idx"], ITERS)
+    assert pos.shape[0] == len(rpos) and idx.numel() == len(ref["idx"])
+    assert np.array_equal(idx.cpu().numpy().view(np.uint32), ref["idx"])
+    g = pos.cpu().numpy()
+    assert np.array_equal(g.view(np.uint32), rpos.astype(np.float32).view(np.uint32)), \
+        "max |diff| %g" % np.abs(g - rpos).max()
+    inf = info.cpu().numpy()[0]
+    assert inf[0] == 0 and inf[1] == len(rpos) and inf[2] == 0 and inf[3] == len(ref["idx"])
+    plan.close()
+
+
+def gpu_grad(ctx, d, reduce="mean", adjoint_f64=True):
+    plan = FitPlan(ctx, 1, DIM, L.PLACE_QEF, ITERS, adjoint_f64=adjoint_f64)
+    dens = torch.from_numpy(d).cuda().requires_grad_(True)
+    pos = ExtractFit.apply(dens, plan)
+    loss = box_loss(pos, reduce)
+    loss.backward()
+    out = float(loss.detach()), dens.grad.double().cpu().numpy()
+    plan.close()
+    return out
+
+
+def compare_kept(g, g64, near_branch):
+    keep = near_branch == 0
+    gk = g64[keep]
+    rel_l2 = np.linalg.norm(g[keep] - gk) / np.linalg.norm(gk)
+    gmax = np.abs(gk).max()
+    sup = keep & (np.abs(g64) > 1e-6 * gmax)
+    ok = np.abs(g[sup] - g64[sup]) <= 1e-3 * np.abs(g64[sup]) + 1e-4 * gmax
+    return rel_l2, ok.mean(), keep.mean(), sup.sum()
+
+
+def test_fit_gradient_fp32_adjoint(ctx):
+    d = sphere_noise()
+    _, g = gpu_grad(ctx, d, adjoint_f64=False)
+    nb = np.zeros(DIM ** 3, np.uint8)
+    _, g64, _, _ = cpu.fit_loss_f64(DIM, d.astype(np.float64), ITERS, BOX, want_grad=True, near_branch=nb)
+    rel_l2, ok, _, _ = compare_kept(g, g64, nb)
+    print("FP32 adjoint: rel_l2 %.3g, entries within tol %.4f" % (rel_l2, ok))
+    assert rel_l2 <= 1e-2
+
+
+def test_fit_gradient_matches_fp64_adjoint(ctx):
+    d = sphere_noise()
+    loss, g = gpu_grad(ctx, d)
+    nb = np.zeros(DIM ** 3, np.uint8)
+    loss64, g64, counts, _ = cpu.fit_loss_f64(DIM, d.astype(np.float64), ITERS, BOX, want_grad=True,
+                                              near_branch=nb)
+    assert abs(loss - loss64) <= 1e-4 * abs(loss64), (loss, loss64)
+    rel_l2, ok, kept, nsup = compare_kept(g, g64, nb)
+    print("loss %.9g vs %.9g  rel_l2 %.3g  entries within tol %.5f of %d (samples kept %.4f; vertices %d, "
+          "QEF-placed %d)" % (loss, loss64, rel_l2, ok, nsup, kept, counts[0], counts[2]))
+    assert rel_l2 <= 2e-4
+    assert ok >= 0.999
+    assert kept >= 0.98
+
+
+def test_fit_batched_equals_single(ctx):
+    ds = [sphere_noise(seed=s, radius=r) for s, r in ((7, 18.0), (8, 21.0), (9, 24.0))]
+    plan = FitPlan(ctx, 3, DIM, L.PLACE_QEF, ITERS)
+    dens = torch.from_numpy(np.concatenate(ds)).cuda().requires_grad_(True)
+    pos = ExtractFit.apply(dens, plan)
+    loss = box_loss(pos, "sum")
+    loss.backward()
+    gb = dens.grad.double().cpu().numpy().reshape(3, -1)
+    info = plan.info.cpu().numpy()
+    plan.close()
+    for k, d in enumerate(ds):
+        l1, g1 = gpu_grad(ctx, d, "sum")
+        assert np.abs(gb[k] - g1).max() <= 1e-5 * np.abs(g1).max(), k
+        assert info[k, 1] > 0
+
+
+def test_fit_adam_moves_mesh_to_target(ctx):
+    d = sphere_noise(seed=12, sigma=0.0)
+    plan = FitPlan(ctx, 1, DIM, L.PLACE_QEF, 4)
+    dens = torch.from_numpy(d).cuda().requires_grad_(True)
+    opt = torch.optim.Adam([dens], lr=0.05)
+    losses = []
+    # the surface has to travel up to 10 cells; Adam moves each sample by at
+    # most ~lr per step, so 40 steps take the loss down by about a fifth
+    for _ in range(40):
+        opt.zero_grad()
+        pos = ExtractFit.apply(dens, plan)
+        loss = box_loss(pos)
+        loss.backward()
+        opt.step()
+        losses.append(float(loss.detach()))
+    print("loss %.4g -> %.4g" % (losses[0], losses[-1]))
+    assert all(np.isfinite(losses))
+    assert losses[-1] < 0.9 * losses[0]
+    assert sum(b < a for a, b in zip(losses, losses[1:])) >= 0.6 * (len(losses) - 1)
+    plan.close()
+
+
+def test_batched_fit_spheres_fp64_spot_check(ctx):
+    n = 8
+    dens, sph = workloads.fit_batch(n, dim=DIM, seed=21)
+    plan = FitPlan(ctx, n, DIM, L.PLACE_QEF, ITERS)
+    d = dens.clone().requires_grad_(True)
+    pos = ExtractFit.apply(d, plan)
+    loss = sphere_union_loss(pos, plan.info, sph)
+    loss.backward()
+    g = d.grad.double().cpu().numpy().reshape(n, -1)
+    hd = dens.cpu().numpy().astype(np.float64).reshape(n, -1)
+    hs = sph.cpu().numpy()
+    plan.close()
+    loss64 = 0.0
+    for k in range(n):
+        want = k in (0, 3, 7)
+        nb = np.zeros(DIM ** 3, np.uint8)
+        lk, gk, _, _ = cpu.fit_loss_spheres_f64(DIM, hd[k], ITERS, hs[k], want_grad=want, near_branch=nb)
+        loss64 += lk
+        if want:
+            rel_l2, ok, kept, _ = compare_kept(g[k], gk, nb)
+            print("chunk %d: rel_l2 %.3g, entries within tol %.5f, samples kept %.4f" % (k, rel_l2, ok, kept))
+            assert rel_l2 <= 2e-4 and ok >= 0.999, k
+    assert abs(float(loss) - loss64) <= 1e-4 * abs(loss64), (float(loss), loss64)
