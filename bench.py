@@ -29,7 +29,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "chunks/s (mixed-LOD batch vs per-chunk, same GB300, exact topology)"
-FP32_OPS_PER_SAMPLE = 337  # terrain FBM, 5 octaves, counted from the kernel source (see DESIGN.md)
+FP32_OPS_PER_SAMPLE = 337  # terrain FBM, 5 octaves, counted from the kernel source
+# DRAM bytes (read + write) per sample of k_sample_label from one ncu capture on
+# the 256-chunk update (110,890,368 samples, 401.31 MB): traffic grows with the
+# samples, so a full launch is scaled from it (profiles/k_sample_label_lod_update_256.txt)
+FILL_DRAM_BYTES_PER_SAMPLE = 401.31e6 / 110_890_368
 
 
 def parse():
@@ -338,7 +342,8 @@ def run_gb300(args):
     roofline = {"kernel": "k_sample_label (density FBM + occupancy words)", "bound": "fp32",
                 "achieved": fill_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fill_achieved / fp32_peak,
                 "peak_kind": "nominal 152 SM x 128 FP32 lanes x %.0f MHz (no measured FP32 peak exists)" % sm_max,
-                "traffic": None, "ms_per_launch": st_ms[0],
+                "traffic": FILL_DRAM_BYTES_PER_SAMPLE * samples, "traffic_unit": "bytes per launch (scaled ncu)",
+                "algorithmic_bytes": 4 * samples + 4 * words, "ms_per_launch": st_ms[0],
                 "flops_per_launch": FP32_OPS_PER_SAMPLE * samples,
                 "extraction_hbm": {"kernels": "count+scan+offsets+emit", "achieved": ext_gbs, "peak": hbm_peak,
                                    "unit": "GB/s", "frac": ext_gbs / hbm_peak, "bytes": ext_bytes,
