@@ -1,5 +1,6 @@
 // C ABI (include/bmf.h): context, scratch arena, per-chunk entry points and
 // the batched, CUDA-graph-captured update.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -63,6 +64,14 @@ struct bmf_batch {
   int64_t* h_pinned = nullptr;
   ChunkDev* h_stage = nullptr;       // pinned staging for bmf_batch_set_descs
   cudaEvent_t stage_done = nullptr;  // the last staging copy has been consumed
+  // terrain fill: line items {chunk, first line}, largest chunks first, and
+  // the work queue of the persistent form; fill_mode 0 = x-plane kernel,
+  // 1 = one CTA per item, 2 = persistent CTAs on the queue
+  int2* d_fill_items = nullptr;
+  int n_fill_items = 0;
+  int* d_queue = nullptr;
+  int fill_grid = 0;
+  int fill_mode = 0;
 };
 
 namespace {
@@ -490,11 +499,41 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
   if ((s = bail(cudaMemcpy(b->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice),
                 "upload units")) != BMF_OK)
     return s;
+  if (b->field.kind == BMF_FIELD_TERRAIN_FBM) {
+    // line items, largest chunks first (longest-processing-time order for the queue)
+    std::vector<int> order(n_chunks);
+    for (int i = 0; i < n_chunks; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int c) { return b->h_chunks[a].dim > b->h_chunks[c].dim; });
+    std::vector<int2> items;
+    for (int i : order) {
+      const int n_it = fill_terrain_items(b->h_chunks[i].dim);
+      for (int k = 0; k < n_it; ++k) items.push_back(make_int2(i, k * fill_terrain_lines()));
+    }
+    b->n_fill_items = (int)items.size();
+    if ((s = bail(cudaMalloc(&b->d_fill_items, sizeof(int2) * items.size()), "fill items")) != BMF_OK) return s;
+    if ((s = bail(cudaMalloc(&b->d_queue, sizeof(int)), "fill queue")) != BMF_OK) return s;
+    if ((s = bail(cudaMemcpy(b->d_fill_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice),
+                  "upload fill items")) != BMF_OK)
+      return s;
+    b->fill_grid = fill_terrain_resident_ctas();
+    b->fill_mode = 2;
+  }
   *out = b;
   return BMF_OK;
 }
 
 namespace {
+
+// Density fill + occupancy words of a whole update.
+void batch_fill(bmf_batch* b, cudaStream_t st) {
+  if (b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0)
+    launch_fill_terrain(b->d_chunks, b->d_fill_items, b->n_fill_items, b->fill_mode == 2 ? b->d_queue : nullptr,
+                        b->fill_grid, b->field, b->d_dens, b->d_words, b->d_flags, st);
+  else
+    launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
+                        b->d_words, b->d_flags, st);
+}
 
 bmf_status batch_proc_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   if (vcap <= b->proc_vcap && icap <= b->proc_icap) return BMF_OK;
@@ -526,8 +565,7 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   bmf_ctx* ctx = b->ctx;
   const bool proc = b->opts.iters > 0;
   BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
-  launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
-                      b->d_words, b->d_flags, st);
+  batch_fill(b, st);
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st);
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
@@ -646,8 +684,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   for (auto& e : ev) BMF_CUDA(ctx, cudaEventCreate(&e));
   BMF_CUDA(ctx, cudaEventRecord(ev[0], st));
   BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
-  launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
-                      b->d_words, b->d_flags, st);
+  batch_fill(b, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[1], st));
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[2], st));
@@ -836,7 +873,8 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
                   b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
-                  b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey};
+                  b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey,
+                  b->d_fill_items, b->d_queue};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);

@@ -32,9 +32,21 @@ struct WordScratch {
   uint32_t* gpl;    // Mode Q: 3 bit-planes of the per-cell vertex-group count
 };
 
+// Fill + label.  A terrain field of a single chunk goes through the line
+// kernel (k_fill_terrain) directly; batches pass their own item queue to
+// launch_fill_terrain.
 void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units, int max_dim,
                          const FieldDev& field, const float* dens_in, float* dens_out, uint32_t* words,
                          uint32_t* flags, cudaStream_t st);
+// Terrain FBM fill over line items {chunk, first line} (kFillLines lines
+// each; d_items null = chunk 0's items in order).  d_queue non-null: grid
+// persistent CTAs take items from the queue (reset here); else one CTA per item.
+void launch_fill_terrain(const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue, int grid,
+                         const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
+                         cudaStream_t st);
+int fill_terrain_items(int dim);   // items of one chunk
+int fill_terrain_lines();          // lines per item
+int fill_terrain_resident_ctas();  // persistent grid: SMs x resident CTAs per SM
 void launch_cell_masks(int dim, const uint32_t* W, uint8_t* masks, cudaStream_t st);
 // contains_mesh flags of chunks whose words were produced elsewhere.
 void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, uint32_t* flags,

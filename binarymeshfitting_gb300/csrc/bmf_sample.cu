@@ -103,6 +103,190 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
   if (lane == 0 && f) atomicOr(flags + c, f);
 }
 
+// ---------------------------------------------------------------------------
+// Terrain FBM fill over (x, y) lines: the work item is kFillLines consecutive
+// lines of one chunk (line = x * dim + y); each thread owns one line and walks
+// it in runs of kFillRun z-samples.  All threads of an item share the run's z
+// coordinates, so everything that depends on z alone -- the lattice cell Z,
+// the fraction zf, zf - 1 and fade(zf), per octave and sample -- is computed
+// once per CTA into shared memory, and the z-lattice cell changes at the same
+// sample for every lane (a warp-uniform branch).
+//
+// Between two changes of Z a corner's hash, hence its gradient, is fixed, so
+// the gradient is set up once per such segment as g = s + cz * z: for
+// v = +/-z, s = +/-u and cz = +/-1; otherwise s = (+/-u) + (+/-v) and
+// cz = -0.0 (corners at zf >= 0) or +0.0 (corners at zf - 1 < 0), which makes
+// cz * z a zero of the sign that leaves s unchanged.  Every value is
+// bit-identical to perlin()'s (+/-u) + (+/-v), including signed zeros, and
+// the per-sample gradient work moves from byte permutes on the integer pipe to
+// one multiply and one add.
+//
+// Items come from a device queue (persistent CTAs grab the next item with an
+// atomic ticket; the queue is ordered largest chunks first) or, with no queue,
+// one CTA per item.
+// ---------------------------------------------------------------------------
+constexpr int kFillRun = 8;     // divides 32: a run's inside bits land in one word
+constexpr int kFillLines = 256; // lines per item = threads per CTA
+constexpr int kMaxOctaves = 32;
+
+// Per hash h: x = u selector (x or y) | sign of u << 31; y = v selector (x or
+// y) | (v == z ? 1 : sign of v) << 31; z = 0 when v == z else all ones (keeps
+// v); w = cz bits for a corner at zf: +/-1.0f when v == z else -0.0f.
+__host__ __device__ inline uint4 seg_grad_code(int h) {
+  h &= 15;
+  const bool vz = (h & 12) != 0 && (h & 13) != 12;
+  const uint32_t sel_x = 0x3210u, sel_y = 0x7654u;
+  uint4 t;
+  t.x = ((h & 8) ? sel_y : sel_x) | ((uint32_t)(h & 1) << 31);
+  t.y = ((h & 12) == 0 ? sel_y : sel_x) | ((vz ? 1u : (uint32_t)((h >> 1) & 1)) << 31);
+  t.z = vz ? 0u : 0xFFFFFFFFu;
+  t.w = vz ? (0x3F800000u | ((uint32_t)((h >> 1) & 1) << 31)) : 0x80000000u;
+  return t;
+}
+
+// s and cz of one corner at lattice offsets (xc, yc); dz = corner at zf - 1.
+template <int DZ>
+__device__ __forceinline__ void seg_corner(uint4 t, float xc, float yc, float& s, float& cz) {
+  const uint32_t xb = __float_as_uint(xc), yb = __float_as_uint(yc);
+  const float su = __uint_as_float(__byte_perm(xb, yb, t.x) ^ (t.x & 0x80000000u));
+  const float sv = __uint_as_float((__byte_perm(xb, yb, t.y) & t.z) ^ (t.y & 0x80000000u));
+  s = su + sv;
+  cz = __uint_as_float(DZ ? (t.w & ~t.z) : t.w);
+}
+
+__global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __restrict__ chunks,
+                                                             const int2* __restrict__ items, int n_items,
+                                                             int* __restrict__ queue, FieldDev field,
+                                                             float* __restrict__ dens_out,
+                                                             uint32_t* __restrict__ words,
+                                                             uint32_t* __restrict__ flags) {
+  __shared__ int perm2[512];
+  __shared__ uint4 gtab[512];
+  __shared__ float4 zt[kMaxOctaves * kFillRun];
+  __shared__ int s_item;
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+    perm2[i] = field.perm[i & 255];
+    gtab[i] = seg_grad_code(field.perm[i & 255]);
+  }
+  const int oct = min((int)field.p[5], kMaxOctaves);
+  const float h0 = field.p[0], ampl = field.p[1], freq = field.p[2], lac = field.p[3], gain = field.p[4];
+  for (int pass = 0;; ++pass) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1) : (pass == 0 ? (int)blockIdx.x : n_items);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) break;
+    const int2 item = items ? items[it] : make_int2(0, it * kFillLines);
+    const ChunkDev ch = chunks[item.x];
+    const int dim = ch.dim, zc = ch.zc;
+    const int line = item.y + (int)threadIdx.x;
+    const bool active = line < dim * dim;
+    const int x = active ? line / dim : 0, y = active ? line - x * dim : 0;
+    const float px = ch.ox + (float)x * ch.scale, py = ch.oy + (float)y * ch.scale;
+    const int64_t dbase = ch.dens + (int64_t)line * dim;
+    uint32_t* wline = words + ch.words + (int64_t)line * zc;
+    const int nruns = (dim + kFillRun - 1) / kFillRun;
+    uint32_t wacc = 0u, fl = 0u;
+    for (int zr = 0; zr < nruns; ++zr) {
+      const int z0 = zr * kFillRun, n = min(kFillRun, dim - z0);
+      __syncthreads();
+      if ((int)threadIdx.x < oct * kFillRun) {
+        const int o = threadIdx.x / kFillRun, k = threadIdx.x % kFillRun;
+        float fr = freq;
+        for (int i = 0; i < o; ++i) fr = fr * lac;
+        const float pz = ch.oz + (float)(z0 + k) * ch.scale;
+        const float zs = pz * fr;
+        const float fz = floorf(zs);
+        const float zf = zs - fz;
+        zt[threadIdx.x] = make_float4(zf, zf - 1.0f, fade(zf), __int_as_float(((int)fz) & 255));
+      }
+      __syncthreads();
+      if (!active) continue;
+      float sum[kFillRun];
+#pragma unroll
+      for (int k = 0; k < kFillRun; ++k) sum[k] = 0.0f;
+      float amp = 1.0f, fr = freq;
+      for (int o = 0; o < oct; ++o) {
+        const float xs = px * fr, ys = py * fr;
+        const float fx = floorf(xs), fy = floorf(ys);
+        const int X = ((int)fx) & 255, Y = ((int)fy) & 255;
+        const float xf = xs - fx, yf = ys - fy;
+        const float u = fade(xf), v = fade(yf);
+        const float x1 = xf - 1.0f, y1 = yf - 1.0f;
+        const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
+        const int pA = perm2[A], pA1 = perm2[A + 1], pB = perm2[B], pB1 = perm2[B + 1];
+        float s[8], cz[8];
+        int Zp = -1;
+#pragma unroll
+        for (int k = 0; k < kFillRun; ++k) {
+          if (k >= n) break;
+          const float4 t = zt[o * kFillRun + k];
+          const int Z = __float_as_int(t.w);
+          if (Z != Zp) {  // same for every lane of the CTA
+            Zp = Z;
+            const int AA = pA + Z, AB = pA1 + Z, BA = pB + Z, BB = pB1 + Z;
+            seg_corner<0>(gtab[AA], xf, yf, s[0], cz[0]);
+            seg_corner<0>(gtab[BA], x1, yf, s[1], cz[1]);
+            seg_corner<0>(gtab[AB], xf, y1, s[2], cz[2]);
+            seg_corner<0>(gtab[BB], x1, y1, s[3], cz[3]);
+            seg_corner<1>(gtab[AA + 1], xf, yf, s[4], cz[4]);
+            seg_corner<1>(gtab[BA + 1], x1, yf, s[5], cz[5]);
+            seg_corner<1>(gtab[AB + 1], xf, y1, s[6], cz[6]);
+            seg_corner<1>(gtab[BB + 1], x1, y1, s[7], cz[7]);
+          }
+          const float zf = t.x, z1 = t.y, w = t.z;
+          const float g000 = s[0] + cz[0] * zf, g100 = s[1] + cz[1] * zf;
+          const float g010 = s[2] + cz[2] * zf, g110 = s[3] + cz[3] * zf;
+          const float g001 = s[4] + cz[4] * z1, g101 = s[5] + cz[5] * z1;
+          const float g011 = s[6] + cz[6] * z1, g111 = s[7] + cz[7] * z1;
+          const float l00 = lerp_t(u, g000, g100), l10 = lerp_t(u, g010, g110);
+          const float l01 = lerp_t(u, g001, g101), l11 = lerp_t(u, g011, g111);
+          const float l0 = lerp_t(v, l00, l10), l1 = lerp_t(v, l01, l11);
+          sum[k] = sum[k] + amp * lerp_t(w, l0, l1);
+        }
+        fr = fr * lac;
+        amp = amp * gain;
+      }
+      uint32_t bits = 0u;
+#pragma unroll
+      for (int k = 0; k < kFillRun; ++k) {
+        if (k >= n) break;
+        const float d = (py - h0) - ampl * sum[k];
+        if (dens_out) dens_out[dbase + z0 + k] = d;
+        if (d < 0.0f) bits |= 1u << k;
+      }
+      wacc |= bits << (z0 & 31);
+      if (((z0 + kFillRun) & 31) == 0 || zr == nruns - 1) {
+        wline[z0 >> 5] = wacc;
+        fl |= (wacc != 0u && wacc != kFull) ? 1u : (wacc == kFull ? 2u : 4u);
+        wacc = 0u;
+      }
+    }
+    fl = __reduce_or_sync(kFull, fl);
+    if ((threadIdx.x & 31) == 0 && fl) atomicOr(flags + item.x, fl);
+    if (!queue) break;
+  }
+}
+
+void launch_fill_terrain(const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue, int grid,
+                         const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
+                         cudaStream_t st) {
+  if (n_items <= 0) return;
+  if (d_queue) cudaMemsetAsync(d_queue, 0, sizeof(int), st);
+  k_fill_terrain<<<d_queue ? grid : n_items, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field,
+                                                                  dens_out, words, flags);
+}
+
+int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
+int fill_terrain_lines() { return kFillLines; }
+int fill_terrain_resident_ctas() {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain, kFillLines, 0);
+  return sms * (per_sm > 0 ? per_sm : 1);
+}
+
 // One byte per cell, padded rows of 32*zc cells (bmf_cell_masks).
 __global__ void k_cell_masks(int dim, int zc, const uint32_t* __restrict__ W, uint8_t* __restrict__ masks) {
   const int zp = 32 * zc;
@@ -138,6 +322,11 @@ void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* w
 void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units, int max_dim,
                          const FieldDev& field, const float* dens_in, float* dens_out, uint32_t* words,
                          uint32_t* flags, cudaStream_t st) {
+  if (field.kind == BMF_FIELD_TERRAIN_FBM && n_chunks == 1) {
+    launch_fill_terrain(d_chunks, nullptr, fill_terrain_items(max_dim), nullptr, 0, field, dens_out, words, flags,
+                        st);
+    return;
+  }
   const int max_zc = (max_dim + 31) / 32;
   const size_t smem = (size_t)max_dim * max_zc * sizeof(uint32_t);
   k_sample_label<<<n_units, 256, smem, st>>>(d_chunks, n_chunks, d_unit_start, field, dens_in, dens_out, words,
