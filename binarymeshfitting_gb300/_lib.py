@@ -71,6 +71,10 @@ class BatchOut(ctypes.Structure):
                 ("n_idx", c_int64)]
 
 
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("fill_mode", c_int32), ("fill_run", c_int32), ("sweep_block", c_int32), ("reserved", c_int32 * 5)]
+
+
 class Config(ctypes.Structure):
     _fields_ = [("device", c_int32), ("flags", c_int32), ("scratch_bytes", ctypes.c_size_t)]
 
@@ -100,6 +104,10 @@ SIGNATURES = {
     "bmf_batch_destroy": (c_int32, [c_void_p]),
     "bmf_batch_set_descs": (c_int32, [c_void_p, ctypes.POINTER(ChunkDesc), c_int32, c_void_p]),
     "bmf_batch_profile": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), ctypes.POINTER(c_float), c_void_p]),
+    "bmf_batch_get_tuning": (c_int32, [c_void_p, ctypes.POINTER(BatchTuning)]),
+    "bmf_batch_set_tuning": (c_int32, [c_void_p, ctypes.POINTER(BatchTuning)]),
+    "bmf_batch_autotune": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), c_int32, c_void_p, ctypes.POINTER(BatchTuning),
+                                     ctypes.POINTER(c_float), c_int32, ctypes.POINTER(c_int32)]),
     "bmf_fit_create": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_int64, c_int64, c_int32,
                                  ctypes.POINTER(c_void_p)]),
     "bmf_fit_forward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_int64),

@@ -72,6 +72,7 @@ struct bmf_batch {
   int* d_queue = nullptr;
   int fill_grid = 0;
   int fill_mode = 0;
+  int fill_run = 8;
 };
 
 namespace {
@@ -516,7 +517,7 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
     if ((s = bail(cudaMemcpy(b->d_fill_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice),
                   "upload fill items")) != BMF_OK)
       return s;
-    b->fill_grid = fill_terrain_resident_ctas();
+    b->fill_grid = fill_terrain_resident_ctas(b->fill_run);
     b->fill_mode = 2;
   }
   *out = b;
@@ -528,8 +529,9 @@ namespace {
 // Density fill + occupancy words of a whole update.
 void batch_fill(bmf_batch* b, cudaStream_t st) {
   if (b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0)
-    launch_fill_terrain(b->d_chunks, b->d_fill_items, b->n_fill_items, b->fill_mode == 2 ? b->d_queue : nullptr,
-                        b->fill_grid, b->field, b->d_dens, b->d_words, b->d_flags, st);
+    launch_fill_terrain(b->fill_run, b->d_chunks, b->d_fill_items, b->n_fill_items,
+                        b->fill_mode == 2 ? b->d_queue : nullptr, b->fill_grid, b->field, b->d_dens, b->d_words,
+                        b->d_flags, st);
   else
     launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
                         b->d_words, b->d_flags, st);
@@ -712,6 +714,134 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   for (int k = 0; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
   ctx->launches += 5 + pk;
+  return BMF_OK;
+}
+
+bmf_status bmf_batch_get_tuning(const bmf_batch* b, bmf_batch_tuning* t) {
+  if (!b || !t) return BMF_ERR_INVALID_ARGUMENT;
+  std::memset(t, 0, sizeof(*t));
+  t->fill_mode = b->fill_mode;
+  t->fill_run = b->fill_run;
+  t->sweep_block = b->ps.block > 0 ? b->ps.block : 256;
+  return BMF_OK;
+}
+
+bmf_status bmf_batch_set_tuning(bmf_batch* b, const bmf_batch_tuning* t) {
+  if (!b || !t) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  const bool terrain = b->field.kind == BMF_FIELD_TERRAIN_FBM;
+  if (t->fill_mode < 0 || t->fill_mode > 2 || (!terrain && t->fill_mode != 0) ||
+      (t->fill_run != 4 && t->fill_run != 8 && t->fill_run != 16) ||
+      (t->sweep_block != 128 && t->sweep_block != 256 && t->sweep_block != 512))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
+                "bmf_batch_set_tuning: fill_mode 0..2 (1, 2 for terrain fields only), fill_run 4/8/16, "
+                "sweep_block 128/256/512");
+  b->fill_mode = t->fill_mode;
+  if (t->fill_run != b->fill_run) {
+    b->fill_run = t->fill_run;
+    if (terrain) b->fill_grid = fill_terrain_resident_ctas(b->fill_run);
+  }
+  b->ps.block = t->sweep_block;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return BMF_OK;
+}
+
+namespace {
+float median_of(std::vector<float> v) {
+  std::sort(v.begin(), v.end());
+  return v.empty() ? 0.0f : v[v.size() / 2];
+}
+}  // namespace
+
+bmf_status bmf_batch_autotune(bmf_batch* b, bmf_batch_out* out, int32_t reps, void* stream, bmf_batch_tuning* chosen,
+                              float* h_ms, int32_t max_report, int32_t* n_report) {
+  if (!b) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  if (!out || !out->d_pos || !out->d_idx || reps <= 0)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_autotune: output arena and reps > 0 required");
+  cudaStream_t st = (cudaStream_t)stream;
+  bmf_status s;
+  bmf_batch_tuning best;
+  if ((s = bmf_batch_get_tuning(b, &best)) != BMF_OK) return s;
+  std::vector<float> report;
+  cudaEvent_t e0, e1;
+  BMF_CUDA(ctx, cudaEventCreate(&e0));
+  BMF_CUDA(ctx, cudaEventCreate(&e1));
+  auto time_it = [&](auto&& enqueue, float* ms) -> bmf_status {
+    std::vector<float> t;
+    enqueue();  // warm-up
+    for (int r = 0; r < reps; ++r) {
+      BMF_CUDA(ctx, cudaEventRecord(e0, st));
+      enqueue();
+      BMF_CUDA(ctx, cudaEventRecord(e1, st));
+      BMF_CUDA(ctx, cudaEventSynchronize(e1));
+      BMF_CUDA(ctx, cudaPeekAtLastError());
+      float v = 0.0f;
+      BMF_CUDA(ctx, cudaEventElapsedTime(&v, e0, e1));
+      t.push_back(v);
+    }
+    *ms = median_of(t);
+    return BMF_OK;
+  };
+  // stage 1: density fill + labels
+  if (b->field.kind == BMF_FIELD_TERRAIN_FBM) {
+    const int cand[7][2] = {{0, 8}, {1, 4}, {1, 8}, {1, 16}, {2, 4}, {2, 8}, {2, 16}};
+    float best_ms = 1e30f;
+    for (const auto& c : cand) {
+      bmf_batch_tuning t = best;
+      t.fill_mode = c[0];
+      t.fill_run = c[1];
+      if ((s = bmf_batch_set_tuning(b, &t)) != BMF_OK) return s;
+      float ms = 0.0f;
+      s = time_it([&] {
+        cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st);
+        batch_fill(b, st);
+      }, &ms);
+      if (s != BMF_OK) return s;
+      report.push_back(ms);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best.fill_mode = c[0];
+        best.fill_run = c[1];
+      }
+    }
+    if ((s = bmf_batch_set_tuning(b, &best)) != BMF_OK) return s;
+  }
+  // stage 2: the sweeps, on the mesh of one real update
+  if (b->opts.iters > 0) {
+    if ((s = bmf_batch_run(b, out, 0, 1, stream)) != BMF_OK) return s;
+    const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
+    const StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
+    const int blocks[3] = {128, 256, 512};
+    float best_ms = 1e30f;
+    for (int bs : blocks) {
+      b->ps.block = bs;
+      float ms = 0.0f;
+      s = time_it([&] {
+        launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary,
+                       b->d_valence, b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals,
+                       b->ps, &sa, st);
+      }, &ms);
+      if (s != BMF_OK) return s;
+      report.push_back(ms);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best.sweep_block = bs;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if ((s = bmf_batch_set_tuning(b, &best)) != BMF_OK) return s;
+  // leave a correct update in `out`
+  if ((s = bmf_batch_run(b, out, 0, 1, stream)) != BMF_OK) return s;
+  if (chosen) *chosen = best;
+  if (n_report) *n_report = (int32_t)report.size();
+  if (h_ms)
+    for (int i = 0; i < (int)report.size() && i < max_report; ++i) h_ms[i] = report[i];
   return BMF_OK;
 }
 

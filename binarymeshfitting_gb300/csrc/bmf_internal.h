@@ -41,12 +41,13 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
 // Terrain FBM fill over line items {chunk, first line} (kFillLines lines
 // each; d_items null = chunk 0's items in order).  d_queue non-null: grid
 // persistent CTAs take items from the queue (reset here); else one CTA per item.
-void launch_fill_terrain(const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue, int grid,
-                         const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
+// run = z-samples per step (4, 8 or 16).
+void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,
+                         int grid, const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
                          cudaStream_t st);
-int fill_terrain_items(int dim);   // items of one chunk
-int fill_terrain_lines();          // lines per item
-int fill_terrain_resident_ctas();  // persistent grid: SMs x resident CTAs per SM
+int fill_terrain_items(int dim);          // items of one chunk
+int fill_terrain_lines();                 // lines per item
+int fill_terrain_resident_ctas(int run);  // persistent grid: SMs x resident CTAs per SM
 void launch_cell_masks(int dim, const uint32_t* W, uint8_t* masks, cudaStream_t st);
 // contains_mesh flags of chunks whose words were produced elsewhere.
 void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, uint32_t* flags,
@@ -73,6 +74,7 @@ struct ProcessScratch {
   float* dual_p;      // 3 * n_prims
   float* dual_n;      // 3 * n_prims
   uint32_t* tmp;      // scan scratch (block totals)
+  int block;          // threads per CTA of the dual / primal sweeps (0 = 256)
 };
 // nv / n_prims size the grids; when d_counts is given the actual vertex and
 // index counts are read from d_counts[0] / d_counts[1] on the device (so the

@@ -358,7 +358,9 @@ int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, 
   int launched = 3;
   // CSR offsets: exclusive scan of init_valence (MeshProcessor.cpp:32-40)
   launch_exclusive_scan_u8_to_u32(valence, s.off, nv, d_counts, s.tmp, st);
-  const int vb = (int)((nv + 255) / 256), pb = (int)((n_prims + 255) / 256);
+  const int tb = s.block > 0 ? s.block : 256;
+  const int vb = (int)((nv + 255) / 256);
+  const int vbt = (int)((nv + tb - 1) / tb), pbt = (int)((n_prims + tb - 1) / tb);
   const uint32_t* cursor = nullptr;
   if (sa) {
     launch_adj_build(sa->mode, sa->chunks, sa->n_chunks, sa->words, sa->ws, sa->vkey, s.off, d_counts, nv, s.adj, st);
@@ -377,13 +379,13 @@ int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, 
   for (int m = 0; m < iters; ++m) {
     const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
     if (N == 3)
-      k_dual<3><<<pb, 256, 0, st>>>(n_prims, nv, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
+      k_dual<3><<<pbt, tb, 0, st>>>(n_prims, nv, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
     else
-      k_dual<4><<<pb, 256, 0, st>>>(n_prims, nv, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
+      k_dual<4><<<pbt, tb, 0, st>>>(n_prims, nv, d_counts, idx, pos, nrm, s.dual_p, s.dual_n, normal_mode);
     // primal after every dual step but the last (MeshProcessor.cpp:229-232),
     // and once more after the loop with set_colors false (ChunkGenerator.cpp:120)
     const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
-    k_primal<<<vb, 256, 0, st>>>(nv, n_prims, n_slots, d_counts, s.off, cursor, valence, s.adj, boundary, s.dual_p,
+    k_primal<<<vbt, tb, 0, st>>>(nv, n_prims, n_slots, d_counts, s.off, cursor, valence, s.adj, boundary, s.dual_p,
                                  s.dual_n, pos, nrm, process_boundary, sn ? 1 : 0, set_colors);
     launched += 2;
   }

@@ -125,9 +125,11 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
 // atomic ticket; the queue is ordered largest chunks first) or, with no queue,
 // one CTA per item.
 // ---------------------------------------------------------------------------
-constexpr int kFillRun = 8;     // divides 32: a run's inside bits land in one word
+// RUN (z-samples per step; 4, 8 or 16, dividing 32 so that a run's inside
+// bits land in one word) is the tile height the batch autotuner picks.
 constexpr int kFillLines = 256; // lines per item = threads per CTA
 constexpr int kMaxOctaves = 32;
+constexpr int kMaxFillRun = 16;
 
 // Per hash h: x = u selector (x or y) | sign of u << 31; y = v selector (x or
 // y) | (v == z ? 1 : sign of v) << 31; z = 0 when v == z else all ones (keeps
@@ -154,6 +156,7 @@ __device__ __forceinline__ void seg_corner(uint4 t, float xc, float yc, float& s
   cz = __uint_as_float(DZ ? (t.w & ~t.z) : t.w);
 }
 
+template <int kFillRun>
 __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __restrict__ chunks,
                                                              const int2* __restrict__ items, int n_items,
                                                              int* __restrict__ queue, FieldDev field,
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
                                                              uint32_t* __restrict__ flags) {
   __shared__ int perm2[512];
   __shared__ uint4 gtab[512];
-  __shared__ float4 zt[kMaxOctaves * kFillRun];
+  __shared__ float4 zt[kMaxOctaves * kMaxFillRun];
   __shared__ int s_item;
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
     perm2[i] = field.perm[i & 255];
@@ -268,22 +271,32 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
   }
 }
 
-void launch_fill_terrain(const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue, int grid,
-                         const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
+void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,
+                         int grid, const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
                          cudaStream_t st) {
   if (n_items <= 0) return;
   if (d_queue) cudaMemsetAsync(d_queue, 0, sizeof(int), st);
-  k_fill_terrain<<<d_queue ? grid : n_items, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field,
-                                                                  dens_out, words, flags);
+  const int g = d_queue ? grid : n_items;
+  if (run == 4)
+    k_fill_terrain<4><<<g, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+  else if (run == 16)
+    k_fill_terrain<16><<<g, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+  else
+    k_fill_terrain<8><<<g, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
 }
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
 int fill_terrain_lines() { return kFillLines; }
-int fill_terrain_resident_ctas() {
+int fill_terrain_resident_ctas(int run) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain, kFillLines, 0);
+  if (run == 4)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4>, kFillLines, 0);
+  else if (run == 16)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16>, kFillLines, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8>, kFillLines, 0);
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 
@@ -323,7 +336,7 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
                          const FieldDev& field, const float* dens_in, float* dens_out, uint32_t* words,
                          uint32_t* flags, cudaStream_t st) {
   if (field.kind == BMF_FIELD_TERRAIN_FBM && n_chunks == 1) {
-    launch_fill_terrain(d_chunks, nullptr, fill_terrain_items(max_dim), nullptr, 0, field, dens_out, words, flags,
+    launch_fill_terrain(8, d_chunks, nullptr, fill_terrain_items(max_dim), nullptr, 0, field, dens_out, words, flags,
                         st);
     return;
   }

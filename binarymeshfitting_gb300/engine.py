@@ -216,6 +216,34 @@ class Batch:
         self.ctx._check(self.ctx.lib.bmf_batch_profile(self.h, ctypes.byref(self.out), ms, _stream(stream)))
         return list(ms)
 
+    def tuning(self):
+        """The plan's launch tuning as a dict (bmf_batch_tuning)."""
+        t = L.BatchTuning()
+        self.ctx._check(self.ctx.lib.bmf_batch_get_tuning(self.h, ctypes.byref(t)))
+        return dict(fill_mode=t.fill_mode, fill_run=t.fill_run, sweep_block=t.sweep_block)
+
+    def set_tuning(self, fill_mode=None, fill_run=None, sweep_block=None):
+        t = L.BatchTuning()
+        self.ctx._check(self.ctx.lib.bmf_batch_get_tuning(self.h, ctypes.byref(t)))
+        if fill_mode is not None:
+            t.fill_mode = fill_mode
+        if fill_run is not None:
+            t.fill_run = fill_run
+        if sweep_block is not None:
+            t.sweep_block = sweep_block
+        self.ctx._check(self.ctx.lib.bmf_batch_set_tuning(self.h, ctypes.byref(t)))
+
+    def autotune(self, reps=3, stream=None):
+        """Runs the plan's autotuner on the allocated arena; returns (chosen
+        tuning dict, median ms per candidate)."""
+        t = L.BatchTuning()
+        ms = (ctypes.c_float * 16)()
+        n = ctypes.c_int32(0)
+        self.ctx._check(self.ctx.lib.bmf_batch_autotune(self.h, ctypes.byref(self.out), reps, _stream(stream),
+                                                        ctypes.byref(t), ms, 16, ctypes.byref(n)))
+        return (dict(fill_mode=t.fill_mode, fill_run=t.fill_run, sweep_block=t.sweep_block),
+                [float(ms[i]) for i in range(min(n.value, 16))])
+
     def chunk_mesh(self, i):
         """Views of chunk i's vertices and (chunk-local) indices in the arena."""
         info = self.bufs["info"][i].tolist()

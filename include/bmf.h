@@ -208,6 +208,28 @@ BMF_API bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_des
  * [5] mesh processing. */
 BMF_API bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms, void* stream);
 
+/* ---- launch tuning of a batch plan (no counterpart in the reference) ----
+ * The knobs that change only speed, never results. */
+typedef struct {
+  int32_t fill_mode;   /* terrain fill: 0 x-plane kernel, 1 one CTA per line item, 2 persistent CTAs taking
+                          line items (largest chunks first) from a device work queue */
+  int32_t fill_run;    /* line kernel tile height: z-samples per thread step, 4, 8 or 16 */
+  int32_t sweep_block; /* threads per CTA of the dual / primal sweeps: 128, 256 or 512 */
+  int32_t reserved[5];
+} bmf_batch_tuning;
+BMF_API bmf_status bmf_batch_get_tuning(const bmf_batch* b, bmf_batch_tuning* t);
+/* Invalidates the captured graph (the next graph run captures again). */
+BMF_API bmf_status bmf_batch_set_tuning(bmf_batch* b, const bmf_batch_tuning* t);
+/* Autotuner: times every fill candidate (terrain fields) and every sweep block
+ * size (iters > 0) on this plan and output arena, `reps` runs each (median of
+ * CUDA-event times on `stream`), keeps the fastest of each stage and returns
+ * the choice in *chosen (nullable).  h_ms (nullable) receives the median
+ * times in candidate order (fill candidates, then sweep candidates), at most
+ * max_report of them; *n_report (nullable) their count.  Synchronises; on
+ * return `out` holds a correct update made with the chosen tuning. */
+BMF_API bmf_status bmf_batch_autotune(bmf_batch* b, bmf_batch_out* out, int32_t reps, void* stream,
+                                      bmf_batch_tuning* chosen, float* h_ms, int32_t max_report, int32_t* n_report);
+
 /* ---- differentiable extraction (no counterpart in the reference) ----
  * With the topology fixed by the signs, Mode Q vertex placement (mass point or
  * QEF on hermite data with grid-gradient normals, qef_simd.h:411-461) and the

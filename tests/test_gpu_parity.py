@@ -84,6 +84,25 @@ def test_field_fill_bit_exact(ctx, kind, params, dim, origin, scale):
     assert_float_exact(g, o, "density")
 
 
+@pytest.mark.parametrize("dim", [2, 3, 17, 32, 129])
+@pytest.mark.parametrize("octaves", [0, 1, 5, 7])
+def test_terrain_fill_line_kernel_sizes(ctx, dim, octaves):
+    """The line-mapped terrain kernel: ragged runs, word ends, octave counts."""
+    params = list(workloads.TERRAIN_PARAMS)
+    params[5] = octaves
+    desc = L.ChunkDesc.make((37.0, -20.0, 1000.25), 2.0, dim)
+    field = L.Field.make(L.FIELD_TERRAIN_FBM, params)
+    g = ctx.sample_block(desc, field).cpu().numpy()
+    o = cpu.fill_field(L.FIELD_TERRAIN_FBM, params, dim, (37.0, -20.0, 1000.25), 2.0)
+    assert_float_exact(g, o, "density")
+    ow, ocm = cpu.label_grid(dim, o)
+    for want_density in (True, False):
+        dens, words, cm = ctx.sample_label(desc, field, want_density=want_density)
+        if want_density:
+            assert_float_exact(dens.cpu().numpy(), o, "density")
+        assert np.array_equal(np_u32(words), ow) and cm == bool(ocm)
+
+
 @pytest.mark.parametrize("case", ALL, ids=[c["name"] for c in ALL])
 def test_label_masks_mode_r(ctx, case):
     dim = case["dim"]
@@ -244,6 +263,37 @@ def test_batch_matches_oracle_per_chunk(ctx, mode, placement, iters, use_graph):
         np.testing.assert_array_equal(got["boundary"].cpu().numpy(), O["boundary"])
         tot_v += len(op)
     assert tot_v == nv
+    b.close()
+
+
+def test_batch_tunings_give_identical_results(ctx):
+    """Every launch tuning (fill kernel form, tile height, sweep block) changes
+    speed only: the whole arena is bit-identical to the default's."""
+    from binarymeshfitting_gb300.engine import Batch
+    descs, rows = _small_batch()
+    b = Batch(ctx, descs, workloads.terrain_field(), mode=L.MODE_R, iters=4, smooth_normals=True)
+    bufs = b.allocate(400000, 2400000, normals=True)
+    assert b.tuning() == dict(fill_mode=2, fill_run=8, sweep_block=256)
+    nv, ni = b.run(use_graph=True)
+    ref = [bufs[k][:n].clone() for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"].clone()]
+    for fm, fr, sb in [(0, 8, 256), (1, 4, 128), (1, 16, 512), (2, 4, 256), (2, 16, 128), (1, 8, 512)]:
+        b.set_tuning(fill_mode=fm, fill_run=fr, sweep_block=sb)
+        for use_graph in (False, True):
+            assert b.run(use_graph=use_graph) == (nv, ni)
+            got = [bufs[k][:n] for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"]]
+            for r, g_ in zip(ref, got):
+                assert torch.equal(r.view(torch.int32) if r.is_floating_point() else r,
+                                   g_.view(torch.int32) if g_.is_floating_point() else g_), (fm, fr, sb)
+    chosen, ms = b.autotune(reps=2)
+    assert len(ms) == 10 and all(m > 0 for m in ms)
+    assert chosen["fill_mode"] in (0, 1, 2) and chosen["sweep_block"] in (128, 256, 512)
+    assert b.tuning() == chosen
+    got = [bufs[k][:n] for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"]]
+    for r, g_ in zip(ref, got):
+        assert torch.equal(r.view(torch.int32) if r.is_floating_point() else r,
+                           g_.view(torch.int32) if g_.is_floating_point() else g_)
+    with pytest.raises(L.BmfError):
+        b.set_tuning(fill_run=5)
     b.close()
 
 

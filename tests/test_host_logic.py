@@ -37,3 +37,4 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.ExtractOpts) == 24
     assert ctypes.sizeof(_lib.Mesh) == 80
     assert ctypes.sizeof(_lib.BatchOut) == 72
+    assert ctypes.sizeof(_lib.BatchTuning) == 32
