@@ -191,8 +191,8 @@ bmf_status extract_core(bmf_ctx* ctx, int mode, int placement, ChunkDev* d_chunk
   BMF_LAUNCHED(ctx, 1);
   launch_chunk_offsets(d_chunks, n_chunks, tot, d_flags, mo.vcap, mo.icap, d_info, d_totals, st);
   BMF_LAUNCHED(ctx, 1);
-  launch_emit(mode, placement, d_chunks, n_chunks, d_units, n_units, d_words, d_dens, d_flags, ws, mo, st);
-  BMF_LAUNCHED(ctx, 1);
+  BMF_LAUNCHED(ctx, launch_emit(mode, placement, d_chunks, n_chunks, d_units, n_units, d_words, d_dens, d_flags, ws,
+                                mo, d_totals, st));
   return BMF_OK;
 }
 
@@ -358,6 +358,9 @@ bmf_status bmf_polygonize(bmf_ctx* ctx, int32_t dim, const float* d_density, con
   launch_word_flags(d_c, 1, d_words, d_flags, st);
   BMF_LAUNCHED(ctx, 1);
   MeshOut mo{out->d_pos, out->d_nrm, out->d_boundary, out->d_valence, out->d_idx, nullptr, out->vcap, out->icap};
+  if (mode == BMF_MODE_Q && placement == BMF_PLACE_QEF &&
+      (s = scratch(ctx, S_VKEY, (size_t)out->vcap + 1, &mo.vkey)) != BMF_OK)
+    return s;
   if ((s = extract_core(ctx, mode, placement, d_c, 1, d_u, dim, d_words, d_density, d_flags,
                         (int64_t)dim * dim * c.zc, mo, nullptr, d_totals, st)) != BMF_OK)
     return s;
@@ -414,7 +417,9 @@ bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf
   launch_sample_label(d_c, 1, d_u, dim, dim, fd, nullptr, d_dens, d_words, d_flags, st);
   BMF_LAUNCHED(ctx, 1);
   MeshOut mo{out->d_pos, out->d_nrm, out->d_boundary, out->d_valence, out->d_idx, nullptr, out->vcap, out->icap};
-  if (opts->iters > 0 && (s = scratch(ctx, S_VKEY, (size_t)out->vcap + 1, &mo.vkey)) != BMF_OK) return s;
+  if ((opts->iters > 0 || (opts->mode == BMF_MODE_Q && opts->placement == BMF_PLACE_QEF)) &&
+      (s = scratch(ctx, S_VKEY, (size_t)out->vcap + 1, &mo.vkey)) != BMF_OK)
+    return s;
   WordScratch ws{};
   if ((s = extract_core(ctx, opts->mode, opts->placement, d_c, 1, d_u, dim, d_words, d_dens, d_flags,
                         (int64_t)dim * dim * c.zc, mo, nullptr, d_totals, st, &ws)) != BMF_OK)
@@ -526,6 +531,11 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
 
 namespace {
 
+// Vertex keys are kept for the sweeps' adjacency and for per-vertex QEF placement.
+bool batch_keys(const bmf_batch* b) {
+  return b->opts.iters > 0 || (b->opts.mode == BMF_MODE_Q && b->opts.placement == BMF_PLACE_QEF);
+}
+
 // Density fill + occupancy words of a whole update.
 void batch_fill(bmf_batch* b, cudaStream_t st) {
   if (b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0)
@@ -573,10 +583,9 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
-             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, proc ? b->d_vkey : nullptr};
-  launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_dens,
-              b->d_flags, b->ws, mo, st);
-  int64_t k = 5;
+             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, batch_keys(b) ? b->d_vkey : nullptr};
+  int64_t k = 4 + launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units,
+                              b->d_words, b->d_dens, b->d_flags, b->ws, mo, b->d_totals, st);
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
     const StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
@@ -605,7 +614,7 @@ bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, in
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_run: output arena needs d_pos and d_idx");
   cudaStream_t st = (cudaStream_t)stream;
   bmf_status s;
-  if (b->opts.iters > 0 && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
+  if (batch_keys(b) && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
   if (use_graph) {
     if (!b->exec || !same_out(b->graph_out, *out)) {
       if (b->exec) {
@@ -681,7 +690,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   cudaStream_t st = (cudaStream_t)stream;
   bmf_status s;
   const bool proc = b->opts.iters > 0;
-  if (proc && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
+  if (batch_keys(b) && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
   cudaEvent_t ev[7];
   for (auto& e : ev) BMF_CUDA(ctx, cudaEventCreate(&e));
   BMF_CUDA(ctx, cudaEventRecord(ev[0], st));
@@ -696,9 +705,9 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
                        b->d_totals, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[4], st));
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
-             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, proc ? b->d_vkey : nullptr};
-  launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_dens,
-              b->d_flags, b->ws, mo, st);
+             out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, batch_keys(b) ? b->d_vkey : nullptr};
+  const int ek = launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words,
+                             b->d_dens, b->d_flags, b->ws, mo, b->d_totals, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[5], st));
   int pk = 0;
   if (proc) {
@@ -713,7 +722,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   BMF_CUDA(ctx, cudaPeekAtLastError());
   for (int k = 0; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
-  ctx->launches += 5 + pk;
+  ctx->launches += 4 + ek + pk;
   return BMF_OK;
 }
 
@@ -863,6 +872,7 @@ struct bmf_fit {
   uint32_t *d_idxg = nullptr, *d_vkey = nullptr;
   uint8_t *d_valence = nullptr, *d_boundary = nullptr;
   float* d_g = nullptr;           // position-gradient work buffer
+  uint32_t* d_qlist = nullptr;    // QEF-placed vertices of the FP64 backward (+ counter at [vcap])
   const float* last_density = nullptr;
   int64_t* h_pinned = nullptr;
 };
@@ -873,7 +883,7 @@ bmf_status bmf_fit_destroy(bmf_fit* f) {
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   void* ptrs[] = {f->d_chunks, f->d_units, f->d_flags, f->d_tot, f->d_words, f->d_totals, f->ws.vcnt, f->ws.icnt,
                   f->ws.gpl, f->ps.off, f->ps.cursor, f->ps.adj, f->ps.dual_p, f->ps.dual_n, f->ps.tmp, f->d_idxg,
-                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g};
+                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (f->h_pinned) cudaFreeHost(f->h_pinned);
@@ -931,6 +941,7 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
             cudaMalloc(&f->d_vkey, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
             cudaMalloc(&f->d_valence, vcap + 1) == cudaSuccess && cudaMalloc(&f->d_boundary, vcap + 1) == cudaSuccess &&
             cudaMalloc(&f->d_g, sizeof(float) * 3 * (vcap + 1)) == cudaSuccess &&
+            cudaMalloc(&f->d_qlist, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
             cudaMallocHost(&f->h_pinned, sizeof(int64_t) * 4) == cudaSuccess &&
             cudaMemcpy(f->d_chunks, hc.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(f->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -957,9 +968,8 @@ bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uin
   launch_scan_chunks(f->d_chunks, f->n, f->ws, f->d_tot, st);
   launch_chunk_offsets(f->d_chunks, f->n, f->d_tot, f->d_flags, f->vcap, f->icap, d_chunk_info, f->d_totals, st);
   MeshOut mo{d_pos, nullptr, f->d_boundary, f->d_valence, d_idx, f->d_idxg, f->vcap, f->icap, f->d_vkey};
-  launch_emit(BMF_MODE_Q, f->placement, f->d_chunks, f->n, f->d_units, f->n * f->dim, f->d_words, d_density,
-              f->d_flags, f->ws, mo, st);
-  int k = 5;
+  int k = 4 + launch_emit(BMF_MODE_Q, f->placement, f->d_chunks, f->n, f->d_units, f->n * f->dim, f->d_words,
+                          d_density, f->d_flags, f->ws, mo, f->d_totals, st);
   if (f->iters > 0) {
     const StructuredAdj sa{BMF_MODE_Q, f->d_chunks, f->n, f->d_words, f->ws, f->d_vkey};
     k += launch_process(4, f->vcap, f->icap / 4, f->d_totals, d_pos, nullptr, f->d_boundary, f->d_valence, f->d_idxg,
@@ -992,9 +1002,10 @@ bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_
   int k = launch_process_bwd(4, f->vcap, f->icap / 4, f->d_totals, f->d_boundary, f->d_valence, f->d_idxg, f->iters,
                              0, f->ps, f->d_g, st);
   BMF_CUDA(ctx, cudaMemsetAsync(d_grad_density, 0, sizeof(float) * (size_t)f->n * f->dim * f->dim * f->dim, st));
-  launch_place_bwd(f->placement, (f->flags & BMF_FIT_ADJOINT_F64) != 0, f->d_chunks, f->n, f->d_words,
-                   f->last_density, f->d_vkey, f->d_totals, f->vcap, f->d_g, d_grad_density, st);
-  BMF_LAUNCHED(ctx, k + 1);
+  const bool f64 = (f->flags & BMF_FIT_ADJOINT_F64) != 0;
+  launch_place_bwd(f->placement, f64, f->d_chunks, f->n, f->d_words, f->last_density, f->d_vkey, f->d_totals,
+                   f->vcap, f->d_g, d_grad_density, f->d_qlist, f->d_qlist + f->vcap, st);
+  BMF_LAUNCHED(ctx, k + (f64 && f->placement == BMF_PLACE_QEF ? 2 : 1));
   return BMF_OK;
 }
 

@@ -745,11 +745,16 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
         for (int g = 0; g < ng; ++g, ++vid) {
           const int64_t gv = ch.vout + vid;
           if (gv >= out.vcap) continue;
-          float P[3];
-          q_place<PLACE>(D, dim, x, y, z, mask, g, P);
-          out.pos[3 * gv] = P[0];
-          out.pos[3 * gv + 1] = P[1];
-          out.pos[3 * gv + 2] = P[2];
+          // QEF positions come from k_place_qef (thread per vertex) when the
+          // vertex keys are kept; only here on the few lanes of surface cells
+          // otherwise
+          if (PLACE != 2 || !out.vkey) {
+            float P[3];
+            q_place<PLACE>(D, dim, x, y, z, mask, g, P);
+            out.pos[3 * gv] = P[0];
+            out.pos[3 * gv + 1] = P[1];
+            out.pos[3 * gv + 2] = P[2];
+          }
           if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
           if (out.boundary) out.boundary[gv] = bnd;
           if (out.vkey) out.vkey[gv] = ((uint32_t)(((int64_t)x * dim + y) * dim + z) << 2) | (uint32_t)g;
@@ -962,13 +967,20 @@ __device__ void eig3_refine(const double A[3][3], const float V0[3][3], double w
   for (int i = 0; i < 3; ++i) w[i] = B[i][i];
 }
 
-template <int PLACE, typename T>
+// LIST = 0: every vertex; 1: every vertex, but QEF-placed ones are only
+// appended to qlist (for a dense second pass); 2: the vertices of qlist.
+template <int PLACE, typename T, int LIST>
 __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ chunks, int n_chunks,
                                                    const uint32_t* __restrict__ words, const float* __restrict__ dens,
                                                    const uint32_t* __restrict__ vkey,
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
-                                                   const float* __restrict__ grad_pos, float* __restrict__ grad_dens) {
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                                   const float* __restrict__ grad_pos, float* __restrict__ grad_dens,
+                                                   uint32_t* __restrict__ qlist, uint32_t* __restrict__ qcount) {
+  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (LIST == 2) {
+    if (v >= (int64_t)*qcount) return;
+    v = qlist[v];
+  }
   if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
   const int c = find_chunk_by_vertex(chunks, n_chunks, v);
   const ChunkDev ch = chunks[c];
@@ -1001,6 +1013,10 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
     if (q.solve(s, &info))
       use_qef = s[0] >= (float)x && s[0] <= (float)(x + 1) && s[1] >= (float)y && s[1] <= (float)(y + 1) &&
                 s[2] >= (float)z && s[2] <= (float)(z + 1);
+    if (LIST == 1 && use_qef) {
+      qlist[atomicAdd(qcount, 1u)] = (uint32_t)v;
+      return;
+    }
     if (use_qef) {
       if (sizeof(T) == sizeof(float)) {
 #pragma unroll
@@ -1166,15 +1182,22 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
 
 void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
-                      const float* grad_pos, float* grad_dens, cudaStream_t st) {
+                      const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount, cudaStream_t st) {
   const int blocks = (int)((vcap + 127) / 128);
   if (blocks == 0) return;
-#define BMF_PLACE_BWD(P, T) \
-  k_place_bwd<P, T><<<blocks, 128, 0, st>>>(d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos, grad_dens)
-  if (placement == 2) {
-    if (f64) BMF_PLACE_BWD(2, double); else BMF_PLACE_BWD(2, float);
+#define BMF_PLACE_BWD(P, T, L)                                                                                     \
+  k_place_bwd<P, T, L><<<blocks, 128, 0, st>>>(d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos, \
+                                               grad_dens, qlist, qcount)
+  if (placement == 2 && f64 && qlist && qcount) {
+    // float pass for the mass-point vertices, then the FP64 QEF adjoint over
+    // the compacted list of QEF-placed ones (no idle lanes in FP64 code)
+    cudaMemsetAsync(qcount, 0, sizeof(uint32_t), st);
+    BMF_PLACE_BWD(2, float, 1);
+    BMF_PLACE_BWD(2, double, 2);
+  } else if (placement == 2) {
+    if (f64) BMF_PLACE_BWD(2, double, 0); else BMF_PLACE_BWD(2, float, 0);
   } else {
-    BMF_PLACE_BWD(1, float);
+    BMF_PLACE_BWD(1, float, 0);
   }
 #undef BMF_PLACE_BWD
 }
@@ -1295,9 +1318,33 @@ void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_to
   k_chunk_offsets<<<1, 1024, 0, st>>>(d_chunks, n_chunks, d_tot, flags, vcap, icap, d_info, d_totals);
 }
 
-void launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start,
-                 int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
-                 MeshOut out, cudaStream_t st) {
+// Mode Q QEF placement, one thread per vertex (dense lanes, unlike the
+// warp-per-word emit where only surface cells' lanes work): the same
+// q_place<2> on the vertex's cell and group, decoded from its key.
+__global__ void __launch_bounds__(128) k_place_qef(const ChunkDev* __restrict__ chunks, int n_chunks,
+                                                   const uint32_t* __restrict__ words, const float* __restrict__ dens,
+                                                   const uint32_t* __restrict__ vkey,
+                                                   const int64_t* __restrict__ d_counts, int64_t vcap,
+                                                   float* __restrict__ pos) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= min(vcap, d_counts[0])) return;
+  const int c = find_chunk_by_vertex(chunks, n_chunks, v);
+  const ChunkDev ch = chunks[c];
+  const int dim = ch.dim;
+  const uint32_t key = vkey[v];
+  const int lin = (int)(key >> 2), g = (int)(key & 3u);
+  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+  const int mask = cell_mask_at(words + ch.words, dim, ch.zc, x, y, z);
+  float P[3];
+  q_place<2>(dens + ch.dens, dim, x, y, z, mask, g, P);
+  pos[3 * v] = P[0];
+  pos[3 * v + 1] = P[1];
+  pos[3 * v + 2] = P[2];
+}
+
+int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start,
+                int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
+                MeshOut out, const int64_t* d_counts, cudaStream_t st) {
   if (mode == 0) {
     k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else if (placement == 0) {
@@ -1305,8 +1352,15 @@ void launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks
   } else if (placement == 1) {
     k_emit<1, 1><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else {
+    if (!out.vkey || !d_counts) out.vkey = nullptr;  // no keys: the emit places in place
     k_emit<1, 2><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
+    if (out.vkey && out.vcap > 0) {
+      k_place_qef<<<(int)((out.vcap + 127) / 128), 128, 0, st>>>(d_chunks, n_chunks, words, dens, out.vkey, d_counts,
+                                                                out.vcap, out.pos);
+      return 2;
+    }
   }
+  return 1;
 }
 
 }  // namespace bmf

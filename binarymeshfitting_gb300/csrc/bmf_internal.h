@@ -62,9 +62,11 @@ void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, 
 // per-chunk info table {voff, vcount, ioff, icount, contains_mesh, status}.
 void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_tot, const uint32_t* flags,
                           int64_t vcap, int64_t icap, int64_t* d_info, int64_t* d_totals, cudaStream_t st);
-void launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start,
-                 int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
-                 MeshOut out, cudaStream_t st);
+// Returns the kernels launched: Mode Q QEF placement with vertex keys and
+// d_counts (total vertices on the device) adds the per-vertex k_place_qef.
+int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start,
+                int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
+                MeshOut out, const int64_t* d_counts, cudaStream_t st);
 
 // MeshProcessor: operates on one flat mesh (vertices [0, nv), prims of N).
 struct ProcessScratch {
@@ -109,9 +111,12 @@ int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_coun
 // Adjoint of Mode Q placement (placement 1 mass point, 2 QEF; f64: the QEF
 // derivative from an FP64 re-solve); accumulates into grad_dens (the caller
 // clears it).
+// qlist (vcap entries) + qcount: scratch of the two-pass FP64 form (nullable:
+// one pass, idle lanes in the FP64 code).
 void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
-                      const float* grad_pos, float* grad_dens, cudaStream_t st);
+                      const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount,
+                      cudaStream_t st);
 void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n, const int64_t* d_n,
                                      uint32_t* block_tmp, cudaStream_t st);
 

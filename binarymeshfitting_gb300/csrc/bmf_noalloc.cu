@@ -104,7 +104,7 @@ extern "C" bmf_status bmf_polygonize_noalloc(int32_t dim, const float* d_density
   launch_scan_chunks(d_c, 1, ws, d_tot, st);
   launch_chunk_offsets(d_c, 1, d_tot, d_flags, out->vcap, out->icap, nullptr, d_totals, st);
   MeshOut mo{out->d_pos, out->d_nrm, out->d_boundary, out->d_valence, out->d_idx, nullptr, out->vcap, out->icap};
-  launch_emit(mode, placement, d_c, 1, d_u, dim, d_words, d_density, d_flags, ws, mo, st);
+  launch_emit(mode, placement, d_c, 1, d_u, dim, d_words, d_density, d_flags, ws, mo, nullptr, st);
   if (cudaPeekAtLastError() != cudaSuccess) return BMF_ERR_CUDA;
   int64_t totals[2] = {0, 0};
   uint32_t flags = 0;
