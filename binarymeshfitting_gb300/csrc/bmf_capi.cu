@@ -16,7 +16,7 @@ namespace {
 
 enum Slot {
   S_CHUNKS, S_UNITS, S_FLAGS, S_TOT, S_INFO, S_TOTALS, S_WORDS, S_DENS, S_VCNT, S_ICNT, S_GPL,
-  S_OFF, S_CURSOR, S_ADJ, S_DUALP, S_DUALN, S_SCANTMP, S_VKEY, S_NUM
+  S_OFF, S_CURSOR, S_ADJ, S_DUALP, S_DUALN, S_SCANTMP, S_VKEY, S_CLIST, S_NUM
 };
 
 constexpr int kMaxDim = 512;
@@ -73,6 +73,9 @@ struct bmf_batch {
   int fill_grid = 0;
   int fill_mode = 0;
   int fill_run = 8;
+  // Mode R work list, sized by the output capacity (vcap + icap / 3 + 1)
+  uint2* d_clist = nullptr;
+  int64_t clist_cap = 0;
 };
 
 namespace {
@@ -184,6 +187,14 @@ bmf_status extract_core(bmf_ctx* ctx, int mode, int placement, ChunkDev* d_chunk
   if ((s = scratch(ctx, S_ICNT, (size_t)words_total, &ws.icnt)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_GPL, (size_t)words_total * 3, &ws.gpl)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_TOT, (size_t)n_chunks * 2, &tot)) != BMF_OK) return s;
+  if (mode == BMF_MODE_R) {
+    // work list of active cells: each one owns a vertex or emits a triangle
+    ws.clist_cap = mo.vcap + mo.icap / 3 + 1;
+    uint2* list;
+    if ((s = scratch(ctx, S_CLIST, (size_t)ws.clist_cap + 1, &list)) != BMF_OK) return s;
+    ws.clist = list;
+    ws.ccount = (uint32_t*)(list + ws.clist_cap);
+  }
   if (ws_out) *ws_out = ws;
   launch_count(mode, d_chunks, n_chunks, d_units, n_units, d_words, d_flags, ws, st);
   BMF_LAUNCHED(ctx, 1);
@@ -531,6 +542,23 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
 
 namespace {
 
+// The Mode R work list for an output arena of (vcap, icap) (+ its counter).
+bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
+  if (b->opts.mode != BMF_MODE_R) return BMF_OK;
+  const int64_t cap = vcap + icap / 3 + 1;
+  if (cap > b->clist_cap) {
+    if (b->d_clist) cudaFree(b->d_clist);
+    b->d_clist = nullptr;
+    b->clist_cap = 0;
+    BMF_CUDA(b->ctx, cudaMalloc(&b->d_clist, sizeof(uint2) * (cap + 1)));
+    b->clist_cap = cap;
+  }
+  b->ws.clist = b->d_clist;
+  b->ws.ccount = (uint32_t*)(b->d_clist + b->clist_cap);
+  b->ws.clist_cap = b->clist_cap;
+  return BMF_OK;
+}
+
 // Vertex keys are kept for the sweeps' adjacency and for per-vertex QEF placement.
 bool batch_keys(const bmf_batch* b) {
   return b->opts.iters > 0 || (b->opts.mode == BMF_MODE_Q && b->opts.placement == BMF_PLACE_QEF);
@@ -615,6 +643,7 @@ bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, in
   cudaStream_t st = (cudaStream_t)stream;
   bmf_status s;
   if (batch_keys(b) && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
+  if ((s = batch_list_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
   if (use_graph) {
     if (!b->exec || !same_out(b->graph_out, *out)) {
       if (b->exec) {
@@ -691,6 +720,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   bmf_status s;
   const bool proc = b->opts.iters > 0;
   if (batch_keys(b) && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
+  if ((s = batch_list_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
   cudaEvent_t ev[7];
   for (auto& e : ev) BMF_CUDA(ctx, cudaEventCreate(&e));
   BMF_CUDA(ctx, cudaEventRecord(ev[0], st));
@@ -1015,7 +1045,7 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
                   b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
                   b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey,
-                  b->d_fill_items, b->d_queue};
+                  b->d_fill_items, b->d_queue, b->d_clist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);

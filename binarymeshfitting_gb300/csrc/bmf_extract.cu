@@ -125,9 +125,16 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
   const bool cm = contains_mesh(__ldg(flags + c));
   __shared__ int s_busy[kWordBlock];
   __shared__ int s_nbusy;
+  __shared__ uint32_t s_act[kWordBlock];  // Mode R work list: active cells of each busy word
+  __shared__ uint32_t s_apos[kWordBlock];
+  __shared__ uint32_t s_acnt, s_abase;
+  const bool listing = MODE == 0 && ws.clist != nullptr;
   for (int base = 0; base < nw; base += kWordBlock) {
     // level 1: one thread per word; quiet words get zero counts right away
-    if (threadIdx.x == 0) s_nbusy = 0;
+    if (threadIdx.x == 0) {
+      s_nbusy = 0;
+      s_acnt = 0;
+    }
     __syncthreads();
     if (base + (int)threadIdx.x < nw) {
       const int wi = base + threadIdx.x;
@@ -159,6 +166,13 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
       vc = __popc(X) + __popc(Y) + __popc(Z);
       const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
       const int nt = interior ? tri_count(lw.mask(lane)) : 0;
+      if (listing) {
+        const uint32_t act = __ballot_sync(kFull, nt != 0 || (((X | Y | Z) >> lane) & 1u));
+        if (lane == 0) {
+          s_act[li] = act;
+          s_apos[li] = act ? atomicAdd(&s_acnt, (uint32_t)__popc(act)) : 0u;
+        }
+      }
       int t = 3 * nt;
       // bit-planes of the per-cell triangle count (0..5): a cell's first
       // primitive is ibase + 3 * (popc(p0 & lt) + 2 popc(p1 & lt) + 4 popc(p2 & lt))
@@ -188,6 +202,22 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
     }
     }
     __syncthreads();
+    if (listing) {
+      // one global reservation per block of words, then each busy word's
+      // active cells in lane order
+      if (threadIdx.x == 0) s_abase = s_acnt ? atomicAdd(ws.ccount, s_acnt) : 0u;
+      __syncthreads();
+      for (int li = warp; li < nbusy; li += nwarps) {
+        const uint32_t act = s_act[li];
+        if (!((act >> lane) & 1u)) continue;
+        const int wi = s_busy[li];
+        const int y = wi / zc, zb = wi - y * zc;
+        const int64_t slot = (int64_t)s_abase + s_apos[li] + __popc(act & lane_lt(lane));
+        if (slot < ws.clist_cap)
+          ws.clist[slot] = make_uint2((uint32_t)c, (uint32_t)(((int64_t)x * dim + y) * dim + 32 * zb + lane));
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -1305,6 +1335,7 @@ void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const ui
 
 void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
                   const uint32_t* words, const uint32_t* flags, WordScratch ws, cudaStream_t st) {
+  if (mode == 0 && ws.clist) cudaMemsetAsync(ws.ccount, 0, sizeof(uint32_t), st);
   if (mode == 0) k_count<0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
   else k_count<1><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
 }
@@ -1316,6 +1347,92 @@ void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, 
 void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_tot, const uint32_t* flags,
                           int64_t vcap, int64_t icap, int64_t* d_info, int64_t* d_totals, cudaStream_t st) {
   k_chunk_offsets<<<1, 1024, 0, st>>>(d_chunks, n_chunks, d_tot, flags, vcap, icap, d_info, d_totals);
+}
+
+// Mode R emission over the work list, one thread per active cell (the
+// warp-per-word form runs most lanes idle: a busy word holds a few surface
+// cells).  Per cell it writes exactly what k_emit<0,0> writes for the cell's
+// lane: its owned vertices (ids from the scanned word base and the crossing
+// words, calculate_isovertex positions, boundary, key, init_valence) and its
+// triangles (slot from the word's index base and the triangle-count planes).
+__global__ void __launch_bounds__(256) k_emit_cells_r(const ChunkDev* __restrict__ chunks,
+                                                      const uint32_t* __restrict__ words,
+                                                      const float* __restrict__ dens, WordScratch ws, MeshOut out) {
+  const int64_t n = min((int64_t)*ws.ccount, ws.clist_cap);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint2 ent = ws.clist[i];
+    const ChunkDev ch = chunks[ent.x];
+    const int dim = ch.dim, zc = ch.zc;
+    const int lin = (int)ent.y;
+    const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+    const int zb = z >> 5, lane = z & 31;
+    const uint32_t lt = lane_lt(lane);
+    const uint32_t* W = words + ch.words;
+    const uint32_t* vbase = ws.vcnt + ch.words;
+    const float* D = dens + ch.dens;
+    const int64_t wo = ((int64_t)x * dim + y) * zc + zb;
+    const uint32_t w00 = word_at(W, dim, zc, x, y, zb);
+    const uint32_t X = (x + 1 < dim) ? (w00 ^ word_at(W, dim, zc, x + 1, y, zb)) : 0u;
+    const uint32_t Y = (y + 1 < dim) ? (w00 ^ word_at(W, dim, zc, x, y + 1, zb)) : 0u;
+    const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
+    const uint32_t own = ((X >> lane) & 1u) | (((Y >> lane) & 1u) << 1) | (((Z >> lane) & 1u) << 2);
+    if (own) {
+      uint32_t vid = __ldg(vbase + wo) + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
+      for (int a = 0; a < 3; ++a) {
+        if (!((own >> a) & 1u)) continue;
+        const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+        const int64_t gv = ch.vout + vid;
+        ++vid;
+        if (gv >= out.vcap) continue;
+        const float s0 = dens_at(D, dim, x, y, z), s1 = dens_at(D, dim, x1, y1, z1);
+        const float mu = (0.0f - s0) / (s1 - s0);
+        const float q0[3] = {(float)x, (float)y, (float)z};
+        const float dl[3] = {(float)(x1 - x), (float)(y1 - y), (float)(z1 - z)};
+        float* P = out.pos + 3 * gv;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float dv = dl[k] * mu;
+          P[k] = dv + q0[k];
+        }
+        if (out.boundary)
+          out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
+                              x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
+        if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
+        if (out.vkey) out.vkey[gv] = ((uint32_t)lin << 2) | (uint32_t)a;
+        if (out.valence) {
+          int val = 0;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int d1 = k >> 1, d2 = k & 1;
+            int cx = x, cy = y, cz = z, e;
+            if (a == 0) { cy -= d1; cz -= d2; e = 2 * d1 + d2; }
+            else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
+            else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
+            if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
+            val += edge_uses(cell_mask_at(W, dim, zc, cx, cy, cz), e);
+          }
+          out.valence[gv] = (uint8_t)val;
+        }
+      }
+    }
+    const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
+    const int mask = interior ? cell_mask_at(W, dim, zc, x, y, z) : 0;
+    const uint64_t tw = c_tri_cases[mask];
+    const int t3 = 3 * (int)(tw >> 60);
+    if (t3 == 0) continue;
+    const uint32_t* pl = ws.gpl + 3 * (ch.words + wo);
+    const int before = __popc(__ldg(pl) & lt) + 2 * __popc(__ldg(pl + 1) & lt) + 4 * __popc(__ldg(pl + 2) & lt);
+    int64_t gi = ch.iout + (int64_t)__ldg(ws.icnt + ch.words + wo) + 3 * before;
+    for (int k = 0; k < t3; ++k, ++gi) {
+      const int e = tri_edge(tw, k);
+      const uint32_t vid = r_vertex_id(W, vbase, dim, zc, x + c_edge_owner[e][0], y + c_edge_owner[e][1],
+                                       z + c_edge_owner[e][2], c_edge_owner[e][3]);
+      if (gi < out.icap) {
+        out.idx[gi] = vid;
+        if (out.idx_global) out.idx_global[gi] = (uint32_t)(ch.vout + vid);
+      }
+    }
+  }
 }
 
 // Mode Q QEF placement, one thread per vertex (dense lanes, unlike the
@@ -1345,7 +1462,12 @@ __global__ void __launch_bounds__(128) k_place_qef(const ChunkDev* __restrict__ 
 int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start,
                 int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
                 MeshOut out, const int64_t* d_counts, cudaStream_t st) {
-  if (mode == 0) {
+  if (mode == 0 && ws.clist) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_emit_cells_r<<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+  } else if (mode == 0) {
     k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else if (placement == 0) {
     k_emit<1, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);

@@ -29,7 +29,13 @@ struct MeshOut {
 struct WordScratch {
   uint32_t* vcnt;   // vertices hosted by the word's 32 cells; scanned in place to the chunk-local base
   uint32_t* icnt;   // indices emitted by the word's cells; scanned in place
-  uint32_t* gpl;    // Mode Q: 3 bit-planes of the per-cell vertex-group count
+  uint32_t* gpl;    // 3 bit-planes of the per-cell triangle (Mode R) / vertex-group (Mode Q) count
+  // Mode R work list (nullable): every cell that owns a vertex or emits a
+  // triangle, as {chunk, (x*dim + y)*dim + z}, in no particular order;
+  // *ccount (zeroed before the count kernel) entries, at most clist_cap kept.
+  uint2* clist;
+  uint32_t* ccount;
+  int64_t clist_cap;
 };
 
 // Fill + label.  A terrain field of a single chunk goes through the line
