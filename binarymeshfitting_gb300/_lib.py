@@ -71,6 +71,13 @@ class BatchOut(ctypes.Structure):
                 ("n_idx", c_int64)]
 
 
+class LodParams(ctypes.Structure):
+    _fields_ = [("root_pos", c_float * 3), ("root_size", c_float), ("focus", c_float * 3),
+                ("split_multiplier", c_float), ("size_modifier", c_float), ("min_level", c_int32),
+                ("max_level", c_int32), ("dim", c_int32), ("base_overlap", c_float),
+                ("boundary_processing", c_int32), ("iters", c_int32)]
+
+
 class BatchTuning(ctypes.Structure):
     _fields_ = [("fill_mode", c_int32), ("fill_run", c_int32), ("sweep_block", c_int32), ("reserved", c_int32 * 5)]
 
@@ -104,6 +111,11 @@ SIGNATURES = {
     "bmf_batch_destroy": (c_int32, [c_void_p]),
     "bmf_batch_set_descs": (c_int32, [c_void_p, ctypes.POINTER(ChunkDesc), c_int32, c_void_p]),
     "bmf_batch_profile": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), ctypes.POINTER(c_float), c_void_p]),
+    "bmf_lod_generate": (c_int32, [c_void_p, ctypes.POINTER(LodParams), c_void_p, c_int32, c_void_p, c_void_p]),
+    "bmf_format": (c_int32, [c_void_p, ctypes.POINTER(Mesh), c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64,
+                             ctypes.POINTER(c_int64), c_void_p]),
+    "bmf_batch_format": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                   c_int64, c_void_p]),
     "bmf_batch_get_tuning": (c_int32, [c_void_p, ctypes.POINTER(BatchTuning)]),
     "bmf_batch_set_tuning": (c_int32, [c_void_p, ctypes.POINTER(BatchTuning)]),
     "bmf_batch_autotune": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), c_int32, c_void_p, ctypes.POINTER(BatchTuning),

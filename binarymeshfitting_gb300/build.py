@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libbmf_gb300.so")
-SOURCES = ["bmf_sample.cu", "bmf_extract.cu", "bmf_process.cu", "bmf_capi.cu", "bmf_noalloc.cu"]
+SOURCES = ["bmf_sample.cu", "bmf_extract.cu", "bmf_process.cu", "bmf_capi.cu", "bmf_noalloc.cu", "bmf_lod.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "-I" + os.path.join(HERE, "..")]

@@ -16,7 +16,7 @@ namespace {
 
 enum Slot {
   S_CHUNKS, S_UNITS, S_FLAGS, S_TOT, S_INFO, S_TOTALS, S_WORDS, S_DENS, S_VCNT, S_ICNT, S_GPL,
-  S_OFF, S_CURSOR, S_ADJ, S_DUALP, S_DUALN, S_SCANTMP, S_VKEY, S_CLIST, S_NUM
+  S_OFF, S_CURSOR, S_ADJ, S_DUALP, S_DUALN, S_SCANTMP, S_VKEY, S_CLIST, S_LOD, S_NUM
 };
 
 constexpr int kMaxDim = 512;
@@ -398,6 +398,44 @@ bmf_status bmf_process(bmf_ctx* ctx, bmf_mesh* mesh, int32_t iters, int32_t proc
   return process_mesh(ctx, mesh, iters, process_boundary, smooth_normals, (cudaStream_t)stream);
 }
 
+bmf_status bmf_lod_generate(bmf_ctx* ctx, const bmf_lod_params* p, bmf_chunk_desc* d_descs, int32_t cap,
+                            int32_t* d_count, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  if (!p || !d_descs || !d_count || cap <= 0 || cap > kLodMaxLeaves || p->max_level < 0 || p->max_level > 20 ||
+      p->min_level < 0 || !dim_ok(p->dim) || !(p->root_size > 0.0f))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
+                "bmf_lod_generate: params, device outputs, 0 < cap <= 16384, max_level <= 20 and a valid dim needed");
+  char* scr;
+  bmf_status s;
+  if ((s = scratch(ctx, S_LOD, lod_scratch_bytes(cap), &scr)) != BMF_OK) return s;
+  BMF_LAUNCHED(ctx, lod_generate(*p, d_descs, cap, d_count, scr, (cudaStream_t)stream));
+  return BMF_OK;
+}
+
+bmf_status bmf_format(bmf_ctx* ctx, const bmf_mesh* mesh, int32_t unwind, int32_t smooth_normals, float* d_p,
+                      float* d_n, float* d_c, int64_t cap, int64_t* h_count, void* stream) {
+  if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
+  if (!mesh || !mesh->d_pos || !d_p || !d_n || !d_c || cap < 0 || mesh->n_verts < 0 || mesh->n_idx < 0 ||
+      (unwind && (mesh->prim_size != 4 || !mesh->d_idx)) || (unwind && smooth_normals && !mesh->d_nrm))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
+                "bmf_format: mesh and output buffers required; unwinding needs quads (prim_size 4) and, with "
+                "smooth_normals, vertex normals");
+  const int64_t count = unwind ? mesh->n_idx / 4 * 4 : mesh->n_verts;
+  if (count > cap) {
+    if (h_count) *h_count = count;
+    return fail(ctx, BMF_ERR_CAPACITY, "bmf_format: output capacity exceeded (needed count reported)");
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  BMF_LAUNCHED(ctx, launch_format(nullptr, 1, mesh->n_verts, mesh->n_idx, nullptr, mesh->d_pos, mesh->d_nrm,
+                                  mesh->d_idx, unwind, smooth_normals, d_p, d_n, d_c, cap, st));
+  BMF_CUDA(ctx, cudaPeekAtLastError());
+  if (h_count) {
+    BMF_CUDA(ctx, cudaStreamSynchronize(st));
+    *h_count = count;
+  }
+  return BMF_OK;
+}
+
 bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field,
                              const bmf_extract_opts* opts, bmf_mesh* out, void* stream) {
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
@@ -753,6 +791,22 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   for (int k = 0; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
   ctx->launches += 4 + ek + pk;
+  return BMF_OK;
+}
+
+bmf_status bmf_batch_format(bmf_batch* b, const bmf_batch_out* out, int32_t unwind, int32_t smooth_normals,
+                            float* d_p, float* d_n, float* d_c, int64_t cap, void* stream) {
+  if (!b) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
+  if (!out || !out->d_pos || !out->d_idx || !d_p || !d_n || !d_c || cap < 0 || (unwind && N != 4) ||
+      (unwind && smooth_normals && !out->d_nrm))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
+                "bmf_batch_format: output buffers required; unwinding needs quads (Mode Q) and, with "
+                "smooth_normals, vertex normals");
+  BMF_LAUNCHED(ctx, launch_format(b->d_chunks, b->n, out->vcap, out->icap, b->d_totals, out->d_pos, out->d_nrm,
+                                  out->d_idx, unwind, smooth_normals, d_p, d_n, d_c, cap, (cudaStream_t)stream));
+  BMF_CUDA(ctx, cudaPeekAtLastError());
   return BMF_OK;
 }
 

@@ -23,6 +23,11 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
 static __constant__ uint64_t c_tri_cases[256] = BMF_TRI_CASES_INIT;
 static __constant__ uint64_t c_group_cases[256] = BMF_GROUP_CASES_INIT;
 static __constant__ uint64_t c_edge_uses[256] = BMF_EDGE_USES_INIT;
+// Global-memory copies for staging into shared memory with coalesced loads
+// (thread-indexed constant loads would serialise).
+static __device__ uint64_t g_tri_cases[256] = BMF_TRI_CASES_INIT;
+static __device__ uint64_t g_group_cases[256] = BMF_GROUP_CASES_INIT;
+static __device__ uint64_t g_edge_uses[256] = BMF_EDGE_USES_INIT;
 
 __device__ __forceinline__ int tri_count(int mask) { return (int)(c_tri_cases[mask] >> 60); }
 __device__ __forceinline__ int tri_edge(uint64_t w, int i) { return (int)((w >> (4 * i)) & 0xF); }

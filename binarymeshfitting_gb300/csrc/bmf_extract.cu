@@ -67,6 +67,23 @@ struct LineWords {
 
 constexpr int kWordBlock = 256;  // threads per CTA of the count / emit kernels
 
+// The case tables staged in shared memory: per-lane lookups with different
+// masks serialise on the constant cache, not on shared memory.
+struct SmemTabs {
+  uint64_t tri[256];
+  uint64_t uses[256];
+  uint64_t grp[256];
+};
+__device__ __forceinline__ void load_tabs(SmemTabs& t) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    t.tri[i] = __ldg(g_tri_cases + i);
+    t.uses[i] = __ldg(g_edge_uses + i);
+    t.grp[i] = __ldg(g_group_cases + i);
+  }
+  __syncthreads();
+}
+__device__ __forceinline__ int tab_uses(const SmemTabs& t, int mask, int e) { return (int)((t.uses[mask] >> (4 * e)) & 0xF); }
+
 // A word is quiet when its 32 cells can neither own a crossing nor have a
 // mixed corner mask: the four line words around it are identical, so are the
 // four next-block words, and the line has no z-crossing.  Then X = Y = Z = 0
@@ -123,6 +140,8 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t* W = words + ch.words;
   const bool cm = contains_mesh(__ldg(flags + c));
+  __shared__ SmemTabs T;
+  load_tabs(T);
   __shared__ int s_busy[kWordBlock];
   __shared__ int s_nbusy;
   __shared__ uint32_t s_act[kWordBlock];  // Mode R work list: active cells of each busy word
@@ -165,7 +184,7 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
       const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
       vc = __popc(X) + __popc(Y) + __popc(Z);
       const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
-      const int nt = interior ? tri_count(lw.mask(lane)) : 0;
+      const int nt = interior ? (int)(T.tri[lw.mask(lane)] >> 60) : 0;
       if (listing) {
         const uint32_t act = __ballot_sync(kFull, nt != 0 || (((X | Y | Z) >> lane) & 1u));
         if (lane == 0) {
@@ -187,7 +206,7 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
       ic = (uint32_t)t;
     } else {
       const bool interior = x <= dim - 2 && y <= dim - 2 && z <= dim - 2;
-      const int ng = interior ? group_count(lw.mask(lane)) : 0;
+      const int ng = interior ? (int)((T.grp[lw.mask(lane)] >> 48) & 0xF) : 0;
       const uint32_t g0 = __ballot_sync(kFull, ng & 1), g1 = __ballot_sync(kFull, ng & 2),
                      g2 = __ballot_sync(kFull, ng & 4);
       vc = __popc(g0) + 2 * __popc(g1) + 4 * __popc(g2);
@@ -1258,6 +1277,8 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
                                                    const uint32_t* __restrict__ vkey, const uint32_t* __restrict__ off,
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
                                                    uint32_t* __restrict__ adj) {
+  __shared__ SmemTabs T;
+  load_tabs(T);
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
   const int c = find_chunk_by_vertex(chunks, n_chunks, v);
@@ -1285,8 +1306,8 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
       else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
       if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
       const int m = cell_mask_at(W, dim, zc, cx, cy, cz);
-      if (!edge_uses(m, e)) continue;
-      const uint64_t tw = c_tri_cases[m];
+      if (!tab_uses(T, m, e)) continue;
+      const uint64_t tw = T.tri[m];
       const int nt = (int)(tw >> 60);
       const int64_t wi = ((int64_t)cx * dim + cy) * zc + (cz >> 5);
       const uint32_t lt = lane_lt(cz & 31);
@@ -1301,8 +1322,9 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
     const int g = k;
     const int m = cell_mask_at(W, dim, zc, x, y, z);
     uint32_t ids[12];
+    const uint64_t gw = T.grp[m];
     for (int e = 0; e < 12; ++e) {
-      if (group_of(m, e) != g) continue;
+      if ((int)((gw >> (4 * e)) & 0xF) != g) continue;
       const int c0 = edge_c0(e), a = e >> 2;
       const int sx = x + ((c0 >> 2) & 1), sy = y + ((c0 >> 1) & 1), sz = z + (c0 & 1);
       if (!q_edge_interior(dim, sx, sy, sz, a)) continue;
@@ -1358,6 +1380,8 @@ void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_to
 __global__ void __launch_bounds__(256) k_emit_cells_r(const ChunkDev* __restrict__ chunks,
                                                       const uint32_t* __restrict__ words,
                                                       const float* __restrict__ dens, WordScratch ws, MeshOut out) {
+  __shared__ SmemTabs T;
+  load_tabs(T);
   const int64_t n = min((int64_t)*ws.ccount, ws.clist_cap);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const uint2 ent = ws.clist[i];
@@ -1409,7 +1433,7 @@ __global__ void __launch_bounds__(256) k_emit_cells_r(const ChunkDev* __restrict
             else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
             else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
             if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
-            val += edge_uses(cell_mask_at(W, dim, zc, cx, cy, cz), e);
+            val += tab_uses(T, cell_mask_at(W, dim, zc, cx, cy, cz), e);
           }
           out.valence[gv] = (uint8_t)val;
         }
@@ -1417,7 +1441,7 @@ __global__ void __launch_bounds__(256) k_emit_cells_r(const ChunkDev* __restrict
     }
     const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
     const int mask = interior ? cell_mask_at(W, dim, zc, x, y, z) : 0;
-    const uint64_t tw = c_tri_cases[mask];
+    const uint64_t tw = T.tri[mask];
     const int t3 = 3 * (int)(tw >> 60);
     if (t3 == 0) continue;
     const uint32_t* pl = ws.gpl + 3 * (ch.words + wo);

@@ -1,6 +1,7 @@
 // Host-side declarations shared by the library's translation units.
 #pragma once
 
+#include "../../include/bmf.h"
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -108,6 +109,17 @@ int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, 
                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,
                    int process_boundary, int smooth_normals, ProcessScratch s, const StructuredAdj* sa,
                    cudaStream_t st);
+// Device-side LOD descriptor generation (bmf_lod.cu).  cap <= kLodMaxLeaves.
+constexpr int kLodMaxLeaves = 16384;
+size_t lod_scratch_bytes(int cap);
+int lod_generate(const bmf_lod_params& p, bmf_chunk_desc* d_descs, int cap, int32_t* d_count, void* scratch,
+                 cudaStream_t st);
+// GLChunk::format_data: per-vertex p/n/c (unwind 0) or unwound quads with
+// one normal each (unwind 1); d_chunks non-null resolves chunk-local indices
+// of a batch arena.  Returns the kernels launched.
+int launch_format(const ChunkDev* d_chunks, int n_chunks, int64_t nv, int64_t ni, const int64_t* d_counts,
+                  const float* pos, const float* nrm, const uint32_t* idx, int unwind, int smooth, float* p, float* n,
+                  float* c, int64_t cap, cudaStream_t st);
 // Adjoint of the position sweeps of launch_process (needs its CSR in s.off /
 // s.adj; uses s.dual_p as scratch).  g holds dL/d(final positions) on entry and
 // dL/d(initial positions) on return.  Returns the number of kernels launched.

@@ -273,6 +273,117 @@ __global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int6
 }
 
 // ---------------------------------------------------------------------------
+// Draw layout (GLChunk::format_data, GLChunk.cpp:278-335): per-vertex p/n/c,
+// or quads unwound to 4 vertices sharing one normal.  Colours are white: the
+// vertex colour is (1, 1, 1) at creation (DMCChunk.cpp:681) and the sweeps
+// only average it.  Counts come from d_counts (vertices, indices) when given.
+// ---------------------------------------------------------------------------
+__global__ void k_format_verts(int64_t nv, const int64_t* __restrict__ d_counts, int64_t cap,
+                               const float* __restrict__ pos, const float* __restrict__ nrm, float* __restrict__ p,
+                               float* __restrict__ n, float* __restrict__ c) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= min(cap, d_counts ? min(nv, d_counts[0]) : nv)) return;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    p[3 * v + k] = __ldg(pos + 3 * v + k);
+    n[3 * v + k] = nrm ? __ldg(nrm + 3 * v + k) : 0.0f;
+    c[3 * v + k] = 1.0f;
+  }
+}
+
+// chunks (nullable): quad slots are arena positions and indices chunk-local;
+// a quad's chunk is the last one whose index offset is <= its first slot.
+__global__ void k_format_quads(const ChunkDev* __restrict__ chunks, int n_chunks, int64_t ni,
+                               const int64_t* __restrict__ d_counts, int64_t cap, const float* __restrict__ pos,
+                               const float* __restrict__ nrm, const uint32_t* __restrict__ idx, int smooth,
+                               float* __restrict__ p, float* __restrict__ n, float* __restrict__ c) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nidx = d_counts ? min(ni, d_counts[1]) : ni;
+  const int64_t i = 4 * q;
+  if (i + 3 >= nidx || i + 3 >= cap) return;
+  int64_t vo = 0, nvb = d_counts ? d_counts[0] : INT64_MAX;
+  if (chunks) {
+    int lo = 0, hi = n_chunks - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (chunks[mid].iout <= i) lo = mid; else hi = mid - 1;
+    }
+    vo = chunks[lo].vout;
+  }
+  int64_t v[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = vo + (int64_t)__ldg(idx + i + k);
+    if (v[k] >= nvb) v[k] = 0;  // an index outside the mesh reads vertex 0 instead of faulting
+  }
+  float P[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) P[k][d] = __ldg(pos + 3 * v[k] + d);
+  }
+  float m[3];
+  if (smooth) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      float s = __ldg(nrm + 3 * v[0] + d) + __ldg(nrm + 3 * v[1] + d);
+      s = s + __ldg(nrm + 3 * v[2] + d);
+      s = s + __ldg(nrm + 3 * v[3] + d);
+      m[d] = s * 0.25f;
+    }
+  } else {
+    float a[3], b[3], na[3], nb[3], m0[3], m1[3], h[3], o[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      a[d] = P[0][d] - P[1][d];
+      b[d] = P[0][d] - P[2][d];
+    }
+    nrm3(a, na);
+    nrm3(b, nb);
+    cross3(na, nb, m0);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      a[d] = P[2][d] - P[3][d];
+      b[d] = P[2][d] - P[0][d];
+    }
+    nrm3(a, na);
+    nrm3(b, nb);
+    cross3(na, nb, m1);
+    if (isnan(m0[0])) { m0[0] = m1[0]; m0[1] = m1[1]; m0[2] = m1[2]; }
+    if (isnan(m1[0])) { m1[0] = m0[0]; m1[1] = m0[1]; m1[2] = m0[2]; }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) h[d] = (m0[d] + m1[d]) * 0.5f;
+    nrm3(h, o);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) m[d] = -o[d];
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      p[3 * (i + k) + d] = P[k][d];
+      n[3 * (i + k) + d] = m[d];
+      c[3 * (i + k) + d] = 1.0f;
+    }
+  }
+}
+
+int launch_format(const ChunkDev* d_chunks, int n_chunks, int64_t nv, int64_t ni, const int64_t* d_counts,
+                  const float* pos, const float* nrm, const uint32_t* idx, int unwind, int smooth, float* p, float* n,
+                  float* c, int64_t cap, cudaStream_t st) {
+  if (!unwind) {
+    if (nv <= 0) return 0;
+    k_format_verts<<<(int)((nv + 255) / 256), 256, 0, st>>>(nv, d_counts, cap, pos, nrm, p, n, c);
+  } else {
+    const int64_t nq = ni / 4;
+    if (nq <= 0) return 0;
+    k_format_quads<<<(int)((nq + 255) / 256), 256, 0, st>>>(d_chunks, n_chunks, ni, d_counts, cap, pos, nrm, idx,
+                                                            smooth, p, n, c);
+  }
+  return 1;
+}
+
+// ---------------------------------------------------------------------------
 // Adjoint of the position sweeps.  A dual step averages each primitive's N
 // vertices; a primal step replaces every updated vertex (adjacency non-empty,
 // not a frozen boundary vertex) by the mean of its primitives' dual points and

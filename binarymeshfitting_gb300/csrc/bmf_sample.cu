@@ -166,6 +166,9 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
   __shared__ int perm2[512];
   __shared__ uint4 gtab[512];
   __shared__ float4 zt[kMaxOctaves * kMaxFillRun];
+  // density of the CTA's lines for one 32-sample word block, flushed with
+  // coalesced 128-byte row stores (rows padded to 33: conflict-free columns)
+  extern __shared__ float s_stage[];
   __shared__ int s_item;
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
     perm2[i] = field.perm[i & 255];
@@ -186,7 +189,6 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
     const bool active = line < dim * dim;
     const int x = active ? line / dim : 0, y = active ? line - x * dim : 0;
     const float px = ch.ox + (float)x * ch.scale, py = ch.oy + (float)y * ch.scale;
-    const int64_t dbase = ch.dens + (int64_t)line * dim;
     uint32_t* wline = words + ch.words + (int64_t)line * zc;
     const int nruns = (dim + kFillRun - 1) / kFillRun;
     uint32_t wacc = 0u, fl = 0u;
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         zt[threadIdx.x] = make_float4(zf, zf - 1.0f, fade(zf), __int_as_float(((int)fz) & 255));
       }
       __syncthreads();
-      if (!active) continue;
+      if (active) {
       float sum[kFillRun];
 #pragma unroll
       for (int k = 0; k < kFillRun; ++k) sum[k] = 0.0f;
@@ -251,11 +253,12 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         amp = amp * gain;
       }
       uint32_t bits = 0u;
+      float* row = s_stage + threadIdx.x * 33 + (z0 & 31);
 #pragma unroll
       for (int k = 0; k < kFillRun; ++k) {
         if (k >= n) break;
         const float d = (py - h0) - ampl * sum[k];
-        if (dens_out) dens_out[dbase + z0 + k] = d;
+        row[k] = d;
         if (d < 0.0f) bits |= 1u << k;
       }
       wacc |= bits << (z0 & 31);
@@ -264,11 +267,39 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         fl |= (wacc != 0u && wacc != kFull) ? 1u : (wacc == kFull ? 2u : 4u);
         wacc = 0u;
       }
+      }  // active
+      if (dens_out && (((z0 + kFillRun) & 31) == 0 || zr == nruns - 1)) {
+        // flush the word block: warp w writes rows [32w, 32w + 32), one
+        // 32-sample segment per row per instruction
+        __syncthreads();
+        const int zb0 = z0 & ~31, nz = min(32, dim - zb0);
+        const int lane = threadIdx.x & 31, w0 = threadIdx.x & ~31;
+        for (int j = 0; j < 32; ++j) {
+          const int l = w0 + j;
+          if (item.y + l < dim * dim && lane < nz)
+            dens_out[ch.dens + (int64_t)(item.y + l) * dim + zb0 + lane] = s_stage[l * 33 + lane];
+        }
+      }
     }
     fl = __reduce_or_sync(kFull, fl);
     if ((threadIdx.x & 31) == 0 && fl) atomicOr(flags + item.x, fl);
     if (!queue) break;
   }
+}
+
+constexpr size_t kStageBytes = sizeof(float) * kFillLines * 33;
+
+// The kernels' static + staging shared memory exceeds the 48 KB default: opt
+// in once per device.
+static void fill_terrain_smem_optin() {
+  static bool done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && done[dev]) return;
+  cudaFuncSetAttribute(k_fill_terrain<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
+  cudaFuncSetAttribute(k_fill_terrain<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
+  cudaFuncSetAttribute(k_fill_terrain<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
+  if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
 void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,
@@ -277,12 +308,14 @@ void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items,
   if (n_items <= 0) return;
   if (d_queue) cudaMemsetAsync(d_queue, 0, sizeof(int), st);
   const int g = d_queue ? grid : n_items;
+  fill_terrain_smem_optin();
+  const size_t sm = kStageBytes;
   if (run == 4)
-    k_fill_terrain<4><<<g, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+    k_fill_terrain<4><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
   else if (run == 16)
-    k_fill_terrain<16><<<g, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+    k_fill_terrain<16><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
   else
-    k_fill_terrain<8><<<g, kFillLines, 0, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+    k_fill_terrain<8><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
 }
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
@@ -291,12 +324,13 @@ int fill_terrain_resident_ctas(int run) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  fill_terrain_smem_optin();
   if (run == 4)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4>, kFillLines, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4>, kFillLines, kStageBytes);
   else if (run == 16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16>, kFillLines, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16>, kFillLines, kStageBytes);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8>, kFillLines, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8>, kFillLines, kStageBytes);
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 

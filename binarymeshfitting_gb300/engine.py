@@ -1,6 +1,8 @@
 """Python host layer over the C ABI: device buffers are torch tensors, every
 compute call goes through libbmf_gb300.so (no CPU path)."""
 import ctypes
+
+import numpy as np
 from dataclasses import dataclass
 from typing import Optional
 
@@ -156,6 +158,46 @@ class Context:
                                          int(smooth_normals), _stream(stream)))
         return mesh
 
+    def lod_generate(self, root_pos, root_size, focus, split_multiplier=1.0, size_modifier=0.0, min_level=1,
+                     max_level=7, dim=33, base_overlap=0.035, boundary_processing=False, iters=0, cap=16384,
+                     stream=None):
+        """WorldOctree split policy on the device: (n, 6) int32 tensor of
+        bmf_chunk_desc rows (origin xyz and scale as float32 bits, dim, level)
+        in the reference's leaf order."""
+        p = L.LodParams()
+        for i in range(3):
+            p.root_pos[i] = float(root_pos[i])
+            p.focus[i] = float(focus[i])
+        p.root_size, p.split_multiplier, p.size_modifier = float(root_size), float(split_multiplier), float(size_modifier)
+        p.min_level, p.max_level, p.dim = int(min_level), int(max_level), int(dim)
+        p.base_overlap, p.boundary_processing, p.iters = float(base_overlap), int(boundary_processing), int(iters)
+        rows = torch.empty((cap, 6), dtype=torch.int32, device=self.device)
+        cnt = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._check(self.lib.bmf_lod_generate(self.h, ctypes.byref(p), _ptr(rows), cap, _ptr(cnt), _stream(stream)))
+        n = int(cnt.item())
+        if n < 0:
+            raise L.BmfError(L.ERR_CAPACITY, "more leaves than cap=%d" % cap)
+        return rows[:n]
+
+    @staticmethod
+    def descs_from_rows(rows):
+        """Host bmf_chunk_desc list from lod_generate rows."""
+        r = rows.cpu().numpy()
+        f = r[:, :4].copy().view(np.float32)
+        return [L.ChunkDesc.make(f[i, :3], f[i, 3], int(r[i, 4]), int(r[i, 5])) for i in range(len(r))]
+
+    def format(self, mesh: ChunkMesh, unwind=False, smooth_normals=False, stream=None):
+        """GLChunk::format_data: (p, n, c) device tensors of shape (count, 3)."""
+        m = L.Mesh(mesh.pos.data_ptr(), mesh.nrm.data_ptr() if mesh.nrm is not None else None,
+                   mesh.boundary.data_ptr(), mesh.valence.data_ptr(), mesh.idx.data_ptr(), mesh.n_verts,
+                   mesh.n_idx, mesh.n_verts, mesh.n_idx, int(mesh.contains_mesh), mesh.prim_size)
+        cnt = mesh.n_idx // 4 * 4 if unwind else mesh.n_verts
+        p, n, c = (torch.empty((max(cnt, 1), 3), dtype=torch.float32, device=self.device) for _ in range(3))
+        got = ctypes.c_int64(0)
+        self._check(self.lib.bmf_format(self.h, ctypes.byref(m), int(unwind), int(smooth_normals), _ptr(p), _ptr(n),
+                                        _ptr(c), cnt, ctypes.byref(got), _stream(stream)))
+        return p[:got.value], n[:got.value], c[:got.value]
+
     def extract_chunk(self, desc: L.ChunkDesc, field: L.Field, mode=L.MODE_R, placement=L.PLACE_CENTER, iters=0,
                       process_boundary=False, smooth_normals=False, stream=None):
         opts = L.ExtractOpts(mode, placement, iters, int(process_boundary), int(smooth_normals), 0)
@@ -215,6 +257,14 @@ class Batch:
         ms = (ctypes.c_float * 6)()
         self.ctx._check(self.ctx.lib.bmf_batch_profile(self.h, ctypes.byref(self.out), ms, _stream(stream)))
         return list(ms)
+
+    def format(self, unwind=False, smooth_normals=False, stream=None):
+        """GLChunk::format_data over the whole arena of the last run: (p, n, c)."""
+        cnt = self.out.n_idx // 4 * 4 if unwind else self.out.n_verts
+        p, n, c = (torch.empty((max(cnt, 1), 3), dtype=torch.float32, device=self.ctx.device) for _ in range(3))
+        self.ctx._check(self.ctx.lib.bmf_batch_format(self.h, ctypes.byref(self.out), int(unwind), int(smooth_normals),
+                                                      _ptr(p), _ptr(n), _ptr(c), cnt, _stream(stream)))
+        return p[:cnt], n[:cnt], c[:cnt]
 
     def tuning(self):
         """The plan's launch tuning as a dict (bmf_batch_tuning)."""

@@ -208,6 +208,50 @@ BMF_API bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_des
  * [5] mesh processing. */
 BMF_API bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms, void* stream);
 
+/* ---- device-side descriptor generation: the WorldOctree LOD split policy ----
+ * WorldOctree::split_leaves / node_needs_split (WorldOctree.cpp:129-161,
+ * 237-247) from a root cube: a node splits while level < min_level, or while
+ * level < max_level and |focus - middle| < size * split_multiplier +
+ * size_modifier + size / 2; the leaves become chunk descriptors in the
+ * reference's leaf order (its depth-first stack order), framed as
+ * DMCChunk::label_grid frames them (DMCChunk.cpp:94-97) with the overlap rule
+ * of ChunkGenerator::extract_chunk (ChunkGenerator.cpp:98). */
+typedef struct {
+  float root_pos[3];      /* root corner; WorldOctree::init(s) uses size 2s at -s per axis */
+  float root_size;
+  float focus[3];
+  float split_multiplier; /* WorldProperties (WorldOctree.cpp:21-33) */
+  float size_modifier;
+  int32_t min_level;
+  int32_t max_level;      /* <= 20 */
+  int32_t dim;            /* samples per chunk axis (chunk_resolution) */
+  float base_overlap;     /* WorldProperties::overlap */
+  int32_t boundary_processing;
+  int32_t iters;
+} bmf_lod_params;
+/* Writes at most `cap` (<= 16384) descriptors to d_descs (device) and their
+ * count to *d_count (device int; -1 when the tree has more leaves than cap).
+ * Asynchronous on `stream` (graph-capturable). */
+BMF_API bmf_status bmf_lod_generate(bmf_ctx* ctx, const bmf_lod_params* p, bmf_chunk_desc* d_descs, int32_t cap,
+                                    int32_t* d_count, void* stream);
+
+/* ---- draw layout: GLChunk::format_data (GLChunk.cpp:278-335), headless ----
+ * Writes 3 floats each of position, normal and colour per output vertex into
+ * d_p, d_n, d_c (device, at least `cap` vertices).  unwind == 0: one output
+ * vertex per mesh vertex (normal 0 when the mesh has none); unwind == 1: the
+ * quads (prim_size 4) unwound to 4 vertices each, all four with one normal:
+ * smooth_normals ? the mean of the 4 vertex normals (needs d_nrm) : the flat
+ * normal -normalize((m0 + m1) / 2) of the quad's two corner triangles.  The
+ * colour is white, the vertex colour of this path (DMCChunk.cpp:681, averaged
+ * by the sweeps).  *h_count (nullable) receives the vertices written. */
+BMF_API bmf_status bmf_format(bmf_ctx* ctx, const bmf_mesh* mesh, int32_t unwind, int32_t smooth_normals, float* d_p,
+                              float* d_n, float* d_c, int64_t cap, int64_t* h_count, void* stream);
+/* The same over a batch arena after bmf_batch_run (chunk-local indices are
+ * resolved through the plan's chunk table; output in arena order; counts
+ * read on the device, so it can follow the run without a sync). */
+BMF_API bmf_status bmf_batch_format(bmf_batch* b, const bmf_batch_out* out, int32_t unwind, int32_t smooth_normals,
+                                    float* d_p, float* d_n, float* d_c, int64_t cap, void* stream);
+
 /* ---- launch tuning of a batch plan (no counterpart in the reference) ----
  * The knobs that change only speed, never results. */
 typedef struct {

@@ -825,6 +825,121 @@ static void v3sub(const float* a, const float* b, float o[3]) {
   o[2] = a[2] - b[2];
 }
 
+/* WorldOctree::split_leaves (WorldOctree.cpp:129-161): depth-first with an
+ * explicit stack (children pushed 0..7 at the MCDX/MCDY/MCDZ offsets of
+ * WorldOctree.cpp:177-199 / Tables.hpp:7-9, popped last-in first-out);
+ * node_needs_split (WorldOctree.cpp:237-247) with middle = pos + size / 2
+ * (WorldOctreeNode.cpp:27); each leaf framed like DMCChunk::label_grid
+ * (DMCChunk.cpp:94-97) with ChunkGenerator.cpp:98's overlap.  prm: root
+ * xyz, root size, focus xyz, split_multiplier, size_modifier, base_overlap;
+ * out rows: origin xyz, scale, dim, level.  Returns the leaf count (at most
+ * cap rows written) or -1 when the stack would exceed 64 * 8 entries. */
+int64_t bmfo_lod_generate(const float* prm, int min_level, int max_level, int dim, int boundary_processing,
+                          int iters, float* out, int64_t cap) {
+  typedef struct { float p[3], size; int level; } node;
+  node stack[64 * 8 + 8];
+  int top = 0;
+  int64_t n = 0;
+  static const int mx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, my[8] = {0, 0, 0, 0, 1, 1, 1, 1}, mz[8] = {0, 0, 1, 1, 0, 0, 1, 1};
+  node r = {{prm[0], prm[1], prm[2]}, prm[3], 0};
+  stack[top++] = r;
+  while (top > 0) {
+    node c = stack[--top];
+    int split;
+    if (c.level >= max_level) split = 0;
+    else if (c.level < min_level) split = 1;
+    else {
+      float m[3], d[3];
+      for (int k = 0; k < 3; ++k) m[k] = c.p[k] + c.size * 0.5f;
+      for (int k = 0; k < 3; ++k) d[k] = prm[4 + k] - m[k];
+      float dist = sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+      split = dist < (c.size * prm[7] + prm[8]) + c.size * 0.5f;
+    }
+    if (!split) {
+      if (n < cap) {
+        float ov = (c.level == max_level && (!boundary_processing || iters == 0)) ? 0.0f
+                                                                                : prm[9] + 0.005f * (float)iters;
+        float delta = c.size * (1.0f + ov * 2.0f) / (float)(dim - 1);
+        float shift = c.size * ov;
+        float* o = out + 6 * n;
+        o[0] = c.p[0] - shift;
+        o[1] = c.p[1] - shift;
+        o[2] = c.p[2] - shift;
+        o[3] = delta;
+        o[4] = (float)dim;
+        o[5] = (float)c.level;
+      }
+      ++n;
+      continue;
+    }
+    if (top + 8 > 64 * 8) return -1;
+    float cs = c.size * 0.5f;
+    for (int i = 0; i < 8; ++i) {
+      node ch = {{c.p[0] + (float)mx[i] * cs, c.p[1] + (float)my[i] * cs, c.p[2] + (float)mz[i] * cs},
+                 c.size * 0.5f, c.level + 1};
+      stack[top++] = ch;
+    }
+  }
+  return n;
+}
+
+/* GLChunk::format_data (GLChunk.cpp:278-335).  unwind == 0: p, n, c per
+ * vertex (c is white: DMCChunk.cpp:681 sets (1, 1, 1) and the sweeps only
+ * average colours).  unwind == 1: per quad (i += 4) its 4 corners, one normal
+ * for all four: smooth ? (n0 + n1 + n2 + n3) * 0.25 : -normalize((m0 + m1) *
+ * 0.5) with m0 = cross(normalize(p0 - p1), normalize(p0 - p2)),
+ * m1 = cross(normalize(p2 - p3), normalize(p2 - p0)), a NaN x taking the
+ * other.  Returns the vertices written. */
+int64_t bmfo_format(int64_t nverts, const float* pos, const float* nrm, int64_t nidx, const uint32_t* idx, int unwind,
+                    int smooth_normals, float* p, float* n, float* c) {
+  if (!unwind) {
+    for (int64_t i = 0; i < nverts; ++i)
+      for (int k = 0; k < 3; ++k) {
+        p[3 * i + k] = pos[3 * i + k];
+        n[3 * i + k] = nrm ? nrm[3 * i + k] : 0.0f;
+        c[3 * i + k] = 1.0f;
+      }
+    return nverts;
+  }
+  for (int64_t i = 0; i + 3 < nidx; i += 4) {
+    const float* q[4];
+    for (int k = 0; k < 4; ++k) q[k] = pos + 3 * (int64_t)idx[i + k];
+    float m[3];
+    if (smooth_normals) {
+      for (int k = 0; k < 3; ++k) {
+        float s = nrm[3 * (int64_t)idx[i] + k] + nrm[3 * (int64_t)idx[i + 1] + k];
+        s = s + nrm[3 * (int64_t)idx[i + 2] + k];
+        s = s + nrm[3 * (int64_t)idx[i + 3] + k];
+        m[k] = s * 0.25f;
+      }
+    } else {
+      float a[3], b[3], na[3], nb[3], m0[3], m1[3], h[3], o[3];
+      v3sub(q[0], q[1], a);
+      v3sub(q[0], q[2], b);
+      v3norm(a, na);
+      v3norm(b, nb);
+      v3cross(na, nb, m0);
+      v3sub(q[2], q[3], a);
+      v3sub(q[2], q[0], b);
+      v3norm(a, na);
+      v3norm(b, nb);
+      v3cross(na, nb, m1);
+      if (isnan(m0[0])) memcpy(m0, m1, sizeof(m0));
+      if (isnan(m1[0])) memcpy(m1, m0, sizeof(m1));
+      for (int k = 0; k < 3; ++k) h[k] = (m0[k] + m1[k]) * 0.5f;
+      v3norm(h, o);
+      for (int k = 0; k < 3; ++k) m[k] = -o[k];
+    }
+    for (int j = 0; j < 4; ++j)
+      for (int k = 0; k < 3; ++k) {
+        p[3 * (i + j) + k] = q[j][k];
+        n[3 * (i + j) + k] = m[k];
+        c[3 * (i + j) + k] = 1.0f;
+      }
+  }
+  return nidx / 4 * 4;
+}
+
 void bmfo_process(int N, int64_t nverts, float* pos, float* nrm, const uint8_t* vboundary, const uint8_t* vvalence,
                   int64_t nidx, const uint32_t* idx, int iters, int process_boundary, int smooth_normals) {
   if (nverts == 0 || nidx < N) return; /* MeshProcessor.cpp:28-29 */

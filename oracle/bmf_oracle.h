@@ -68,6 +68,14 @@ int bmfo_extract_q(int dim, const float* density, const uint32_t* words, int pla
 /* ---- MeshProcessor<N> (MeshProcessor.cpp:26-306) in the order
  * ChunkGenerator::extract_chunk uses (ChunkGenerator.cpp:112-124).  pos and
  * nrm are updated in place (nrm holds the starting normals, usually 0). */
+/* WorldOctree::split_leaves + chunk framing: rows (origin xyz, scale, dim,
+ * level) in the reference's leaf order; returns the leaf count. */
+int64_t bmfo_lod_generate(const float* prm, int min_level, int max_level, int dim, int boundary_processing,
+                          int iters, float* out, int64_t cap);
+/* GLChunk::format_data: per vertex (unwind 0) or unwound quads with one
+ * normal each (unwind 1); returns the vertices written. */
+int64_t bmfo_format(int64_t nverts, const float* pos, const float* nrm, int64_t nidx, const uint32_t* idx, int unwind,
+                    int smooth_normals, float* p, float* n, float* c);
 void bmfo_process(int N, int64_t nverts, float* pos, float* nrm, const uint8_t* vboundary, const uint8_t* vvalence,
                   int64_t nidx, const uint32_t* idx, int iters, int process_boundary, int smooth_normals);
 

@@ -43,6 +43,10 @@ def lib():
         L.bmfo_fit_loss_f64.argtypes = [c_int, vp, c_int, vp, vp, vp, vp, vp]
         L.bmfo_fit_loss_spheres_f64.restype = ctypes.c_double
         L.bmfo_fit_loss_spheres_f64.argtypes = [c_int, vp, c_int, vp, c_int, vp, vp, vp, vp]
+        L.bmfo_lod_generate.restype = i64
+        L.bmfo_lod_generate.argtypes = [vp, c_int, c_int, c_int, c_int, c_int, vp, i64]
+        L.bmfo_format.restype = i64
+        L.bmfo_format.argtypes = [i64, vp, vp, i64, vp, c_int, c_int, vp, vp, vp]
         L.bmfo_extract_batch.restype = i64
         L.bmfo_extract_batch.argtypes = [c_int, vp, c_int, vp, c_int, c_int, c_int, c_int, vp, c_int]
         _lib = L
@@ -126,6 +130,31 @@ def process(N, pos, boundary, valence, idx, iters, process_boundary=False, smoot
     lib().bmfo_process(N, len(b), _p(p), _p(n), _p(b), _p(v), len(ix), _p(ix), iters, int(process_boundary),
                        int(smooth_normals))
     return p.reshape(-1, 3), n.reshape(-1, 3)
+
+
+def lod_generate(root_pos, root_size, focus, split_multiplier, size_modifier, min_level, max_level, dim,
+                 base_overlap=0.035, boundary_processing=False, iters=0, cap=1 << 16):
+    """WorldOctree::split_leaves restated: (n, 6) float32 rows (origin xyz,
+    scale, dim, level) in the reference's leaf order."""
+    prm = np.array(list(root_pos) + [root_size] + list(focus) + [split_multiplier, size_modifier, base_overlap],
+                   np.float32)
+    out = np.zeros((cap, 6), np.float32)
+    n = lib().bmfo_lod_generate(_p(prm), min_level, max_level, dim, int(boundary_processing), iters, _p(out), cap)
+    assert 0 <= n <= cap
+    return out[:n]
+
+
+def format_data(pos, nrm, idx, unwind, smooth_normals):
+    """GLChunk::format_data restated: returns (p, n, c) as (count, 3) float32."""
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    nrm = None if nrm is None else np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(idx, np.uint32)
+    cnt = len(idx) // 4 * 4 if unwind else len(pos)
+    p, n, c = (np.zeros((max(cnt, 1), 3), np.float32) for _ in range(3))
+    got = lib().bmfo_format(len(pos), _p(pos), _p(nrm), len(idx), _p(idx), int(unwind), int(smooth_normals),
+                            _p(p), _p(n), _p(c))
+    assert got == cnt
+    return p[:cnt], n[:cnt], c[:cnt]
 
 
 def qef_f32(pos, nrm):
