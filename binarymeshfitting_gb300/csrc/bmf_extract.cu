@@ -1377,7 +1377,7 @@ void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_to
 // lane: its owned vertices (ids from the scanned word base and the crossing
 // words, calculate_isovertex positions, boundary, key, init_valence) and its
 // triangles (slot from the word's index base and the triangle-count planes).
-__global__ void __launch_bounds__(256) k_emit_cells_r(const ChunkDev* __restrict__ chunks,
+__global__ void __launch_bounds__(256, 3) k_emit_cells_r(const ChunkDev* __restrict__ chunks,
                                                       const uint32_t* __restrict__ words,
                                                       const float* __restrict__ dens, WordScratch ws, MeshOut out) {
   __shared__ SmemTabs T;

@@ -130,6 +130,10 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
 constexpr int kFillLines = 256; // lines per item = threads per CTA
 constexpr int kMaxOctaves = 32;
 constexpr int kMaxFillRun = 16;
+// z terms {zf, zf - 1, fade(zf), Z} per (octave, z): for every z of the
+// item's lines at once when octaves * dim fit, else per run
+constexpr int kZtEntries = 1024;
+static_assert(kZtEntries >= kMaxOctaves * kMaxFillRun, "per-run z terms fit");
 
 // Per hash h: x = u selector (x or y) | sign of u << 31; y = v selector (x or
 // y) | (v == z ? 1 : sign of v) << 31; z = 0 when v == z else all ones (keeps
@@ -165,7 +169,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
                                                              uint32_t* __restrict__ flags) {
   __shared__ int perm2[512];
   __shared__ uint4 gtab[512];
-  __shared__ float4 zt[kMaxOctaves * kMaxFillRun];
+  __shared__ float4 zt[kZtEntries];
   // density of the CTA's lines for one 32-sample word block, flushed with
   // coalesced 128-byte row stores (rows padded to 33: conflict-free columns)
   extern __shared__ float s_stage[];
@@ -191,11 +195,25 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
     const float px = ch.ox + (float)x * ch.scale, py = ch.oy + (float)y * ch.scale;
     uint32_t* wline = words + ch.words + (int64_t)line * zc;
     const int nruns = (dim + kFillRun - 1) / kFillRun;
+    // the z terms depend on the chunk only: all of them once per item when they fit
+    const bool whole = oct * dim <= kZtEntries;
+    if (whole) {
+      for (int e = threadIdx.x; e < oct * dim; e += blockDim.x) {
+        const int o = e / dim, z = e - o * dim;
+        float fr = freq;
+        for (int i = 0; i < o; ++i) fr = fr * lac;
+        const float pz = ch.oz + (float)z * ch.scale;
+        const float zs = pz * fr;
+        const float fz = floorf(zs);
+        const float zf = zs - fz;
+        zt[e] = make_float4(zf, zf - 1.0f, fade(zf), __int_as_float(((int)fz) & 255));
+      }
+    }
     uint32_t wacc = 0u, fl = 0u;
     for (int zr = 0; zr < nruns; ++zr) {
       const int z0 = zr * kFillRun, n = min(kFillRun, dim - z0);
-      __syncthreads();
-      if ((int)threadIdx.x < oct * kFillRun) {
+      if (!whole || zr == 0) __syncthreads();
+      if (!whole && (int)threadIdx.x < oct * kFillRun) {
         const int o = threadIdx.x / kFillRun, k = threadIdx.x % kFillRun;
         float fr = freq;
         for (int i = 0; i < o; ++i) fr = fr * lac;
@@ -205,7 +223,9 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         const float zf = zs - fz;
         zt[threadIdx.x] = make_float4(zf, zf - 1.0f, fade(zf), __int_as_float(((int)fz) & 255));
       }
-      __syncthreads();
+      if (!whole) __syncthreads();
+      // z terms of (octave o, sample k of this run)
+      const int zt_o = whole ? dim : kFillRun, zt_k = whole ? z0 : 0;
       if (active) {
       float sum[kFillRun];
 #pragma unroll
@@ -225,7 +245,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) {
           if (k >= n) break;
-          const float4 t = zt[o * kFillRun + k];
+          const float4 t = zt[o * zt_o + zt_k + k];
           const int Z = __float_as_int(t.w);
           if (Z != Zp) {  // same for every lane of the CTA
             Zp = Z;
@@ -279,6 +299,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
           if (item.y + l < dim * dim && lane < nz)
             dens_out[ch.dens + (int64_t)(item.y + l) * dim + zb0 + lane] = s_stage[l * 33 + lane];
         }
+        __syncthreads();  // the next word block's rows overwrite the stage
       }
     }
     fl = __reduce_or_sync(kFull, fl);
