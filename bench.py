@@ -30,10 +30,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "chunks/s (mixed-LOD batch vs per-chunk, same GB300, exact topology)"
 FP32_OPS_PER_SAMPLE = 337  # terrain FBM, 5 octaves, counted from the kernel source
-# DRAM bytes (read + write) per sample of k_sample_label from one ncu capture on
-# the 256-chunk update (110,890,368 samples, 401.31 MB): traffic grows with the
-# samples, so a full launch is scaled from it (profiles/k_sample_label_lod_update_256.txt)
-FILL_DRAM_BYTES_PER_SAMPLE = 401.31e6 / 110_890_368
+# DRAM bytes (read + write) per sample of k_fill_terrain from one ncu capture on
+# the 256-chunk update (110,890,368 samples, 47.65 MB read + 448.53 MB written):
+# traffic grows with the samples, so a full launch is scaled from it
+# (profiles/k_fill_terrain_lod_update_256.txt)
+FILL_DRAM_BYTES_PER_SAMPLE = (47.65e6 + 448.53e6) / 110_890_368
 
 
 def parse():
@@ -342,7 +343,17 @@ def run_gb300(args):
     ext_bytes = words * (4 + 8 + 8 + 4) + nv * per_vertex + ni * 4
     ext_ms = st_ms[1] + st_ms[2] + st_ms[3] + st_ms[4]
     ext_gbs = ext_bytes / (ext_ms / 1000.0) / 1e9
-    roofline = {"kernel": "k_sample_label (density FBM + occupancy words)", "bound": "fp32",
+    # algorithmic HBM bytes of the mesh processing (CSR scan + adjacency + iters x (dual, primal)),
+    # each array counted once per pass: dual reads indices + positions (+ normals) and writes
+    # dual points + normals; primal reads offsets, adjacency, dual points + normals, flags and
+    # writes positions + normals
+    n_prims = ni // 3 if args.mode == "R" else ni // 4
+    nb = 12 if normals else 0
+    dual_b = 4 * ni + 12 * nv + nb * nv + (12 + nb) * n_prims
+    primal_b = 4 * nv + 4 * ni + (12 + nb) * n_prims + 2 * nv + (12 + nb) * nv
+    proc_bytes = args.iters * (dual_b + primal_b) + (1 + 4) * nv + (4 + 4) * nv + 4 * ni
+    proc_gbs = proc_bytes / (st_ms[5] / 1000.0) / 1e9 if st_ms[5] > 0 else 0.0
+    roofline = {"kernel": "k_fill_terrain (density FBM + occupancy words)", "bound": "fp32",
                 "achieved": fill_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fill_achieved / fp32_peak,
                 "peak_kind": "nominal 152 SM x 128 FP32 lanes x %.0f MHz (no measured FP32 peak exists)" % sm_max,
                 "traffic": FILL_DRAM_BYTES_PER_SAMPLE * samples, "traffic_unit": "bytes per launch (scaled ncu)",
@@ -351,6 +362,10 @@ def run_gb300(args):
                 "extraction_hbm": {"kernels": "count+scan+offsets+emit", "achieved": ext_gbs, "peak": hbm_peak,
                                    "unit": "GB/s", "frac": ext_gbs / hbm_peak, "bytes": ext_bytes,
                                    "ms": ext_ms, "peak_kind": peak_kind},
+                "processing_hbm": {"kernels": "scan+adj_build+%d x (dual, primal)" % args.iters,
+                                   "achieved": proc_gbs, "peak": hbm_peak, "unit": "GB/s",
+                                   "frac": proc_gbs / hbm_peak, "bytes": proc_bytes, "ms": st_ms[5],
+                                   "peak_kind": peak_kind},
                 "stage_ms": {"fill_label": st_ms[0], "count": st_ms[1], "scan": st_ms[2], "offsets": st_ms[3],
                              "emit": st_ms[4], "process": st_ms[5]}}
 
