@@ -15,7 +15,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libbmf_gb300.so")
-SOURCES = ["bmf_sample.cu", "bmf_extract.cu", "bmf_process.cu", "bmf_capi.cu", "bmf_noalloc.cu", "bmf_lod.cu"]
+SOURCES = ["bmf_sample.cu", "bmf_extract.cu", "bmf_process.cu", "bmf_capi.cu", "bmf_noalloc.cu", "bmf_lod.cu",
+           "bmf_adjoint64.cu"]
+# Sources whose arithmetic does not mirror the reference's float rounding may
+# contract multiplies and adds (every other TU is built with --fmad=false).
+FMA_SOURCES = {"bmf_adjoint64.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "-I" + os.path.join(HERE, "..")]
@@ -45,7 +49,8 @@ def build(force=False, verbose=False, extra_flags=()):
 
     def compile_one(src):
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + NVCC_FLAGS + list(extra_flags)
+        flags = [("--fmad=true" if f == "--fmad=false" and src in FMA_SOURCES else f) for f in NVCC_FLAGS]
+        cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + flags + list(extra_flags)
         if verbose:
             cmd += ["-Xptxas", "-v"]
         r = subprocess.run(cmd, capture_output=True, text=True)

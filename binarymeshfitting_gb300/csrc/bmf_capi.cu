@@ -187,9 +187,9 @@ bmf_status extract_core(bmf_ctx* ctx, int mode, int placement, ChunkDev* d_chunk
   if ((s = scratch(ctx, S_ICNT, (size_t)words_total, &ws.icnt)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_GPL, (size_t)words_total * 3, &ws.gpl)) != BMF_OK) return s;
   if ((s = scratch(ctx, S_TOT, (size_t)n_chunks * 2, &tot)) != BMF_OK) return s;
-  if (mode == BMF_MODE_R) {
-    // work list of active cells: each one owns a vertex or emits a triangle
-    ws.clist_cap = mo.vcap + mo.icap / 3 + 1;
+  {
+    // work list of active cells: each one owns a vertex or emits a primitive
+    ws.clist_cap = mo.vcap + mo.icap / (mode == BMF_MODE_R ? 3 : 4) + 1;
     uint2* list;
     if ((s = scratch(ctx, S_CLIST, (size_t)ws.clist_cap + 1, &list)) != BMF_OK) return s;
     ws.clist = list;
@@ -580,10 +580,9 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
 
 namespace {
 
-// The Mode R work list for an output arena of (vcap, icap) (+ its counter).
+// The work list of active cells for an output arena of (vcap, icap) (+ its counter).
 bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
-  if (b->opts.mode != BMF_MODE_R) return BMF_OK;
-  const int64_t cap = vcap + icap / 3 + 1;
+  const int64_t cap = vcap + icap / (b->opts.mode == BMF_MODE_R ? 3 : 4) + 1;
   if (cap > b->clist_cap) {
     if (b->d_clist) cudaFree(b->d_clist);
     b->d_clist = nullptr;
@@ -957,6 +956,7 @@ struct bmf_fit {
   uint8_t *d_valence = nullptr, *d_boundary = nullptr;
   float* d_g = nullptr;           // position-gradient work buffer
   uint32_t* d_qlist = nullptr;    // QEF-placed vertices of the FP64 backward (+ counter at [vcap])
+  uint2* d_clist = nullptr;       // work list of active cells (+ counter after it)
   const float* last_density = nullptr;
   int64_t* h_pinned = nullptr;
 };
@@ -967,7 +967,7 @@ bmf_status bmf_fit_destroy(bmf_fit* f) {
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   void* ptrs[] = {f->d_chunks, f->d_units, f->d_flags, f->d_tot, f->d_words, f->d_totals, f->ws.vcnt, f->ws.icnt,
                   f->ws.gpl, f->ps.off, f->ps.cursor, f->ps.adj, f->ps.dual_p, f->ps.dual_n, f->ps.tmp, f->d_idxg,
-                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist};
+                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist, f->d_clist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (f->h_pinned) cudaFreeHost(f->h_pinned);
@@ -1026,6 +1026,7 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
             cudaMalloc(&f->d_valence, vcap + 1) == cudaSuccess && cudaMalloc(&f->d_boundary, vcap + 1) == cudaSuccess &&
             cudaMalloc(&f->d_g, sizeof(float) * 3 * (vcap + 1)) == cudaSuccess &&
             cudaMalloc(&f->d_qlist, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
+            cudaMalloc(&f->d_clist, sizeof(uint2) * (vcap + icap / 4 + 2)) == cudaSuccess &&
             cudaMallocHost(&f->h_pinned, sizeof(int64_t) * 4) == cudaSuccess &&
             cudaMemcpy(f->d_chunks, hc.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(f->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -1033,6 +1034,9 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
     bmf_fit_destroy(f);
     return fail(ctx, BMF_ERR_OUT_OF_MEMORY, "bmf_fit_create: device allocation failed");
   }
+  f->ws.clist = f->d_clist;
+  f->ws.clist_cap = vcap + icap / 4 + 1;
+  f->ws.ccount = (uint32_t*)(f->d_clist + f->ws.clist_cap);
   *out = f;
   return BMF_OK;
 }

@@ -18,6 +18,7 @@
 // list (DMC_CellsBlock).
 #include "bmf_device.cuh"
 #include "bmf_internal.h"
+#include "bmf_qef.cuh"
 
 namespace bmf {
 
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
   __shared__ uint32_t s_act[kWordBlock];  // Mode R work list: active cells of each busy word
   __shared__ uint32_t s_apos[kWordBlock];
   __shared__ uint32_t s_acnt, s_abase;
-  const bool listing = MODE == 0 && ws.clist != nullptr;
+  const bool listing = ws.clist != nullptr;
   for (int base = 0; base < nw; base += kWordBlock) {
     // level 1: one thread per word; quiet words get zero counts right away
     if (threadIdx.x == 0) {
@@ -214,6 +215,13 @@ __global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chun
       q_quad_words(W, dim, zc, x, y, zb, Xi, Yi, Zi);
       ic = 4u * (__popc(Xi) + __popc(Yi) + __popc(Zi));
       if (lane == 0) { ws.gpl[3 * o] = g0; ws.gpl[3 * o + 1] = g1; ws.gpl[3 * o + 2] = g2; }
+      if (listing) {
+        const uint32_t act = __ballot_sync(kFull, ng != 0 || (((Xi | Yi | Zi) >> lane) & 1u));
+        if (lane == 0) {
+          s_act[li] = act;
+          s_apos[li] = act ? atomicAdd(&s_acnt, (uint32_t)__popc(act)) : 0u;
+        }
+      }
     }
     if (lane == 0) {
       ws.vcnt[o] = vc;
@@ -441,240 +449,6 @@ __device__ __forceinline__ uint32_t q_vertex_base(const uint32_t* vbase, const u
          4 * __popc(__ldg(gpl + 3 * wi + 2) & lt);
 }
 
-__device__ __forceinline__ float dens_at(const float* D, int dim, int x, int y, int z) {
-  return __ldg(D + ((int64_t)x * dim + y) * dim + z);
-}
-
-// Central-difference grid gradient, one-sided at the chunk faces.
-__device__ __forceinline__ void grid_gradient(const float* D, int dim, int x, int y, int z, float g[3]) {
-  const int c[3] = {x, y, z};
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    int lo[3] = {x, y, z}, hi[3] = {x, y, z};
-    float h = 0.5f;
-    if (c[a] > 0) lo[a]--; else h = 1.0f;
-    if (c[a] < dim - 1) hi[a]++; else h = 1.0f;
-    g[a] = (dens_at(D, dim, hi[0], hi[1], hi[2]) - dens_at(D, dim, lo[0], lo[1], lo[2])) * h;
-  }
-}
-
-// QEF solve, restating qef_simd.h:150-579 lane by lane in FP32 with the exact
-// 1/sqrt in place of _mm_rsqrt_ps.
-__device__ __forceinline__ float dot4(const float a[4], const float b[4]) {
-  const float m0 = a[0] * b[0], m1 = a[1] * b[1], m2 = a[2] * b[2], m3 = a[3] * b[3];
-  return (m0 + m1) + (m3 + m2);
-}
-__device__ __forceinline__ void vec_mul_m4(const float a[4], const float B[4][4], float out[4]) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    float r = a[0] * B[0][k];
-    r = r + a[1] * B[1][k];
-    r = r + a[2] * B[2][k];
-    r = r + a[3] * B[3][k];
-    out[k] = r;
-  }
-}
-
-// What the QEF adjoint needs from a solve: the eigen decomposition the
-// Jacobi sweeps produced, the kept reciprocals, the mass point and the
-// centred right-hand side r = ATb - ATA * masspoint.
-struct QefSolveInfo {
-  float V[3][3];
-  float sigma[3];
-  float inv[3];
-  float mp[3];
-  float r[3];
-};
-
-struct QefAccum {
-  float ata[4][4];
-  float atb[4];
-  float acc[4];
-  int count;
-  __device__ __forceinline__ void init() {
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) ata[r][k] = 0.0f;
-      atb[r] = 0.0f;
-      acc[r] = 0.0f;
-    }
-    count = 0;
-  }
-  // qef_simd_add, qef_simd.h:411-430
-  __device__ __forceinline__ void add(const float pp[3], const float nn[3]) {
-    const float p[4] = {pp[0], pp[1], pp[2], 1.0f};
-    const float n[4] = {nn[0], nn[1], nn[2], 0.0f};
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) ata[r][k] = ata[r][k] + n[r] * n[k];
-    }
-    const float d = dot4(p, n);
-    const float dd[4] = {d, d, d, 0.0f};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) atb[k] = atb[k] + dd[k] * n[k];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) acc[k] = acc[k] + p[k];
-    ++count;
-  }
-  // qef_simd_solve + svd_solve_ATA_ATb (qef_simd.h:304-461); returns false
-  // for fewer than 2 or more than 12 inputs (qef_simd.h:556-560).
-  __device__ bool solve(float out[3], QefSolveInfo* info = nullptr) const {
-    if (count < 2 || count > 12) {
-      out[0] = out[1] = out[2] = 0.0f;
-      return false;
-    }
-    float mp[4], pr[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) mp[k] = acc[k] / acc[3];
-    vec_mul_m4(mp, ata, pr);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) pr[k] = atb[k] - pr[k];
-    float V[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 0}};
-    float vt[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) vt[r][k] = ata[r][k];
-    }
-#pragma unroll 1
-    for (int sweep = 0; sweep < 5; ++sweep) {
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        const int a = q == 2 ? 1 : 0, b = q == 0 ? 1 : 2;
-        if (vt[a][b] != 0.0f) {
-          // givens_coeffs_sym
-          const float pp = vt[a][a], pq = vt[a][b], qq = vt[b][b];
-          const float tau = (qq - pp) / (pq * 2.0f);
-          const float stt = sqrtf(tau * tau + 1.0f);
-          const float tn = 1.0f / ((tau >= 0.0f) ? (tau + stt) : (tau - stt));
-          float cc = 1.0f / sqrtf(1.0f + tn * tn);
-          float ss = tn * cc;
-          if (pq == 0.0f) { cc = 1.0f; ss = 0.0f; }
-          // rotateq_xy
-          const float c2 = cc * cc, s2 = ss * ss;
-          const float mx = ((2.0f * cc) * ss) * pq;
-          const float nx = (c2 * pp - mx) + s2 * qq;
-          const float ny = (s2 * pp + mx) + c2 * qq;
-          vt[a][a] = nx;
-          vt[b][b] = ny;
-          // rotate_xy
-          const float u3 = vt[0][3 - b], v3 = vt[1 - a][2];
-#pragma unroll
-          for (int r = 0; r < 3; ++r) {
-            const float uu = V[r][a], vv = V[r][b];
-            V[r][a] = cc * uu - ss * vv;
-            V[r][b] = ss * uu + cc * vv;
-          }
-          vt[0][3 - b] = cc * u3 - ss * v3;
-          vt[1 - a][2] = ss * u3 + cc * v3;
-          vt[a][b] = 0.0f;
-        }
-      }
-    }
-    const float sigma[4] = {vt[0][0], vt[1][1], vt[2][2], 0.0f};
-    float invdet[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {  // svd_invdet
-      const float oo = 1.0f / sigma[k];
-      const float a1 = fabsf(sigma[k]), a2 = fabsf(oo);
-      const float mn = (a1 < a2) ? a1 : a2;
-      invdet[k] = (mn >= 0.001f) ? oo : 0.0f;
-    }
-    float mm[3][4], o[4][4];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) mm[r][k] = V[r][k] * invdet[k];
-    }
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) o[r][k] = (r < 3 && k < 3) ? dot4(mm[k], V[r]) : 0.0f;
-    }
-    float xq[4];
-    vec_mul_m4(pr, o, xq);
-    out[0] = xq[0] + mp[0];
-    out[1] = xq[1] + mp[1];
-    out[2] = xq[2] + mp[2];
-    if (info) {
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) info->V[r][k] = V[r][k];
-        info->sigma[r] = sigma[r];
-        info->inv[r] = invdet[r];
-        info->mp[r] = mp[r];
-        info->r[r] = pr[r];
-      }
-    }
-    return true;
-  }
-};
-
-// Crossing point (and hermite normal) of edge e of cell (x, y, z).
-__device__ __forceinline__ void hermite(const float* D, int dim, int x, int y, int z, int e, bool want_n, float p[3],
-                                        float n[3]) {
-  const int ca = edge_c0(e), cb = edge_c1(e);
-  const int a0[3] = {x + ((ca >> 2) & 1), y + ((ca >> 1) & 1), z + (ca & 1)};
-  const int a1[3] = {x + ((cb >> 2) & 1), y + ((cb >> 1) & 1), z + (cb & 1)};
-  const float s0 = dens_at(D, dim, a0[0], a0[1], a0[2]), s1 = dens_at(D, dim, a1[0], a1[1], a1[2]);
-  const float mu = (0.0f - s0) / (s1 - s0);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float dv = ((float)a1[k] - (float)a0[k]) * mu;
-    p[k] = dv + (float)a0[k];
-  }
-  if (want_n) {
-    float g0[3], g1[3], g[3];
-    grid_gradient(D, dim, a0[0], a0[1], a0[2], g0);
-    grid_gradient(D, dim, a1[0], a1[1], a1[2], g1);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) g[k] = g0[k] + (g1[k] - g0[k]) * mu;
-    const float l2 = (g[0] * g[0] + g[1] * g[1]) + g[2] * g[2];
-    const float inv = 1.0f / sqrtf(l2);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) n[k] = g[k] * inv;
-  }
-}
-
-template <int PLACE>
-__device__ __forceinline__ void q_place(const float* D, int dim, int x, int y, int z, int mask, int g, float out[3]) {
-  if (PLACE == 0) {
-    out[0] = (float)x + 0.5f;
-    out[1] = (float)y + 0.5f;
-    out[2] = (float)z + 0.5f;
-    return;
-  }
-  float mp[3] = {0.0f, 0.0f, 0.0f};
-  int cnt = 0;
-  QefAccum q;
-  if (PLACE == 2) q.init();
-  for (int e = 0; e < 12; ++e) {
-    if (group_of(mask, e) != g) continue;
-    float p[3], n[3];
-    hermite(D, dim, x, y, z, e, PLACE == 2, p, n);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) mp[k] = mp[k] + p[k];
-    ++cnt;
-    if (PLACE == 2) q.add(p, n);
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) mp[k] = mp[k] / (float)cnt;
-  if (PLACE == 2) {
-    float s[3];
-    q.solve(s);
-    const bool ok = s[0] >= (float)x && s[0] <= (float)(x + 1) && s[1] >= (float)y && s[1] <= (float)(y + 1) &&
-                    s[2] >= (float)z && s[2] <= (float)(z + 1);
-    if (ok) {
-      out[0] = s[0]; out[1] = s[1]; out[2] = s[2];
-      return;
-    }
-  }
-  out[0] = mp[0]; out[1] = mp[1]; out[2] = mp[2];
-}
-
 template <int MODE, int PLACE>
 __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunks, int n_chunks,
                                               const int* __restrict__ unit_start, const uint32_t* __restrict__ words,
@@ -862,373 +636,6 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
   }
 }
 
-// ---------------------------------------------------------------------------
-// Adjoint of the Mode Q vertex placement with respect to the density.
-// Per vertex the forward's branch (QEF solution inside the cell, or the mass
-// point) is replayed exactly as k_emit took it (same hermite data, same FP32
-// QEF).  The incoming position gradient then goes through the QEF -- x = m +
-// V f(S) V^T r, r = ATb - ATA m, differentiated with the truncation pattern
-// held fixed (Daleckii-Krein: F_ij = (f_i - f_j)/(s_i - s_j), F_ii = f'(s_i))
-// -- or through the mass point, then through every hermite pair: the normal
-// n = G/|G| of the lerped central-difference gradients and the crossing
-// p = a0 + (a1 - a0) mu, mu = -s0 / (s1 - s0), into the density samples
-// (float atomics).
-//
-// T = float differentiates with the forward's own FP32 eigen decomposition.
-// T = double recomputes the hermite data and the eigen decomposition (cyclic
-// Jacobi to convergence) in FP64 from the same samples: the derivative of
-// the exact-arithmetic placement.  It matters because 1/s^2 amplifies the
-// ~1e-6 absolute FP32 error of a small kept eigenvalue (s in [1e-3, 0.05] is
-// common on smooth surfaces, where a cell's normals are nearly parallel).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int find_chunk_by_vertex(const ChunkDev* __restrict__ chunks, int n, int64_t v);
-
-template <typename T>
-struct QefAdj {
-  T A[3][3];    // ATA
-  T V[3][3];    // eigenvectors (columns)
-  T sigma[3];   // eigenvalues
-  T inv[3];     // kept reciprocals (0 = truncated)
-  T mp[3];      // mass point
-  T r[3];       // ATb - ATA mp
-};
-
-template <typename T>
-__device__ __forceinline__ T dens_t(const float* D, int dim, int x, int y, int z) {
-  return (T)dens_at(D, dim, x, y, z);
-}
-
-template <typename T>
-__device__ __forceinline__ void grid_gradient_t(const float* D, int dim, int x, int y, int z, T g[3]) {
-  const int c[3] = {x, y, z};
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    int lo[3] = {x, y, z}, hi[3] = {x, y, z};
-    T h = (T)0.5;
-    if (c[a] > 0) lo[a]--; else h = (T)1;
-    if (c[a] < dim - 1) hi[a]++; else h = (T)1;
-    g[a] = (dens_t<T>(D, dim, hi[0], hi[1], hi[2]) - dens_t<T>(D, dim, lo[0], lo[1], lo[2])) * h;
-  }
-}
-
-// Hermite pair of edge e in precision T (the crossing, the lerped gradient,
-// its length and the unit normal).
-template <typename T>
-struct HermiteT {
-  int a0[3], a1[3];
-  T s0, s1, mu, p[3], g0[3], g1[3], n[3], glen;
-};
-
-template <typename T>
-__device__ __forceinline__ void hermite_t(const float* D, int dim, int x, int y, int z, int e, bool want_n,
-                                          HermiteT<T>& h) {
-  const int ca = edge_c0(e), cb = edge_c1(e);
-  h.a0[0] = x + ((ca >> 2) & 1); h.a0[1] = y + ((ca >> 1) & 1); h.a0[2] = z + (ca & 1);
-  h.a1[0] = x + ((cb >> 2) & 1); h.a1[1] = y + ((cb >> 1) & 1); h.a1[2] = z + (cb & 1);
-  h.s0 = dens_t<T>(D, dim, h.a0[0], h.a0[1], h.a0[2]);
-  h.s1 = dens_t<T>(D, dim, h.a1[0], h.a1[1], h.a1[2]);
-  h.mu = ((T)0 - h.s0) / (h.s1 - h.s0);
-#pragma unroll
-  for (int k = 0; k < 3; ++k) h.p[k] = ((T)h.a1[k] - (T)h.a0[k]) * h.mu + (T)h.a0[k];
-  h.glen = (T)1;
-  if (want_n) {
-    grid_gradient_t<T>(D, dim, h.a0[0], h.a0[1], h.a0[2], h.g0);
-    grid_gradient_t<T>(D, dim, h.a1[0], h.a1[1], h.a1[2], h.g1);
-    T G[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) G[k] = h.g0[k] + (h.g1[k] - h.g0[k]) * h.mu;
-    h.glen = sqrt((G[0] * G[0] + G[1] * G[1]) + G[2] * G[2]);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) h.n[k] = G[k] / h.glen;
-  }
-}
-
-// Symmetric 3x3 eigen decomposition in FP64, A = V diag(w) V^T, refined from
-// the forward's FP32 eigenvectors: V0 is re-orthonormalised (Gram-Schmidt),
-// A is rotated into that basis (nearly diagonal, off-diagonals ~1e-6 |A|)
-// and cyclic Jacobi rotations finish it; convergence is quadratic, so one or
-// two sweeps reach the 1e-17 |A| stopping point instead of five or six from
-// the identity.
-__device__ void eig3_refine(const double A[3][3], const float V0[3][3], double w[3], double V[3][3]) {
-  // columns of V0, orthonormalised
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    double v[3] = {(double)V0[0][c], (double)V0[1][c], (double)V0[2][c]};
-#pragma unroll
-    for (int k = 0; k < c; ++k) {
-      const double d = v[0] * V[0][k] + v[1] * V[1][k] + v[2] * V[2][k];
-#pragma unroll
-      for (int r = 0; r < 3; ++r) v[r] -= d * V[r][k];
-    }
-    const double il = 1.0 / sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) V[r][c] = v[r] * il;
-  }
-  // B = V^T A V
-  double AV[3][3], B[3][3];
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) AV[r][c] = A[r][0] * V[0][c] + A[r][1] * V[1][c] + A[r][2] * V[2][c];
-  }
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) B[r][c] = V[0][r] * AV[0][c] + V[1][r] * AV[1][c] + V[2][r] * AV[2][c];
-  }
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-#pragma unroll
-    for (int c = 0; c < r; ++c) B[r][c] = B[c][r] = 0.5 * (B[r][c] + B[c][r]);
-  }
-  const double tol = 1e-17 * (fabs(B[0][0]) + fabs(B[1][1]) + fabs(B[2][2]));
-#pragma unroll 1
-  for (int sweep = 0; sweep < 16; ++sweep) {
-    if (fabs(B[0][1]) + fabs(B[0][2]) + fabs(B[1][2]) <= tol) break;
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const int p = q == 2 ? 1 : 0, r = q == 0 ? 1 : 2;
-      if (fabs(B[p][r]) <= tol) continue;
-      const double tau = (B[r][r] - B[p][p]) / (2.0 * B[p][r]);
-      const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-      const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const double bkp = B[k][p], bkr = B[k][r];
-        B[k][p] = c * bkp - s * bkr;
-        B[k][r] = s * bkp + c * bkr;
-      }
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const double bpk = B[p][k], brk = B[r][k];
-        B[p][k] = c * bpk - s * brk;
-        B[r][k] = s * bpk + c * brk;
-      }
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const double vkp = V[k][p], vkr = V[k][r];
-        V[k][p] = c * vkp - s * vkr;
-        V[k][r] = s * vkp + c * vkr;
-      }
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < 3; ++i) w[i] = B[i][i];
-}
-
-// LIST = 0: every vertex; 1: every vertex, but QEF-placed ones are only
-// appended to qlist (for a dense second pass); 2: the vertices of qlist.
-template <int PLACE, typename T, int LIST>
-__global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ chunks, int n_chunks,
-                                                   const uint32_t* __restrict__ words, const float* __restrict__ dens,
-                                                   const uint32_t* __restrict__ vkey,
-                                                   const int64_t* __restrict__ d_counts, int64_t vcap,
-                                                   const float* __restrict__ grad_pos, float* __restrict__ grad_dens,
-                                                   uint32_t* __restrict__ qlist, uint32_t* __restrict__ qcount) {
-  int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (LIST == 2) {
-    if (v >= (int64_t)*qcount) return;
-    v = qlist[v];
-  }
-  if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
-  const int c = find_chunk_by_vertex(chunks, n_chunks, v);
-  const ChunkDev ch = chunks[c];
-  const int dim = ch.dim, zc = ch.zc;
-  const uint32_t* W = words + ch.words;
-  const float* D = dens + ch.dens;
-  float* GD = grad_dens + ch.dens;
-  const uint32_t key = vkey[v];
-  const int lin = (int)(key >> 2), g = (int)(key & 3u);
-  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
-  const int mask = cell_mask_at(W, dim, zc, x, y, z);
-  const T gx[3] = {(T)grad_pos[3 * v], (T)grad_pos[3 * v + 1], (T)grad_pos[3 * v + 2]};
-  // the forward's branch: replay of q_place in FP32
-  int cnt = 0;
-  QefAccum q;
-  if (PLACE == 2) q.init();
-  for (int e = 0; e < 12; ++e) {
-    if (group_of(mask, e) != g) continue;
-    float p[3], n[3];
-    hermite(D, dim, x, y, z, e, PLACE == 2, p, n);
-    ++cnt;
-    if (PLACE == 2) q.add(p, n);
-  }
-  if (cnt == 0) return;
-  bool use_qef = false;
-  QefAdj<T> Q;
-  if (PLACE == 2) {
-    float s[3];
-    QefSolveInfo info;
-    if (q.solve(s, &info))
-      use_qef = s[0] >= (float)x && s[0] <= (float)(x + 1) && s[1] >= (float)y && s[1] <= (float)(y + 1) &&
-                s[2] >= (float)z && s[2] <= (float)(z + 1);
-    if (LIST == 1 && use_qef) {
-      qlist[atomicAdd(qcount, 1u)] = (uint32_t)v;
-      return;
-    }
-    if (use_qef) {
-      if (sizeof(T) == sizeof(float)) {
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            Q.A[r][k] = (T)q.ata[r][k];
-            Q.V[r][k] = (T)info.V[r][k];
-          }
-          Q.sigma[r] = (T)info.sigma[r];
-          Q.inv[r] = (T)info.inv[r];
-          Q.mp[r] = (T)info.mp[r];
-          Q.r[r] = (T)info.r[r];
-        }
-      } else {
-        // the same QEF in FP64: ATA, ATb, mass point, converged eigen pairs
-        double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, b[3] = {0, 0, 0}, m[3] = {0, 0, 0};
-        for (int e = 0; e < 12; ++e) {
-          if (group_of(mask, e) != g) continue;
-          HermiteT<double> h;
-          hermite_t<double>(D, dim, x, y, z, e, true, h);
-          const double d = h.n[0] * h.p[0] + h.n[1] * h.p[1] + h.n[2] * h.p[2];
-#pragma unroll
-          for (int r = 0; r < 3; ++r) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) A[r][k] += h.n[r] * h.n[k];
-            b[r] += d * h.n[r];
-            m[r] += h.p[r];
-          }
-        }
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          m[r] /= (double)cnt;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) Q.A[r][k] = (T)A[r][k];
-        }
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-          Q.mp[r] = (T)m[r];
-          Q.r[r] = (T)(b[r] - (A[r][0] * m[0] + A[r][1] * m[1] + A[r][2] * m[2]));
-        }
-        double w[3], V[3][3];
-        eig3_refine(A, info.V, w, V);
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const double oo = 1.0 / w[i];
-          const double mn = fabs(w[i]) < fabs(oo) ? fabs(w[i]) : fabs(oo);
-          Q.sigma[i] = (T)w[i];
-          Q.inv[i] = (T)(mn >= 0.001 ? oo : 0.0);
-#pragma unroll
-          for (int k = 0; k < 3; ++k) Q.V[k][i] = (T)V[k][i];
-        }
-      }
-    }
-  }
-  // QEF adjoint down to gA (symmetric), gr, gm
-  T gA[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, gr[3] = {0, 0, 0}, gm[3] = {gx[0], gx[1], gx[2]};
-  if (use_qef) {
-    T Pm[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        Pm[r][k] = Q.V[r][0] * Q.inv[0] * Q.V[k][0] + Q.V[r][1] * Q.inv[1] * Q.V[k][1] + Q.V[r][2] * Q.inv[2] * Q.V[k][2];
-    }
-#pragma unroll
-    for (int r = 0; r < 3; ++r) gr[r] = Pm[r][0] * gx[0] + Pm[r][1] * gx[1] + Pm[r][2] * gx[2];
-    T Gs[3][3], M[3][3], F[3][3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) Gs[r][k] = (T)0.5 * (gx[r] * Q.r[k] + gx[k] * Q.r[r]);
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        T s = (T)0;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) s += Q.V[r][a] * Gs[r][k] * Q.V[k][b];
-        }
-        M[a][b] = s;
-        // f(s) = 1/s: (f_a - f_b) / (s_a - s_b) = -f_a f_b (no cancellation for
-        // close eigenvalues) and f'(s) = -f^2; a truncated eigenvalue (f = 0)
-        // beside a kept one takes the quotient
-        const T fa = Q.inv[a], fb = Q.inv[b], sa = Q.sigma[a], sb = Q.sigma[b];
-        if (fa != (T)0 && fb != (T)0)
-          F[a][b] = -fa * fb;
-        else if (a == b || fabs(sa - sb) <= (T)1e-6 * (fabs(sa) + fabs(sb)))
-          F[a][b] = (T)0;
-        else
-          F[a][b] = (fa - fb) / (sa - sb);
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        T s = (T)0;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-#pragma unroll
-          for (int b = 0; b < 3; ++b) s += Q.V[r][a] * F[a][b] * M[a][b] * Q.V[k][b];
-        }
-        gA[r][k] = s - (T)0.5 * (gr[r] * Q.mp[k] + gr[k] * Q.mp[r]);
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < 3; ++r) gm[r] -= Q.A[r][0] * gr[0] + Q.A[r][1] * gr[1] + Q.A[r][2] * gr[2];
-  }
-  const T inv_cnt = (T)1 / (T)cnt;
-  // per hermite pair: g_p, g_n, then into the density
-  for (int e = 0; e < 12; ++e) {
-    if (group_of(mask, e) != g) continue;
-    HermiteT<T> h;
-    hermite_t<T>(D, dim, x, y, z, e, PLACE == 2, h);
-    const int ax = e >> 2;
-    T gp[3], gn[3] = {(T)0, (T)0, (T)0};
-    if (!use_qef) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) gp[k] = gx[k] * inv_cnt;
-    } else {
-      const T d = h.n[0] * h.p[0] + h.n[1] * h.p[1] + h.n[2] * h.p[2];
-      const T gd = gr[0] * h.n[0] + gr[1] * h.n[1] + gr[2] * h.n[2];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        gn[k] = (T)2 * (gA[k][0] * h.n[0] + gA[k][1] * h.n[1] + gA[k][2] * h.n[2]) + d * gr[k] + gd * h.p[k];
-        gp[k] = gd * h.n[k] + gm[k] * inv_cnt;
-      }
-    }
-    T gmu = gp[ax];
-    if (use_qef) {
-      const T nd = h.n[0] * gn[0] + h.n[1] * gn[1] + h.n[2] * gn[2];
-      T gG[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        gG[k] = (gn[k] - h.n[k] * nd) / h.glen;
-        gmu += gG[k] * (h.g1[k] - h.g0[k]);
-      }
-      // central differences at both endpoints: g[a] = (s[hi] - s[lo]) * h
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-#pragma unroll
-        for (int end = 0; end < 2; ++end) {
-          const int* q0 = end ? h.a1 : h.a0;
-          const T w = gG[a] * (end ? h.mu : (T)1 - h.mu);
-          int lo[3] = {q0[0], q0[1], q0[2]}, hi[3] = {q0[0], q0[1], q0[2]};
-          T hh = (T)0.5;
-          if (q0[a] > 0) lo[a]--; else hh = (T)1;
-          if (q0[a] < dim - 1) hi[a]++; else hh = (T)1;
-          atomicAdd(GD + ((int64_t)hi[0] * dim + hi[1]) * dim + hi[2], (float)(w * hh));
-          atomicAdd(GD + ((int64_t)lo[0] * dim + lo[1]) * dim + lo[2], (float)(-w * hh));
-        }
-      }
-    }
-    const T den = (h.s1 - h.s0) * (h.s1 - h.s0);
-    atomicAdd(GD + ((int64_t)h.a0[0] * dim + h.a0[1]) * dim + h.a0[2], (float)(gmu * (-h.s1 / den)));
-    atomicAdd(GD + ((int64_t)h.a1[0] * dim + h.a1[1]) * dim + h.a1[2], (float)(gmu * (h.s0 / den)));
-  }
-}
-
 void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
                       const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount, cudaStream_t st) {
@@ -1239,10 +646,12 @@ void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_ch
                                                grad_dens, qlist, qcount)
   if (placement == 2 && f64 && qlist && qcount) {
     // float pass for the mass-point vertices, then the FP64 QEF adjoint over
-    // the compacted list of QEF-placed ones (no idle lanes in FP64 code)
+    // the compacted list of QEF-placed ones (no idle lanes in FP64 code; its
+    // own translation unit, compiled with FMA contraction)
     cudaMemsetAsync(qcount, 0, sizeof(uint32_t), st);
     BMF_PLACE_BWD(2, float, 1);
-    BMF_PLACE_BWD(2, double, 2);
+    launch_place_bwd_f64_list(d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos, grad_dens, qlist,
+                              qcount, st);
   } else if (placement == 2) {
     if (f64) BMF_PLACE_BWD(2, double, 0); else BMF_PLACE_BWD(2, float, 0);
   } else {
@@ -1262,14 +671,6 @@ void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_ch
 // crossing edge of its group; those quad ids are sorted.  No atomics, no sort
 // pass, deterministic.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int find_chunk_by_vertex(const ChunkDev* __restrict__ chunks, int n, int64_t v) {
-  int lo = 0, hi = n - 1;  // last chunk whose vout <= v (empty chunks share the next one's offset)
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (chunks[mid].vout <= v) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
 
 template <int MODE>
 __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ chunks, int n_chunks,
@@ -1357,7 +758,7 @@ void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const ui
 
 void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
                   const uint32_t* words, const uint32_t* flags, WordScratch ws, cudaStream_t st) {
-  if (mode == 0 && ws.clist) cudaMemsetAsync(ws.ccount, 0, sizeof(uint32_t), st);
+  if (ws.clist) cudaMemsetAsync(ws.ccount, 0, sizeof(uint32_t), st);
   if (mode == 0) k_count<0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
   else k_count<1><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
 }
@@ -1459,6 +860,105 @@ __global__ void __launch_bounds__(256, 3) k_emit_cells_r(const ChunkDev* __restr
   }
 }
 
+// Mode Q emission over the work list, one thread per active cell: the cell's
+// group vertices (ids from the word base and the group-count planes; mass
+// point / centre placed here, QEF by k_place_qef when keys are kept) and the
+// quads of the interior crossing edges its sample owns (slot from the word's
+// index base and the popcounts of the owned crossings below it) -- exactly
+// what k_emit<1,P> writes for the cell's lane.
+template <int PLACE>
+__global__ void __launch_bounds__(256, 3) k_emit_cells_q(const ChunkDev* __restrict__ chunks,
+                                                         const uint32_t* __restrict__ words,
+                                                         const float* __restrict__ dens, WordScratch ws, MeshOut out) {
+  __shared__ SmemTabs T;
+  load_tabs(T);
+  const int64_t n = min((int64_t)*ws.ccount, ws.clist_cap);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint2 ent = ws.clist[i];
+    const ChunkDev ch = chunks[ent.x];
+    const int dim = ch.dim, zc = ch.zc;
+    const int lin = (int)ent.y;
+    const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+    const int zb = z >> 5, lane = z & 31;
+    const uint32_t lt = lane_lt(lane);
+    const uint32_t* W = words + ch.words;
+    const uint32_t* vbase = ws.vcnt + ch.words;
+    const float* D = dens + ch.dens;
+    const int64_t wo = ((int64_t)x * dim + y) * zc + zb;
+    const bool interior = x <= dim - 2 && y <= dim - 2 && z <= dim - 2;
+    const int mask = interior ? cell_mask_at(W, dim, zc, x, y, z) : 0;
+    const uint64_t gw = T.grp[mask];
+    const int ng = (int)((gw >> 48) & 0xF);
+    if (ng) {
+      const uint32_t* pl = ws.gpl + 3 * (ch.words + wo);
+      uint32_t vid = __ldg(vbase + wo) + __popc(__ldg(pl) & lt) + 2 * __popc(__ldg(pl + 1) & lt) +
+                     4 * __popc(__ldg(pl + 2) & lt);
+      const int nc = dim - 1;
+      const uint8_t bnd = (x == 0 || y == 0 || z == 0 || x == nc - 1 || y == nc - 1 || z == nc - 1);
+      for (int g = 0; g < ng; ++g, ++vid) {
+        const int64_t gv = ch.vout + vid;
+        if (gv >= out.vcap) continue;
+        if (PLACE != 2 || !out.vkey) {
+          float P[3];
+          q_place<PLACE>(D, dim, x, y, z, mask, g, P);
+          out.pos[3 * gv] = P[0];
+          out.pos[3 * gv + 1] = P[1];
+          out.pos[3 * gv + 2] = P[2];
+        }
+        if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
+        if (out.boundary) out.boundary[gv] = bnd;
+        if (out.vkey) out.vkey[gv] = ((uint32_t)lin << 2) | (uint32_t)g;
+        if (out.valence) {
+          int val = 0;
+          for (int e = 0; e < 12; ++e) {
+            if ((int)((gw >> (4 * e)) & 0xF) != g) continue;
+            const int c0 = edge_c0(e);
+            val += q_edge_interior(dim, x + ((c0 >> 2) & 1), y + ((c0 >> 1) & 1), z + (c0 & 1), e >> 2);
+          }
+          out.valence[gv] = (uint8_t)val;
+        }
+      }
+    }
+    uint32_t Xi, Yi, Zi;
+    q_quad_words(W, dim, zc, x, y, zb, Xi, Yi, Zi);
+    const int own = (int)(((Xi >> lane) & 1u) | (((Yi >> lane) & 1u) << 1) | (((Zi >> lane) & 1u) << 2));
+    if (!own) continue;
+    int64_t gi = ch.iout + (int64_t)__ldg(ws.icnt + ch.words + wo) +
+                 4 * (int64_t)(__popc(Xi & lt) + __popc(Yi & lt) + __popc(Zi & lt));
+    const bool in0 = ((word_at(W, dim, zc, x, y, zb) >> lane) & 1u) != 0u;
+    for (int a = 0; a < 3; ++a) {
+      if (!((own >> a) & 1)) continue;
+      const int b = (a + 1) % 3, cax = (a + 2) % 3;
+      uint32_t q[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int ob = (k == 0 || k == 3) ? -1 : 0, oc = (k < 2) ? -1 : 0;
+        int cc[3] = {x, y, z};
+        cc[b] += ob;
+        cc[cax] += oc;
+        int lo[3] = {0, 0, 0};
+        lo[b] = -ob;
+        lo[cax] = -oc;
+        const int e = a == 0 ? 2 * lo[1] + lo[2] : (a == 1 ? 4 + 2 * lo[0] + lo[2] : 8 + 2 * lo[0] + lo[1]);
+        const int cm = cell_mask_at(W, dim, zc, cc[0], cc[1], cc[2]);
+        q[k] = q_vertex_base(vbase, ws.gpl + 3 * ch.words, dim, zc, cc[0], cc[1], cc[2]) +
+               (uint32_t)((T.grp[cm] >> (4 * e)) & 0xF);
+      }
+      if (!in0) {
+        const uint32_t t = q[1];
+        q[1] = q[3];
+        q[3] = t;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k, ++gi)
+        if (gi < out.icap) {
+          out.idx[gi] = q[k];
+          if (out.idx_global) out.idx_global[gi] = (uint32_t)(ch.vout + q[k]);
+        }
+    }
+  }
+}
+
 // Mode Q QEF placement, one thread per vertex (dense lanes, unlike the
 // warp-per-word emit where only surface cells' lanes work): the same
 // q_place<2> on the vertex's cell and group, decoded from its key.
@@ -1493,6 +993,19 @@ int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks,
     k_emit_cells_r<<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
   } else if (mode == 0) {
     k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
+  } else if (ws.clist) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (placement == 2 && (!out.vkey || !d_counts)) out.vkey = nullptr;
+    if (placement == 0) k_emit_cells_q<0><<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+    else if (placement == 1) k_emit_cells_q<1><<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+    else k_emit_cells_q<2><<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+    if (placement == 2 && out.vkey && out.vcap > 0) {
+      k_place_qef<<<(int)((out.vcap + 127) / 128), 128, 0, st>>>(d_chunks, n_chunks, words, dens, out.vkey, d_counts,
+                                                                out.vcap, out.pos);
+      return 2;
+    }
   } else if (placement == 0) {
     k_emit<1, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else if (placement == 1) {

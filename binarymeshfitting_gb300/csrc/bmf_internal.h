@@ -31,9 +31,11 @@ struct WordScratch {
   uint32_t* vcnt;   // vertices hosted by the word's 32 cells; scanned in place to the chunk-local base
   uint32_t* icnt;   // indices emitted by the word's cells; scanned in place
   uint32_t* gpl;    // 3 bit-planes of the per-cell triangle (Mode R) / vertex-group (Mode Q) count
-  // Mode R work list (nullable): every cell that owns a vertex or emits a
-  // triangle, as {chunk, (x*dim + y)*dim + z}, in no particular order;
-  // *ccount (zeroed before the count kernel) entries, at most clist_cap kept.
+  // Work list (nullable): every cell that owns a vertex or emits a primitive
+  // (Mode R: owned crossing or triangles; Mode Q: vertex groups or owned
+  // interior crossings), as {chunk, (x*dim + y)*dim + z}, in no particular
+  // order; *ccount (zeroed before the count kernel) entries, at most
+  // clist_cap kept.  Its size bound is vcap + icap / prim_size + 1.
   uint2* clist;
   uint32_t* ccount;
   int64_t clist_cap;
@@ -129,6 +131,10 @@ int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_coun
 // Adjoint of Mode Q placement (placement 1 mass point, 2 QEF; f64: the QEF
 // derivative from an FP64 re-solve); accumulates into grad_dens (the caller
 // clears it).
+// The FP64 list pass of launch_place_bwd (bmf_adjoint64.cu).
+void launch_place_bwd_f64_list(const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, const float* dens,
+                               const uint32_t* vkey, const int64_t* d_counts, int64_t vcap, const float* grad_pos,
+                               float* grad_dens, uint32_t* qlist, uint32_t* qcount, cudaStream_t st);
 // qlist (vcap entries) + qcount: scratch of the two-pass FP64 form (nullable:
 // one pass, idle lanes in the FP64 code).
 void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
