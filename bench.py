@@ -29,12 +29,43 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "chunks/s (mixed-LOD batch vs per-chunk, same GB300, exact topology)"
-FP32_OPS_PER_SAMPLE = 337  # terrain FBM, 5 octaves, counted from the kernel source
+# FP32 operations of the line-separable FBM (counted from the kernel source,
+# mul and add separately since contraction is off)
+OPS_PER_SAMPLE_OCTAVE = 9   # l0, l1 (2 each), l1 - l0, w * (.), + l0, amp * n, sum +
+OPS_PER_SAMPLE = 2          # (py - h) - a * sum: the product and the difference
+OPS_PER_LINE_OCTAVE = 24    # xs, ys, 2 floor, xf, yf, 2 fade (7 each), x1, y1, fr, amp
+OPS_PER_LINE = 1            # py - h
+OPS_PER_LAYER = 22          # 4 corner sums s, alpha and beta (3 lerps of 3 operations each)
 # DRAM bytes (read + write) per sample of k_fill_terrain from one ncu capture on
 # the 256-chunk update (110,890,368 samples, 47.65 MB read + 448.53 MB written):
 # traffic grows with the samples, so a full launch is scaled from it
 # (profiles/k_fill_terrain_lod_update_256.txt)
 FILL_DRAM_BYTES_PER_SAMPLE = (47.65e6 + 448.53e6) / 110_890_368
+
+
+def fill_fp32_ops(rows, params):
+    """Algorithmic FP32 operations of one terrain fill over the update: per
+    sample and octave, per line and octave, and one layer set-up per z-lattice
+    cell a line enters (two for its first cell or after a jump of more than
+    one cell), with z-lattice cells taken from float coordinates as the
+    kernels compute them."""
+    freq, lac, octaves = np.float32(params[2]), np.float32(params[3]), int(params[5])
+    total = 0
+    for (oz, scale, dim), n in zip(*np.unique(rows[:, [2, 3, 4]], axis=0, return_counts=True)):
+        dim = int(dim)
+        pz = np.float32(oz) + np.arange(dim, dtype=np.float32) * np.float32(scale)
+        layers = 0
+        fr = freq
+        for _ in range(octaves):
+            cell = np.floor(pz * fr).astype(np.int64)
+            step = np.diff(cell)
+            layers += 2 + int((step == 1).sum()) + 2 * int((step > 1).sum())
+            fr = np.float32(fr * lac)
+        lines = dim * dim
+        per_chunk = (lines * dim * (OPS_PER_SAMPLE_OCTAVE * octaves + OPS_PER_SAMPLE)
+                     + lines * (OPS_PER_LINE_OCTAVE * octaves + OPS_PER_LINE) + lines * layers * OPS_PER_LAYER)
+        total += int(n) * per_chunk
+    return total
 
 
 def parse():
@@ -337,7 +368,8 @@ def run_gb300(args):
     hbm_peak, sm_max, peak_kind = measured_peaks()
     clock_mhz = clk["sm_mhz"] or sm_max
     fp32_peak = 152 * 128 * sm_max * 1e6 / 1e12  # nominal FP32 instruction rate at max clock, Tops/s
-    fill_achieved = FP32_OPS_PER_SAMPLE * samples / (st_ms[0] / 1000.0) / 1e12
+    fill_ops = fill_fp32_ops(rows, workloads.TERRAIN_PARAMS)
+    fill_achieved = fill_ops / (st_ms[0] / 1000.0) / 1e12
     # algorithmic HBM bytes of the extraction kernels (count + scan + offsets + emit)
     per_vertex = 12 + 1 + 1 + 8 + (12 if normals else 0)
     ext_bytes = words * (4 + 8 + 8 + 4) + nv * per_vertex + ni * 4
@@ -358,7 +390,7 @@ def run_gb300(args):
                 "peak_kind": "nominal 152 SM x 128 FP32 lanes x %.0f MHz (no measured FP32 peak exists)" % sm_max,
                 "traffic": FILL_DRAM_BYTES_PER_SAMPLE * samples, "traffic_unit": "bytes per launch (scaled ncu)",
                 "algorithmic_bytes": 4 * samples + 4 * words, "ms_per_launch": st_ms[0],
-                "flops_per_launch": FP32_OPS_PER_SAMPLE * samples,
+                "flops_per_launch": fill_ops, "flops_per_sample": fill_ops / samples,
                 "extraction_hbm": {"kernels": "count+scan+offsets+emit", "achieved": ext_gbs, "peak": hbm_peak,
                                    "unit": "GB/s", "frac": ext_gbs / hbm_peak, "bytes": ext_bytes,
                                    "ms": ext_ms, "peak_kind": peak_kind},
@@ -449,7 +481,7 @@ def run_gb300(args):
                 "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e, "per_chunk": per_chunk,
                 "gpu_launches": launches, "clocks": clk, "bwd_fwd": bwd_fwd,
                 "tuning": {"chosen": tuned, "candidates_ms": tune_ms,
-                           "candidates": "fill (mode, run): (0,8) (1,4) (1,8) (1,16) (2,4) (2,8) (2,16); "
+                           "candidates": "fill (mode, run): (0,8) (1,4) (1,8) (1,16) (1,32) (2,4) (2,8) (2,16) (2,32); "
                                          "sweep block: 128 256 512"}}
         print(json.dumps(line), flush=True)
     if b is not None:

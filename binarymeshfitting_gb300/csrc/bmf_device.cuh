@@ -108,78 +108,94 @@ __device__ __forceinline__ float fade(float t) {
 }
 __device__ __forceinline__ float lerp_t(float t, float a, float b) { return a + t * (b - a); }
 
-// Gradient of K. Perlin's improved noise: +/-u +/-v with u, v picked from
-// (x, y, z) by the low four hash bits.
-__device__ __forceinline__ float grad(int h, float x, float y, float z) {
-  const float u = (h & 8) ? y : x;
-  const float v = (h & 12) == 0 ? y : (((h & 15) == 12 || (h & 15) == 14) ? x : z);
-  const float su = __int_as_float(__float_as_int(u) ^ ((h & 1) << 31));
-  const float sv = __int_as_float(__float_as_int(v) ^ ((h & 2) << 30));
-  return su + sv;
+// ---------------------------------------------------------------------------
+// Improved gradient noise (K. Perlin, SIGGRAPH 2002) in line-separable form.
+//
+// A corner gradient grad(h, x, y, z) = (+/-u) + (+/-v) with u in {x, y} and v in
+// {x, y, z} is written s + c * z: s = (+/-u) + (+/-v) and c = +0 when v is x or
+// y; s = +/-u and c = +/-1 when v is z.  lerp is linear, so a z-layer's x/y
+// interpolant of the four corners is alpha + beta * zk exactly, with
+//     alpha = lerp(v, lerp(u, s00, s10), lerp(u, s01, s11))   (beta: the c's),
+// and the noise value is  l0 = alpha0 + beta0 * zf,  l1 = alpha1 + beta1 * (zf - 1),
+// l0 + w (l1 - l0).  In exact arithmetic this is the textbook value; in float it
+// differs from the textbook order by rounding only, and the CPU oracle evaluates
+// exactly these operations (compiled without contraction), so samples agree
+// bit for bit.  alpha and beta depend on x, y and the lattice cell Z, not on the
+// sample's own z: a z-line sets them up once per lattice cell, and the layer-1
+// pair of cell Z is the layer-0 pair of cell Z + 1 (same hashes, same operations).
+//
+// Per hash h the gradient is coded for byte permutes (seg_grad_code):
+//   x = selector of u (x or y) | sign of u << 31
+//   y = selector of v (x or y) | (v == z ? 1 : sign of v) << 31
+//   z = 0 when v == z (drops v, leaving the -0.0 that keeps s = +/-u exactly), else all ones
+//   w = the bits of c: +/-1.0f when v == z, else +0.0f
+// Tables are 512 entries, entry i coding perm[i & 255], so hash chains index
+// them without masks.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline uint4 seg_grad_code(int h) {
+  h &= 15;
+  const bool vz = (h & 12) != 0 && (h & 13) != 12;
+  const uint32_t sel_x = 0x3210u, sel_y = 0x7654u;
+  uint4 t;
+  t.x = ((h & 8) ? sel_y : sel_x) | ((uint32_t)(h & 1) << 31);
+  t.y = ((h & 12) == 0 ? sel_y : sel_x) | ((vz ? 1u : (uint32_t)((h >> 1) & 1)) << 31);
+  t.z = vz ? 0u : 0xFFFFFFFFu;
+  t.w = vz ? (0x3F800000u | ((uint32_t)((h >> 1) & 1) << 31)) : 0u;
+  return t;
 }
 
-// Improved gradient noise (Perlin, SIGGRAPH 2002); perm lives in shared memory
-// as 32-bit entries.
-__device__ __forceinline__ float perlin(const int* __restrict__ perm, float x, float y, float z) {
+// s and c of one corner at lattice offsets (xc, yc).
+__device__ __forceinline__ void seg_corner(uint4 t, float xc, float yc, float& s, float& c) {
+  const uint32_t xb = __float_as_uint(xc), yb = __float_as_uint(yc);
+  const float su = __uint_as_float(__byte_perm(xb, yb, t.x) ^ (t.x & 0x80000000u));
+  const float sv = __uint_as_float((__byte_perm(xb, yb, t.y) & t.z) ^ (t.y & 0x80000000u));
+  s = su + sv;
+  c = __uint_as_float(t.w);
+}
+
+// alpha / beta of one z-layer from the hashes of its four corners
+// (h00 = AA + k, h10 = BA + k, h01 = AB + k, h11 = BB + k).
+__device__ __forceinline__ void layer_coeffs(const uint4* __restrict__ gtab, int h00, int h10, int h01, int h11,
+                                             float xf, float yf, float x1, float y1, float u, float v, float& a,
+                                             float& b) {
+  float s00, c00, s10, c10, s01, c01, s11, c11;
+  seg_corner(gtab[h00], xf, yf, s00, c00);
+  seg_corner(gtab[h10], x1, yf, s10, c10);
+  seg_corner(gtab[h01], xf, y1, s01, c01);
+  seg_corner(gtab[h11], x1, y1, s11, c11);
+  const float sa = lerp_t(u, s00, s10), sb = lerp_t(u, s01, s11);
+  a = lerp_t(v, sa, sb);
+  const float ca = lerp_t(u, c00, c10), cb = lerp_t(u, c01, c11);
+  b = lerp_t(v, ca, cb);
+}
+
+// One noise value (perm2: the permutation duplicated to 512 entries).
+__device__ __forceinline__ float perlin(const int* __restrict__ perm2, const uint4* __restrict__ gtab, float x, float y,
+                                        float z) {
   const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
   const int X = ((int)fx) & 255, Y = ((int)fy) & 255, Z = ((int)fz) & 255;
   x = x - fx;
   y = y - fy;
   z = z - fz;
   const float u = fade(x), v = fade(y), w = fade(z);
-  const int A = perm[X] + Y, B = perm[(X + 1) & 255] + Y;
-  const int AA = perm[A & 255] + Z, AB = perm[(A + 1) & 255] + Z;
-  const int BA = perm[B & 255] + Z, BB = perm[(B + 1) & 255] + Z;
+  const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
+  const int AA = perm2[A] + Z, AB = perm2[A + 1] + Z, BA = perm2[B] + Z, BB = perm2[B + 1] + Z;
   const float x1 = x - 1.0f, y1 = y - 1.0f, z1 = z - 1.0f;
-  const float g000 = grad(perm[AA & 255], x, y, z), g100 = grad(perm[BA & 255], x1, y, z);
-  const float g010 = grad(perm[AB & 255], x, y1, z), g110 = grad(perm[BB & 255], x1, y1, z);
-  const float g001 = grad(perm[(AA + 1) & 255], x, y, z1), g101 = grad(perm[(BA + 1) & 255], x1, y, z1);
-  const float g011 = grad(perm[(AB + 1) & 255], x, y1, z1), g111 = grad(perm[(BB + 1) & 255], x1, y1, z1);
-  const float l00 = lerp_t(u, g000, g100), l10 = lerp_t(u, g010, g110);
-  const float l01 = lerp_t(u, g001, g101), l11 = lerp_t(u, g011, g111);
-  const float l0 = lerp_t(v, l00, l10), l1 = lerp_t(v, l01, l11);
-  return lerp_t(w, l0, l1);
+  float a0, b0, a1, b1;
+  layer_coeffs(gtab, AA, BA, AB, BB, x, y, x1, y1, u, v, a0, b0);
+  layer_coeffs(gtab, AA + 1, BA + 1, AB + 1, BB + 1, x, y, x1, y1, u, v, a1, b1);
+  const float l0 = a0 + b0 * z;
+  const float l1 = a1 + b1 * z1;
+  return l0 + w * (l1 - l0);
 }
 
-// ---------------------------------------------------------------------------
-// Run evaluation of the terrain FBM: R consecutive z-samples of one (x, y)
-// line, with every x/y-dependent term computed once per octave.  Results are
-// bit-identical to perlin() per sample: the same float operations in the same
-// order; only the integer bookkeeping is reorganised:
-//  * perm2 is the permutation duplicated to 512 entries, so the hash chain
-//    A = P[X]+Y, AA = P[A]+Z, P[AA+1] indexes it without "& 255" masks;
-//  * gcode[i] encodes grad() for hash perm2[i]: .x low 16 bits = byte-permute
-//    selector picking u from (x, y), high 16 = selector picking t from (y, z);
-//    .y low 16 = selector picking v from (t, x), bit 31 = negate u, bit 30 =
-//    negate v.  grad = (+/-u) + (+/-v) exactly as in perlin().
-// ---------------------------------------------------------------------------
 constexpr int kRun = 4;
 
-__host__ __device__ inline uint2 grad_code(int h) {
-  h &= 15;
-  const uint32_t sel_u = (h & 8) ? 0x7654u : 0x3210u;  // y : x
-  const uint32_t sel_t = (h & 12) == 0 ? 0x3210u : 0x7654u;  // y : z
-  const uint32_t sel_v = (h & 13) == 12 ? 0x7654u : 0x3210u;  // x : t
-  uint2 c;
-  c.x = sel_u | (sel_t << 16);
-  c.y = sel_v | ((uint32_t)(h & 1) << 31) | ((uint32_t)((h >> 1) & 1) << 30);
-  return c;
-}
-
-__device__ __forceinline__ float grad_coded(uint2 c, float x, float y, float z) {
-  const uint32_t xb = __float_as_uint(x), yb = __float_as_uint(y), zb = __float_as_uint(z);
-  uint32_t u = __byte_perm(xb, yb, c.x);
-  const uint32_t t = __byte_perm(yb, zb, c.x >> 16);
-  uint32_t v = __byte_perm(t, xb, c.y);
-  u ^= c.y & 0x80000000u;
-  v ^= (c.y << 1) & 0x80000000u;
-  return __uint_as_float(u) + __uint_as_float(v);
-}
-
 // Terrain field (y - h) - a * FBM over a run of n <= kRun samples at
-// z-coordinates pz[k]; px, py are the line's world x, y.
+// z-coordinates pz[k]; px, py are the line's world x, y.  Every x/y-dependent
+// term is computed once per octave, and alpha / beta once per lattice cell.
 __device__ __forceinline__ void terrain_run(const FieldDev& f, const int* __restrict__ perm2,
-                                            const uint2* __restrict__ gcode, float px, float py, const float* pz,
+                                            const uint4* __restrict__ gtab, float px, float py, const float* pz,
                                             int n, float* out) {
   float sum[kRun];
 #pragma unroll
@@ -195,6 +211,8 @@ __device__ __forceinline__ void terrain_run(const FieldDev& f, const int* __rest
     const float x1 = xf - 1.0f, y1 = yf - 1.0f;
     const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
     const int pA = perm2[A], pA1 = perm2[A + 1], pB = perm2[B], pB1 = perm2[B + 1];
+    float a0 = 0.0f, b0 = 0.0f, a1 = 0.0f, b1 = 0.0f;
+    int Zp = -1;
 #pragma unroll
     for (int k = 0; k < kRun; ++k) {
       if (k >= n) break;
@@ -204,15 +222,14 @@ __device__ __forceinline__ void terrain_run(const FieldDev& f, const int* __rest
       const float zf = zs - fz;
       const float w = fade(zf);
       const float z1 = zf - 1.0f;
-      const int AA = pA + Z, AB = pA1 + Z, BA = pB + Z, BB = pB1 + Z;
-      const float g000 = grad_coded(gcode[AA], xf, yf, zf), g100 = grad_coded(gcode[BA], x1, yf, zf);
-      const float g010 = grad_coded(gcode[AB], xf, y1, zf), g110 = grad_coded(gcode[BB], x1, y1, zf);
-      const float g001 = grad_coded(gcode[AA + 1], xf, yf, z1), g101 = grad_coded(gcode[BA + 1], x1, yf, z1);
-      const float g011 = grad_coded(gcode[AB + 1], xf, y1, z1), g111 = grad_coded(gcode[BB + 1], x1, y1, z1);
-      const float l00 = lerp_t(u, g000, g100), l10 = lerp_t(u, g010, g110);
-      const float l01 = lerp_t(u, g001, g101), l11 = lerp_t(u, g011, g111);
-      const float l0 = lerp_t(v, l00, l10), l1 = lerp_t(v, l01, l11);
-      const float nv = lerp_t(w, l0, l1);
+      if (Z != Zp) {
+        Zp = Z;
+        layer_coeffs(gtab, pA + Z, pB + Z, pA1 + Z, pB1 + Z, xf, yf, x1, y1, u, v, a0, b0);
+        layer_coeffs(gtab, pA + Z + 1, pB + Z + 1, pA1 + Z + 1, pB1 + Z + 1, xf, yf, x1, y1, u, v, a1, b1);
+      }
+      const float l0 = a0 + b0 * zf;
+      const float l1 = a1 + b1 * z1;
+      const float nv = l0 + w * (l1 - l0);
       sum[k] = sum[k] + amp * nv;
     }
     fr = fr * f.p[3];
@@ -229,7 +246,8 @@ __device__ __forceinline__ float len3(float x, float y, float z) {
 }
 
 // Evaluates a density field at world position (px, py, pz).
-__device__ __forceinline__ float eval_field(const FieldDev& f, const int* __restrict__ perm, float px, float py,
+__device__ __forceinline__ float eval_field(const FieldDev& f, const int* __restrict__ perm,
+                                            const uint4* __restrict__ gtab, float px, float py,
                                             float pz) {
   switch (f.kind) {
     case BMF_FIELD_SPHERE_WAVE: {
@@ -242,7 +260,7 @@ __device__ __forceinline__ float eval_field(const FieldDev& f, const int* __rest
       const int oct = (int)f.p[5];
       float sum = 0.0f, amp = 1.0f, fr = f.p[2];
       for (int o = 0; o < oct; ++o) {
-        const float n = perlin(perm, px * fr, py * fr, pz * fr);
+        const float n = perlin(perm, gtab, px * fr, py * fr, pz * fr);
         sum = sum + amp * n;
         fr = fr * f.p[3];
         amp = amp * f.p[4];

@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
                                                       uint32_t* __restrict__ words, uint32_t* __restrict__ flags) {
   extern __shared__ uint32_t sw[];
   __shared__ int perm2[512];
-  __shared__ uint2 gcode[512];
+  __shared__ uint4 gtab[512];
   const int u = blockIdx.x;
   const int c = find_chunk(unit_start, n_chunks, u);
   const ChunkDev ch = chunks[c];
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
   const int nw = dim * zc;
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
     perm2[i] = field.perm[i & 255];
-    gcode[i] = grad_code(field.perm[i & 255]);
+    gtab[i] = seg_grad_code(field.perm[i & 255]);
   }
   for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = 0u;
   __syncthreads();
@@ -68,11 +68,11 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
 #pragma unroll
       for (int k = 0; k < kRun; ++k) pz[k] = ch.oz + (float)(z0 + k) * ch.scale;
       if (field.kind == BMF_FIELD_TERRAIN_FBM) {
-        terrain_run(field, perm2, gcode, px, py, pz, n, v);
+        terrain_run(field, perm2, gtab, px, py, pz, n, v);
       } else {
 #pragma unroll
         for (int k = 0; k < kRun; ++k)
-          if (k < n) v[k] = eval_field(field, perm2, px, py, pz[k]);
+          if (k < n) v[k] = eval_field(field, perm2, gtab, px, py, pz[k]);
       }
       if (dens_out) {
 #pragma unroll
@@ -112,53 +112,25 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
 // once per CTA into shared memory, and the z-lattice cell changes at the same
 // sample for every lane (a warp-uniform branch).
 //
-// Between two changes of Z a corner's hash, hence its gradient, is fixed, so
-// the gradient is set up once per such segment as g = s + cz * z: for
-// v = +/-z, s = +/-u and cz = +/-1; otherwise s = (+/-u) + (+/-v) and
-// cz = -0.0 (corners at zf >= 0) or +0.0 (corners at zf - 1 < 0), which makes
-// cz * z a zero of the sign that leaves s unchanged.  Every value is
-// bit-identical to perlin()'s (+/-u) + (+/-v), including signed zeros, and
-// the per-sample gradient work moves from byte permutes on the integer pipe to
-// one multiply and one add.
+// The noise is the line-separable form of bmf_device.cuh: per octave a
+// sample costs l0 = alpha0 + beta0 * zf, l1 = alpha1 + beta1 * (zf - 1),
+// l0 + w (l1 - l0) and the accumulation, nine FP32 operations.  alpha / beta
+// change only when the lattice cell Z does; when Z advances by one, the old
+// layer-1 pair becomes the new layer-0 pair and only layer 1 is set up.
 //
 // Items come from a device queue (persistent CTAs grab the next item with an
 // atomic ticket; the queue is ordered largest chunks first) or, with no queue,
 // one CTA per item.
 // ---------------------------------------------------------------------------
-// RUN (z-samples per step; 4, 8 or 16, dividing 32 so that a run's inside
+// RUN (z-samples per step; 4, 8, 16 or 32, dividing 32 so that a run's inside
 // bits land in one word) is the tile height the batch autotuner picks.
 constexpr int kFillLines = 256; // lines per item = threads per CTA
 constexpr int kMaxOctaves = 32;
-constexpr int kMaxFillRun = 16;
+constexpr int kMaxFillRun = 32;
 // z terms {zf, zf - 1, fade(zf), Z} per (octave, z): for every z of the
 // item's lines at once when octaves * dim fit, else per run
 constexpr int kZtEntries = 1024;
 static_assert(kZtEntries >= kMaxOctaves * kMaxFillRun, "per-run z terms fit");
-
-// Per hash h: x = u selector (x or y) | sign of u << 31; y = v selector (x or
-// y) | (v == z ? 1 : sign of v) << 31; z = 0 when v == z else all ones (keeps
-// v); w = cz bits for a corner at zf: +/-1.0f when v == z else -0.0f.
-__host__ __device__ inline uint4 seg_grad_code(int h) {
-  h &= 15;
-  const bool vz = (h & 12) != 0 && (h & 13) != 12;
-  const uint32_t sel_x = 0x3210u, sel_y = 0x7654u;
-  uint4 t;
-  t.x = ((h & 8) ? sel_y : sel_x) | ((uint32_t)(h & 1) << 31);
-  t.y = ((h & 12) == 0 ? sel_y : sel_x) | ((vz ? 1u : (uint32_t)((h >> 1) & 1)) << 31);
-  t.z = vz ? 0u : 0xFFFFFFFFu;
-  t.w = vz ? (0x3F800000u | ((uint32_t)((h >> 1) & 1) << 31)) : 0x80000000u;
-  return t;
-}
-
-// s and cz of one corner at lattice offsets (xc, yc); dz = corner at zf - 1.
-template <int DZ>
-__device__ __forceinline__ void seg_corner(uint4 t, float xc, float yc, float& s, float& cz) {
-  const uint32_t xb = __float_as_uint(xc), yb = __float_as_uint(yc);
-  const float su = __uint_as_float(__byte_perm(xb, yb, t.x) ^ (t.x & 0x80000000u));
-  const float sv = __uint_as_float((__byte_perm(xb, yb, t.y) & t.z) ^ (t.y & 0x80000000u));
-  s = su + sv;
-  cz = __uint_as_float(DZ ? (t.w & ~t.z) : t.w);
-}
 
 template <int kFillRun>
 __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __restrict__ chunks,
@@ -240,7 +212,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         const float x1 = xf - 1.0f, y1 = yf - 1.0f;
         const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
         const int pA = perm2[A], pA1 = perm2[A + 1], pB = perm2[B], pB1 = perm2[B + 1];
-        float s[8], cz[8];
+        float a0 = 0.0f, b0 = 0.0f, a1 = 0.0f, b1 = 0.0f;
         int Zp = -1;
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) {
@@ -248,26 +220,20 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
           const float4 t = zt[o * zt_o + zt_k + k];
           const int Z = __float_as_int(t.w);
           if (Z != Zp) {  // same for every lane of the CTA
+            const int Z1 = Z + 1;
+            if (Zp >= 0 && Z == ((Zp + 1) & 255)) {  // the next cell: its layer 0 is the old layer 1
+              a0 = a1;
+              b0 = b1;
+            } else {
+              layer_coeffs(gtab, pA + Z, pB + Z, pA1 + Z, pB1 + Z, xf, yf, x1, y1, u, v, a0, b0);
+            }
+            layer_coeffs(gtab, pA + Z1, pB + Z1, pA1 + Z1, pB1 + Z1, xf, yf, x1, y1, u, v, a1, b1);
             Zp = Z;
-            const int AA = pA + Z, AB = pA1 + Z, BA = pB + Z, BB = pB1 + Z;
-            seg_corner<0>(gtab[AA], xf, yf, s[0], cz[0]);
-            seg_corner<0>(gtab[BA], x1, yf, s[1], cz[1]);
-            seg_corner<0>(gtab[AB], xf, y1, s[2], cz[2]);
-            seg_corner<0>(gtab[BB], x1, y1, s[3], cz[3]);
-            seg_corner<1>(gtab[AA + 1], xf, yf, s[4], cz[4]);
-            seg_corner<1>(gtab[BA + 1], x1, yf, s[5], cz[5]);
-            seg_corner<1>(gtab[AB + 1], xf, y1, s[6], cz[6]);
-            seg_corner<1>(gtab[BB + 1], x1, y1, s[7], cz[7]);
           }
           const float zf = t.x, z1 = t.y, w = t.z;
-          const float g000 = s[0] + cz[0] * zf, g100 = s[1] + cz[1] * zf;
-          const float g010 = s[2] + cz[2] * zf, g110 = s[3] + cz[3] * zf;
-          const float g001 = s[4] + cz[4] * z1, g101 = s[5] + cz[5] * z1;
-          const float g011 = s[6] + cz[6] * z1, g111 = s[7] + cz[7] * z1;
-          const float l00 = lerp_t(u, g000, g100), l10 = lerp_t(u, g010, g110);
-          const float l01 = lerp_t(u, g001, g101), l11 = lerp_t(u, g011, g111);
-          const float l0 = lerp_t(v, l00, l10), l1 = lerp_t(v, l01, l11);
-          sum[k] = sum[k] + amp * lerp_t(w, l0, l1);
+          const float l0 = a0 + b0 * zf;
+          const float l1 = a1 + b1 * z1;
+          sum[k] = sum[k] + amp * (l0 + w * (l1 - l0));
         }
         fr = fr * lac;
         amp = amp * gain;
@@ -320,6 +286,7 @@ static void fill_terrain_smem_optin() {
   cudaFuncSetAttribute(k_fill_terrain<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
   cudaFuncSetAttribute(k_fill_terrain<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
   cudaFuncSetAttribute(k_fill_terrain<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
+  cudaFuncSetAttribute(k_fill_terrain<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
   if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
@@ -335,6 +302,8 @@ void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items,
     k_fill_terrain<4><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
   else if (run == 16)
     k_fill_terrain<16><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+  else if (run == 32)
+    k_fill_terrain<32><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
   else
     k_fill_terrain<8><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
 }
@@ -350,6 +319,8 @@ int fill_terrain_resident_ctas(int run) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4>, kFillLines, kStageBytes);
   else if (run == 16)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16>, kFillLines, kStageBytes);
+  else if (run == 32)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<32>, kFillLines, kStageBytes);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8>, kFillLines, kStageBytes);
   return sms * (per_sm > 0 ? per_sm : 1);

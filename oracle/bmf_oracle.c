@@ -92,8 +92,10 @@ static float grad(int h, float x, float y, float z) {
   return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
 }
 
-/* Improved gradient noise (K. Perlin, "Improving Noise", SIGGRAPH 2002). */
-float bmfo_perlin(const uint8_t perm[256], float x, float y, float z) {
+/* Improved gradient noise (K. Perlin, "Improving Noise", SIGGRAPH 2002),
+ * textbook evaluation order: the eight corner gradients, then lerps along x,
+ * y and z.  Kept as the precision yardstick of bmfo_perlin (tests). */
+float bmfo_perlin_textbook(const uint8_t perm[256], float x, float y, float z) {
   float fx = floorf(x), fy = floorf(y), fz = floorf(z);
   int X = ((int)fx) & 255, Y = ((int)fy) & 255, Z = ((int)fz) & 255;
   x = x - fx;
@@ -113,6 +115,68 @@ float bmfo_perlin(const uint8_t perm[256], float x, float y, float z) {
   float l01 = lerpf(u, g001, g101), l11 = lerpf(u, g011, g111);
   float l0 = lerpf(v, l00, l10), l1 = lerpf(v, l01, l11);
   return lerpf(w, l0, l1);
+}
+
+/* Gradient of hash h split into its x/y part s and its z coefficient c:
+ * grad(h, x, y, z) = s + c * z exactly, with s = (+/-u) + (+/-v) and c = +0
+ * when v is x or y, and s = +/-u and c = +/-1 when v is z (u is never z). */
+static void grad_split(int h, float x, float y, float* s, float* c) {
+  h &= 15;
+  float u = h < 8 ? x : y;
+  u = (h & 1) ? -u : u;
+  if (h < 4 || h == 12 || h == 14) {
+    float v = h < 4 ? y : x;
+    *s = u + ((h & 2) ? -v : v);
+    *c = 0.0f;
+  } else {
+    *s = u;
+    *c = (h & 2) ? -1.0f : 1.0f;
+  }
+}
+
+/* One z-layer of the cell: the x/y lerps of the four corners' s and c parts.
+ * The layer's interpolated value at depth zk is alpha + beta * zk. */
+static void layer_coeffs(const uint8_t perm[256], int AAk, int ABk, int BAk, int BBk, float x, float y, float x1,
+                         float y1, float u, float v, float* alpha, float* beta) {
+#define P(i) ((int)perm[(i) & 255])
+  float s00, c00, s10, c10, s01, c01, s11, c11;
+  grad_split(P(AAk), x, y, &s00, &c00);
+  grad_split(P(BAk), x1, y, &s10, &c10);
+  grad_split(P(ABk), x, y1, &s01, &c01);
+  grad_split(P(BBk), x1, y1, &s11, &c11);
+#undef P
+  *alpha = lerpf(v, lerpf(u, s00, s10), lerpf(u, s01, s11));
+  *beta = lerpf(v, lerpf(u, c00, c10), lerpf(u, c01, c11));
+}
+
+/* Improved gradient noise in line-separable form.  Each corner gradient is
+ * s + c * z (grad_split), and lerp is linear, so a z-layer's x/y interpolant is
+ * alpha + beta * zk exactly; the noise is then
+ *     l0 = alpha0 + beta0 * zf,  l1 = alpha1 + beta1 * (zf - 1),  l0 + w (l1 - l0).
+ * In exact arithmetic this is the textbook value; in float it differs from it
+ * by rounding only.  alpha and beta depend on x, y and the lattice cell Z, not
+ * on the sample's own z, so a kernel walking a z-line sets them up once per
+ * lattice cell and spends nine operations per sample and octave.  The layer-1
+ * coefficients of cell Z are the layer-0 coefficients of cell Z + 1 (same
+ * hashes, same operations). */
+float bmfo_perlin(const uint8_t perm[256], float x, float y, float z) {
+  float fx = floorf(x), fy = floorf(y), fz = floorf(z);
+  int X = ((int)fx) & 255, Y = ((int)fy) & 255, Z = ((int)fz) & 255;
+  x = x - fx;
+  y = y - fy;
+  z = z - fz;
+  float u = fade(x), v = fade(y), w = fade(z);
+#define P(i) ((int)perm[(i) & 255])
+  int A = P(X) + Y, AA = P(A) + Z, AB = P(A + 1) + Z;
+  int B = P(X + 1) + Y, BA = P(B) + Z, BB = P(B + 1) + Z;
+#undef P
+  float x1 = x - 1.0f, y1 = y - 1.0f, z1 = z - 1.0f;
+  float a0, b0, a1, b1;
+  layer_coeffs(perm, AA, AB, BA, BB, x, y, x1, y1, u, v, &a0, &b0);
+  layer_coeffs(perm, AA + 1, AB + 1, BA + 1, BB + 1, x, y, x1, y1, u, v, &a1, &b1);
+  float l0 = a0 + b0 * z;
+  float l1 = a1 + b1 * z1;
+  return l0 + w * (l1 - l0);
 }
 
 float bmfo_fbm(const uint8_t perm[256], float x, float y, float z, int octaves, float freq, float lacunarity,

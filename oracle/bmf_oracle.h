@@ -29,6 +29,8 @@ extern "C" {
 float bmfo_sin(float x);
 void bmfo_perm_init(uint64_t seed, uint8_t perm[256]);
 float bmfo_perlin(const uint8_t perm[256], float x, float y, float z);
+/* the same noise in textbook evaluation order (precision yardstick) */
+float bmfo_perlin_textbook(const uint8_t perm[256], float x, float y, float z);
 float bmfo_fbm(const uint8_t perm[256], float x, float y, float z, int octaves, float freq, float lacunarity,
                float gain);
 

@@ -27,6 +27,10 @@ def lib():
         L.bmfo_sin.restype = c_float
         L.bmfo_sin.argtypes = [c_float]
         L.bmfo_fill_field.argtypes = [c_int, vp, c_int, vp, c_float, vp]
+        L.bmfo_perm_init.argtypes = [ctypes.c_uint64, vp]
+        for fn in (L.bmfo_perlin, L.bmfo_perlin_textbook):
+            fn.restype = c_float
+            fn.argtypes = [vp, c_float, c_float, c_float]
         L.bmfo_label_grid.restype = c_int
         L.bmfo_label_grid.argtypes = [c_int, vp, vp]
         L.bmfo_cell_masks.argtypes = [c_int, vp, vp]
@@ -59,6 +63,19 @@ class Counts(ctypes.Structure):
 
 def _p(a):
     return None if a is None else a.ctypes.data
+
+
+def perm(seed):
+    """The noise permutation of a seed (256 bytes)."""
+    out = np.empty(256, np.uint8)
+    lib().bmfo_perm_init(seed, _p(out))
+    return out
+
+
+def perlin(p, x, y, z, textbook=False):
+    """One noise value: the line-separable form, or the textbook order."""
+    fn = lib().bmfo_perlin_textbook if textbook else lib().bmfo_perlin
+    return fn(_p(p), x, y, z)
 
 
 def fill_field(kind, params, dim, origin=(0.0, 0.0, 0.0), scale=1.0):
