@@ -127,123 +127,147 @@ __device__ __forceinline__ void q_quad_words(const uint32_t* W, int dim, int zc,
 }
 
 // ---------------------------------------------------------------------------
-// K2: per-word counts
+// K2: per-word counts, one thread per occupancy word.
+//
+// Everything a word contributes is bit arithmetic on the eight line words
+// around it (lines (x..x+1, y..y+1), blocks zb and zb + 1): its owned
+// crossings X / Y / Z (vertex count by popc, Mode R), its interior quad edges
+// (Mode Q), and the set of its cells whose corner mask is mixed (neither 0 nor
+// 255).  Only mixed cells can emit triangles or hold vertex groups, so the
+// per-cell table lookup runs over the set bits of that mask alone; the
+// counts go into three bit-planes (a cell's first primitive / vertex is
+// base + popc(p0 & lt) + 2 popc(p1 & lt) + 4 popc(p2 & lt)).
 // ---------------------------------------------------------------------------
+
+// Per corner mask: Mode R triangle count (low nibble) and Mode Q vertex-group
+// count (high nibble), four masks per word.
+struct CaseCounts {
+  uint32_t w[64];
+};
+constexpr CaseCounts make_case_counts() {
+  constexpr uint64_t tri[256] = BMF_TRI_CASES_INIT;
+  constexpr uint64_t grp[256] = BMF_GROUP_CASES_INIT;
+  CaseCounts c{};
+  for (int m = 0; m < 256; ++m)
+    c.w[m >> 2] |= (uint32_t)((tri[m] >> 60) | (((grp[m] >> 48) & 0xF) << 4)) << (8 * (m & 3));
+  return c;
+}
+static __device__ const CaseCounts g_case_counts = make_case_counts();
+
+constexpr int kCountThreads = 128;
+
+// Cells z of block zb with z <= hi (bits [0, hi - 32 zb]).
+__device__ __forceinline__ uint32_t zbits_upto(int hi, int zb) {
+  const int n = hi - 32 * zb + 1;
+  return n >= 32 ? kFull : (n <= 0 ? 0u : ((1u << n) - 1u));
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(256) k_count(const ChunkDev* __restrict__ chunks, int n_chunks,
-                                               const int* __restrict__ unit_start, const uint32_t* __restrict__ words,
-                                               const uint32_t* __restrict__ flags, WordScratch ws) {
+__global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restrict__ chunks, int n_chunks,
+                                                         const int* __restrict__ unit_start,
+                                                         const uint32_t* __restrict__ words,
+                                                         const uint32_t* __restrict__ flags, WordScratch ws) {
+  __shared__ uint32_t s_cnt[64];
+  __shared__ int s_c;
   const int u = blockIdx.x;
-  const int c = find_chunk_e(unit_start, n_chunks, u);
+  if (threadIdx.x < 64) s_cnt[threadIdx.x] = g_case_counts.w[threadIdx.x];
+  if (threadIdx.x == 0) s_c = find_chunk_e(unit_start, n_chunks, u);
+  __syncthreads();
+  const int c = s_c;
   const ChunkDev ch = chunks[c];
   const int x = u - __ldg(unit_start + c);
   const int dim = ch.dim, zc = ch.zc, nw = dim * zc;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint32_t* W = words + ch.words;
   const bool cm = contains_mesh(__ldg(flags + c));
-  __shared__ SmemTabs T;
-  load_tabs(T);
-  __shared__ int s_busy[kWordBlock];
-  __shared__ int s_nbusy;
-  __shared__ uint32_t s_act[kWordBlock];  // Mode R work list: active cells of each busy word
-  __shared__ uint32_t s_apos[kWordBlock];
-  __shared__ uint32_t s_acnt, s_abase;
+  const int lane = threadIdx.x & 31;
   const bool listing = ws.clist != nullptr;
-  for (int base = 0; base < nw; base += kWordBlock) {
-    // level 1: one thread per word; quiet words get zero counts right away
-    if (threadIdx.x == 0) {
-      s_nbusy = 0;
-      s_acnt = 0;
-    }
-    __syncthreads();
-    if (base + (int)threadIdx.x < nw) {
-      const int wi = base + threadIdx.x;
+  const bool xin = x + 1 < dim;  // line x + 1 exists (cells and x-crossings of this plane)
+  for (int base = 0; base < nw; base += kCountThreads) {
+    const int wi = base + threadIdx.x;
+    uint32_t vc = 0u, ic = 0u, p0 = 0u, p1 = 0u, p2 = 0u, act = 0u;
+    if (wi < nw && cm) {
       const int y = wi / zc, zb = wi - y * zc;
-      if (cm && !word_is_quiet(W, dim, zc, x, y, zb)) {
-        s_busy[atomicAdd(&s_nbusy, 1)] = wi;
+      const bool yin = y + 1 < dim, nin = zb + 1 < zc;
+      const uint32_t* L00 = W + ((int64_t)x * dim + y) * zc + zb;
+      const uint32_t w00 = __ldg(L00), n00 = nin ? __ldg(L00 + 1) : 0u;
+      const uint32_t w01 = yin ? __ldg(L00 + zc) : 0u, n01 = (yin && nin) ? __ldg(L00 + zc + 1) : 0u;
+      const uint32_t* L10 = L00 + (int64_t)dim * zc;
+      const uint32_t w10 = xin ? __ldg(L10) : 0u, n10 = (xin && nin) ? __ldg(L10 + 1) : 0u;
+      const uint32_t w11 = (xin && yin) ? __ldg(L10 + zc) : 0u, n11 = (xin && yin && nin) ? __ldg(L10 + zc + 1) : 0u;
+      // corner words: bit l = corner (dx, dy, dz) of cell 32 zb + l
+      const uint32_t a0 = w00, a1 = (w00 >> 1) | (n00 << 31), b0 = w01, b1 = (w01 >> 1) | (n01 << 31);
+      const uint32_t c0 = w10, c1 = (w10 >> 1) | (n10 << 31), d0 = w11, d1 = (w11 >> 1) | (n11 << 31);
+      const uint32_t any = a0 | a1 | b0 | b1 | c0 | c1 | d0 | d1, all = a0 & a1 & b0 & b1 & c0 & c1 & d0 & d1;
+      const uint32_t zint = zbits_upto(dim - 2, zb);  // cells z <= dim - 2
+      const uint32_t interior = (xin && yin) ? zint : 0u;
+      const uint32_t mixed = interior & any & ~all;
+      uint32_t t = 0u;
+      for (uint32_t m = mixed; m; m &= m - 1u) {
+        const int l = __ffs(m) - 1;
+        const int mask = (int)(((w00 >> l) & 1u) | (((a1 >> l) & 1u) << 1) | (((w01 >> l) & 1u) << 2) |
+                               (((b1 >> l) & 1u) << 3) | (((w10 >> l) & 1u) << 4) | (((c1 >> l) & 1u) << 5) |
+                               (((w11 >> l) & 1u) << 6) | (((d1 >> l) & 1u) << 7));
+        const uint32_t k = (s_cnt[mask >> 2] >> (8 * (mask & 3))) >> (MODE == 0 ? 0 : 4);
+        const uint32_t n = k & 0xFu;
+        t += n;
+        p0 |= (n & 1u) << l;
+        p1 |= ((n >> 1) & 1u) << l;
+        p2 |= ((n >> 2) & 1u) << l;
+      }
+      if (MODE == 0) {
+        const uint32_t X = xin ? (w00 ^ w10) : 0u;
+        const uint32_t Y = yin ? (w00 ^ w01) : 0u;
+        const uint32_t Z = (w00 ^ a1) & zbits_upto(dim - 2, zb);
+        vc = __popc(X) + __popc(Y) + __popc(Z);
+        ic = 3u * t;
+        act = p0 | p1 | p2 | X | Y | Z;
       } else {
-        const int64_t o = ch.words + (int64_t)x * nw + wi;
-        ws.vcnt[o] = 0u;
-        ws.icnt[o] = 0u;
-        if (ws.gpl) { ws.gpl[3 * o] = 0u; ws.gpl[3 * o + 1] = 0u; ws.gpl[3 * o + 2] = 0u; }
+        // interior quad edges: the four cells around the edge exist
+        const bool yi = y >= 1 && y <= dim - 2, xi = x >= 1 && x <= dim - 2;
+        const uint32_t zlo = zb == 0 ? ~1u : kFull;  // with zint: z in [1, dim - 2]
+        const uint32_t Xi = (yi && xin) ? ((w00 ^ w10) & zint & zlo) : 0u;
+        const uint32_t Yi = (xi && yin) ? ((w00 ^ w01) & zint & zlo) : 0u;
+        const uint32_t Zi = (xi && yi) ? ((w00 ^ a1) & zbits_upto(dim - 2, zb)) : 0u;
+        vc = t;
+        ic = 4u * (__popc(Xi) + __popc(Yi) + __popc(Zi));
+        act = p0 | p1 | p2 | Xi | Yi | Zi;
       }
     }
-    __syncthreads();
-    // level 2: one warp per busy word, one lane per cell
-    const int nbusy = s_nbusy;
-    for (int li = warp; li < nbusy; li += nwarps) {
-    const int wi = s_busy[li];
-    const int y = wi / zc, zb = wi - y * zc;
-    const int64_t o = ch.words + (int64_t)x * nw + wi;
-    const int z = 32 * zb + lane;
-    LineWords lw;
-    lw.load(W, dim, zc, x, y, zb);
-    uint32_t vc, ic;
-    if (MODE == 0) {
-      const uint32_t X = (x + 1 < dim) ? (lw.w00 ^ lw.w10) : 0u;
-      const uint32_t Y = (y + 1 < dim) ? (lw.w00 ^ lw.w01) : 0u;
-      const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
-      vc = __popc(X) + __popc(Y) + __popc(Z);
-      const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
-      const int nt = interior ? (int)(T.tri[lw.mask(lane)] >> 60) : 0;
-      if (listing) {
-        const uint32_t act = __ballot_sync(kFull, nt != 0 || (((X | Y | Z) >> lane) & 1u));
-        if (lane == 0) {
-          s_act[li] = act;
-          s_apos[li] = act ? atomicAdd(&s_acnt, (uint32_t)__popc(act)) : 0u;
-        }
-      }
-      int t = 3 * nt;
-      // bit-planes of the per-cell triangle count (0..5): a cell's first
-      // primitive is ibase + 3 * (popc(p0 & lt) + 2 popc(p1 & lt) + 4 popc(p2 & lt))
-      const uint32_t p0 = __ballot_sync(kFull, nt & 1), p1 = __ballot_sync(kFull, nt & 2),
-                     p2 = __ballot_sync(kFull, nt & 4);
-      if (lane == 0 && ws.gpl) { ws.gpl[3 * o] = p0; ws.gpl[3 * o + 1] = p1; ws.gpl[3 * o + 2] = p2; }
-      t += __shfl_xor_sync(kFull, t, 16);
-      t += __shfl_xor_sync(kFull, t, 8);
-      t += __shfl_xor_sync(kFull, t, 4);
-      t += __shfl_xor_sync(kFull, t, 2);
-      t += __shfl_xor_sync(kFull, t, 1);
-      ic = (uint32_t)t;
-    } else {
-      const bool interior = x <= dim - 2 && y <= dim - 2 && z <= dim - 2;
-      const int ng = interior ? (int)((T.grp[lw.mask(lane)] >> 48) & 0xF) : 0;
-      const uint32_t g0 = __ballot_sync(kFull, ng & 1), g1 = __ballot_sync(kFull, ng & 2),
-                     g2 = __ballot_sync(kFull, ng & 4);
-      vc = __popc(g0) + 2 * __popc(g1) + 4 * __popc(g2);
-      uint32_t Xi, Yi, Zi;
-      q_quad_words(W, dim, zc, x, y, zb, Xi, Yi, Zi);
-      ic = 4u * (__popc(Xi) + __popc(Yi) + __popc(Zi));
-      if (lane == 0) { ws.gpl[3 * o] = g0; ws.gpl[3 * o + 1] = g1; ws.gpl[3 * o + 2] = g2; }
-      if (listing) {
-        const uint32_t act = __ballot_sync(kFull, ng != 0 || (((Xi | Yi | Zi) >> lane) & 1u));
-        if (lane == 0) {
-          s_act[li] = act;
-          s_apos[li] = act ? atomicAdd(&s_acnt, (uint32_t)__popc(act)) : 0u;
-        }
-      }
-    }
-    if (lane == 0) {
+    if (wi < nw) {
+      const int64_t o = ch.words + (int64_t)x * nw + wi;
       ws.vcnt[o] = vc;
       ws.icnt[o] = ic;
-    }
-    }
-    __syncthreads();
-    if (listing) {
-      // one global reservation per block of words, then each busy word's
-      // active cells in lane order
-      if (threadIdx.x == 0) s_abase = s_acnt ? atomicAdd(ws.ccount, s_acnt) : 0u;
-      __syncthreads();
-      for (int li = warp; li < nbusy; li += nwarps) {
-        const uint32_t act = s_act[li];
-        if (!((act >> lane) & 1u)) continue;
-        const int wi = s_busy[li];
-        const int y = wi / zc, zb = wi - y * zc;
-        const int64_t slot = (int64_t)s_abase + s_apos[li] + __popc(act & lane_lt(lane));
-        if (slot < ws.clist_cap)
-          ws.clist[slot] = make_uint2((uint32_t)c, (uint32_t)(((int64_t)x * dim + y) * dim + 32 * zb + lane));
+      if (ws.gpl) {
+        ws.gpl[3 * o] = p0;
+        ws.gpl[3 * o + 1] = p1;
+        ws.gpl[3 * o + 2] = p2;
       }
-      __syncthreads();
+    }
+    if (listing) {
+      // one global reservation per warp; Mode R lists busy words, Mode Q
+      // each word's active cells in bit order
+      const int na = MODE == 0 ? (act != 0u ? 1 : 0) : __popc(act);
+      int incl = na;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += v;
+      }
+      const int tot = __shfl_sync(kFull, incl, 31);
+      uint32_t wbase = 0u;
+      if (lane == 31 && tot) wbase = atomicAdd(ws.ccount, (uint32_t)tot);
+      wbase = __shfl_sync(kFull, wbase, 31);
+      if (act) {
+        int64_t slot = (int64_t)wbase + incl - na;
+        if (MODE == 0) {
+          if (slot < ws.clist_cap) ws.clist[slot] = make_uint2((uint32_t)c, (uint32_t)(x * nw + wi));
+        } else {
+          const int y = wi / zc, zb = wi - y * zc;
+          const uint32_t lin0 = (uint32_t)((((int64_t)x * dim + y) * dim) + 32 * zb);
+          for (uint32_t m = act; m; m &= m - 1u, ++slot)
+            if (slot < ws.clist_cap) ws.clist[slot] = make_uint2((uint32_t)c, lin0 + (uint32_t)(__ffs(m) - 1));
+        }
+      }
     }
   }
 }
@@ -672,6 +696,62 @@ void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_ch
 // pass, deterministic.
 // ---------------------------------------------------------------------------
 
+// Three consecutive inside bits z0..z0+2 of line (x, y) (zero outside the
+// chunk); W is the chunk's words, 32-bit offsets.
+__device__ __forceinline__ uint32_t line_bits3(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int z0) {
+  if (x < 0 || y < 0 || x >= dim || y >= dim) return 0u;
+  const int b0 = z0 >> 5;  // arithmetic shift: block -1 for z0 = -1
+  const uint32_t* L = W + (x * dim + y) * zc;
+  const uint32_t lo = (b0 >= 0 && b0 < zc) ? __ldg(L + b0) : 0u;
+  const uint32_t hi = (b0 + 1 < zc) ? __ldg(L + b0 + 1) : 0u;
+  const uint64_t q = ((uint64_t)hi << 32) | lo;
+  return (uint32_t)(q >> (z0 & 31)) & 7u;
+}
+
+// Mode R adjacency of the vertex on the axis-A edge of sample (x, y, z): the
+// primitives of the (up to) four interior cells around the edge that use it,
+// cells in ascending linear order, triangles in list order.  The inside bits
+// of lines (x-1..x+1, y-1..y+1) at samples z-1..z+1 hold every corner of
+// those cells.
+template <int A>
+__device__ __forceinline__ int adj_edge_r(const SmemTabs& T, const uint32_t* __restrict__ W,
+                                          const uint32_t* __restrict__ pl, const uint32_t* __restrict__ ibase,
+                                          int64_t iout, int dim, int zc, int x, int y, int z, uint32_t* out, int room) {
+  uint32_t nb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      nb[i][j] = (A == 0 ? i >= 1 : (A == 1 ? j >= 1 : true)) ? line_bits3(W, dim, zc, x - 1 + i, y - 1 + j, z - 1)
+                                                               : 0u;
+  int n = 0;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int d1 = (q >> 1) ^ 1, d2 = (q & 1) ^ 1;
+    // cell offsets from (x, y, z) and the edge's number in that cell
+    const int ox = A == 0 ? 0 : -d1, oy = A == 0 ? -d1 : (A == 1 ? 0 : -d2), oz = A == 2 ? 0 : -d2;
+    const int e = 4 * A + 2 * d1 + d2;
+    const int cx = x + ox, cy = y + oy, cz = z + oz;
+    if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
+    int m = 0;
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc)
+      m |= (int)((nb[1 + ox + ((cc >> 2) & 1)][1 + oy + ((cc >> 1) & 1)] >> (1 + oz + (cc & 1))) & 1u) << cc;
+    if (!tab_uses(T, m, e)) continue;
+    const uint64_t tw = T.tri[m];
+    const int nt = (int)(tw >> 60);
+    const int wi = (cx * dim + cy) * zc + (cz >> 5);
+    const uint32_t lt = lane_lt(cz & 31);
+    const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
+                         4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
+    const int64_t first = (iout + (int64_t)__ldg(ibase + wi)) / 3 + pre;
+    for (int t = 0; t < nt; ++t)
+      if ((tri_edge(tw, 3 * t) == e || tri_edge(tw, 3 * t + 1) == e || tri_edge(tw, 3 * t + 2) == e) && n < room)
+        out[n++] = (uint32_t)(first + t);
+  }
+  return n;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ chunks, int n_chunks,
                                                    const uint32_t* __restrict__ words, WordScratch ws,
@@ -679,78 +759,74 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
                                                    uint32_t* __restrict__ adj) {
   __shared__ SmemTabs T;
+  __shared__ int s_crange[2];
   load_tabs(T);
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
-  const int c = find_chunk_by_vertex(chunks, n_chunks, v);
-  const ChunkDev ch = chunks[c];
-  const int dim = ch.dim, zc = ch.zc;
-  const uint32_t* W = words + ch.words;
-  const uint32_t* vbase = ws.vcnt + ch.words;
-  const uint32_t* ibase = ws.icnt + ch.words;
-  const uint32_t* pl = ws.gpl + 3 * ch.words;
-  const uint32_t key = vkey[v];
-  const int lin = (int)(key >> 2), k = (int)(key & 3u);
-  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
-  uint32_t* out = adj + off[v];
-  // the vertex's CSR range (the exclusive scan of init_valence): never write past it
-  const int room = (int)(off[v + 1] - off[v]);
-  int n = 0;
-  if (MODE == 0) {
-    const int a = k;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {  // cells around the edge, ascending linear order
-      const int d1 = (q >> 1) ^ 1, d2 = (q & 1) ^ 1;
-      int cx = x, cy = y, cz = z, e;
-      if (a == 0) { cy -= d1; cz -= d2; e = 2 * d1 + d2; }
-      else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
-      else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
-      if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
-      const int m = cell_mask_at(W, dim, zc, cx, cy, cz);
-      if (!tab_uses(T, m, e)) continue;
-      const uint64_t tw = T.tri[m];
-      const int nt = (int)(tw >> 60);
-      const int64_t wi = ((int64_t)cx * dim + cy) * zc + (cz >> 5);
-      const uint32_t lt = lane_lt(cz & 31);
-      const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
-                           4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
-      const int64_t first = (ch.iout + (int64_t)__ldg(ibase + wi)) / 3 + pre;
-      for (int t = 0; t < nt; ++t)
-        if ((tri_edge(tw, 3 * t) == e || tri_edge(tw, 3 * t + 1) == e || tri_edge(tw, 3 * t + 2) == e) && n < room)
-          out[n++] = (uint32_t)(first + t);
+  const int64_t nv = d_counts ? min(vcap, d_counts[0]) : vcap;
+  for (int64_t v0 = (int64_t)blockIdx.x * blockDim.x; v0 < nv; v0 += (int64_t)gridDim.x * blockDim.x) {
+    // the chunks this tile of vertices spans
+    __syncthreads();
+    if (threadIdx.x == 0) s_crange[0] = find_chunk_by_vertex(chunks, n_chunks, v0);
+    if (threadIdx.x == 32) s_crange[1] = find_chunk_by_vertex(chunks, n_chunks, min(v0 + (int64_t)blockDim.x, nv) - 1);
+    __syncthreads();
+    const int64_t v = v0 + threadIdx.x;
+    if (v >= nv) continue;
+    int c = s_crange[0];
+    for (int hi = s_crange[1]; c < hi;) {  // last chunk in range whose vout <= v
+      const int mid = (c + hi + 1) >> 1;
+      if (chunks[mid].vout <= v) c = mid; else hi = mid - 1;
     }
-  } else {
-    const int g = k;
-    const int m = cell_mask_at(W, dim, zc, x, y, z);
-    uint32_t ids[12];
-    const uint64_t gw = T.grp[m];
-    for (int e = 0; e < 12; ++e) {
-      if ((int)((gw >> (4 * e)) & 0xF) != g) continue;
-      const int c0 = edge_c0(e), a = e >> 2;
-      const int sx = x + ((c0 >> 2) & 1), sy = y + ((c0 >> 1) & 1), sz = z + (c0 & 1);
-      if (!q_edge_interior(dim, sx, sy, sz, a)) continue;
-      uint32_t Xi, Yi, Zi;
-      q_quad_words(W, dim, zc, sx, sy, sz >> 5, Xi, Yi, Zi);
-      const int l = sz & 31;
-      const uint32_t lt = lane_lt(l);
-      uint32_t pre = __popc(Xi & lt) + __popc(Yi & lt) + __popc(Zi & lt);
-      if (a >= 1) pre += (Xi >> l) & 1u;
-      if (a >= 2) pre += (Yi >> l) & 1u;
-      const int64_t wi = ((int64_t)sx * dim + sy) * zc + (sz >> 5);
-      uint32_t id = (uint32_t)((ch.iout + (int64_t)__ldg(ibase + wi)) / 4 + pre);
-      int j = n++;  // insertion into the sorted prefix
-      while (j > 0 && ids[j - 1] > id) { ids[j] = ids[j - 1]; --j; }
-      ids[j] = id;
+    const ChunkDev& ch = chunks[c];
+    const int dim = ch.dim, zc = ch.zc;
+    const int64_t iout = ch.iout;
+    const uint32_t* W = words + ch.words;
+    const uint32_t* ibase = ws.icnt + ch.words;
+    const uint32_t* pl = ws.gpl + 3 * ch.words;
+    const uint32_t key = vkey[v];
+    const int lin = (int)(key >> 2), k = (int)(key & 3u);
+    const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+    uint32_t* out = adj + off[v];
+    // the vertex's CSR range (the exclusive scan of init_valence): never write past it
+    const int room = (int)(off[v + 1] - off[v]);
+    int n = 0;
+    if (MODE == 0) {
+      if (k == 0) n = adj_edge_r<0>(T, W, pl, ibase, iout, dim, zc, x, y, z, out, room);
+      else if (k == 1) n = adj_edge_r<1>(T, W, pl, ibase, iout, dim, zc, x, y, z, out, room);
+      else n = adj_edge_r<2>(T, W, pl, ibase, iout, dim, zc, x, y, z, out, room);
+    } else {
+      const int g = k;
+      const int m = cell_mask_at(W, dim, zc, x, y, z);
+      uint32_t ids[12];
+      const uint64_t gw = T.grp[m];
+      for (int e = 0; e < 12; ++e) {
+        if ((int)((gw >> (4 * e)) & 0xF) != g) continue;
+        const int c0 = edge_c0(e), a = e >> 2;
+        const int sx = x + ((c0 >> 2) & 1), sy = y + ((c0 >> 1) & 1), sz = z + (c0 & 1);
+        if (!q_edge_interior(dim, sx, sy, sz, a)) continue;
+        uint32_t Xi, Yi, Zi;
+        q_quad_words(W, dim, zc, sx, sy, sz >> 5, Xi, Yi, Zi);
+        const int l = sz & 31;
+        const uint32_t lt = lane_lt(l);
+        uint32_t pre = __popc(Xi & lt) + __popc(Yi & lt) + __popc(Zi & lt);
+        if (a >= 1) pre += (Xi >> l) & 1u;
+        if (a >= 2) pre += (Yi >> l) & 1u;
+        const int wi = (sx * dim + sy) * zc + (sz >> 5);
+        uint32_t id = (uint32_t)((iout + (int64_t)__ldg(ibase + wi)) / 4 + pre);
+        int j = n++;  // insertion into the sorted prefix
+        while (j > 0 && ids[j - 1] > id) { ids[j] = ids[j - 1]; --j; }
+        ids[j] = id;
+      }
+      for (int i = 0; i < n && i < room; ++i) out[i] = ids[i];
     }
-    for (int i = 0; i < n && i < room; ++i) out[i] = ids[i];
   }
-  (void)vbase;
 }
 
 void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
                       const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,
                       uint32_t* adj, cudaStream_t st) {
-  const int blocks = (int)((vcap + 255) / 256);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = (int)min((vcap + 255) / 256, (int64_t)sms * 8);
   if (blocks == 0) return;
   if (mode == 0) k_adj_build<0><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
   else k_adj_build<1><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
@@ -759,8 +835,8 @@ void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const ui
 void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
                   const uint32_t* words, const uint32_t* flags, WordScratch ws, cudaStream_t st) {
   if (ws.clist) cudaMemsetAsync(ws.ccount, 0, sizeof(uint32_t), st);
-  if (mode == 0) k_count<0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
-  else k_count<1><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
+  if (mode == 0) k_count<0><<<n_units, kCountThreads, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
+  else k_count<1><<<n_units, kCountThreads, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
 }
 
 void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, uint32_t* d_tot, cudaStream_t st) {
@@ -772,91 +848,212 @@ void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_to
   k_chunk_offsets<<<1, 1024, 0, st>>>(d_chunks, n_chunks, d_tot, flags, vcap, icap, d_info, d_totals);
 }
 
-// Mode R emission over the work list, one thread per active cell (the
-// warp-per-word form runs most lanes idle: a busy word holds a few surface
-// cells).  Per cell it writes exactly what k_emit<0,0> writes for the cell's
-// lane: its owned vertices (ids from the scanned word base and the crossing
-// words, calculate_isovertex positions, boundary, key, init_valence) and its
-// triangles (slot from the word's index base and the triangle-count planes).
-__global__ void __launch_bounds__(256, 3) k_emit_cells_r(const ChunkDev* __restrict__ chunks,
+// k-th set bit (from 0) of m; m must have more than k set bits.
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int k) {
+  int pos = 0, c = __popc(m & 0xFFFFu);
+  if (k >= c) { k -= c; m >>= 16; pos += 16; }
+  c = __popc(m & 0xFFu);
+  if (k >= c) { k -= c; m >>= 8; pos += 8; }
+  c = __popc(m & 0xFu);
+  if (k >= c) { k -= c; m >>= 4; pos += 4; }
+  c = __popc(m & 0x3u);
+  if (k >= c) { k -= c; m >>= 2; pos += 2; }
+  if (k >= (int)(m & 1u)) pos += 1;
+  return pos;
+}
+
+// Mode R emission over the busy-word list.  A CTA takes kTileWords list
+// entries at a time and stages, per word, its neighbourhood (NbCache: the
+// occupancy words of lines (x-1..x+2, y-1..y+2) in blocks zb-1..zb+1 and the
+// scanned vertex bases of lines (x..x+1, y..y+1) in blocks zb..zb+1), its
+// index base and its triangle-count planes in shared memory.  Then one thread
+// per active cell of the tile (a flattened scan of the words' active-cell
+// counts) writes exactly what the reference writes for that cell: its owned
+// vertices (ids from the word base and the crossing words,
+// calculate_isovertex positions, boundary, key, init_valence) and its
+// triangles (slot from the word's index base and the count planes).  Every
+// mask, valence and neighbour vertex id is read from shared memory; only the
+// two endpoint densities of a vertex come from global memory.
+constexpr int kTileWords = 64;
+constexpr int kTileSlots = 48 + 8 + 4;  // neighbour words, vertex bases, index base, 3 planes
+
+struct RTile {
+  NbCache nb[kTileWords];
+  uint32_t ib[kTileWords], p0[kTileWords], p1[kTileWords], p2[kTileWords];
+  uint32_t X[kTileWords], Y[kTileWords], Z[kTileWords], act[kTileWords];
+  int x[kTileWords], y[kTileWords], zb[kTileWords], dim[kTileWords], zc[kTileWords];
+  int64_t w0[kTileWords], dens[kTileWords], vout[kTileWords], iout[kTileWords];
+  int off[kTileWords + 1];
+};
+
+__global__ void __launch_bounds__(256) k_emit_words_r(const ChunkDev* __restrict__ chunks,
                                                       const uint32_t* __restrict__ words,
                                                       const float* __restrict__ dens, WordScratch ws, MeshOut out) {
-  __shared__ SmemTabs T;
-  load_tabs(T);
+  __shared__ uint64_t s_tri[256], s_uses[256];
+  __shared__ RTile R;
+  __shared__ int s_wsum[kTileWords / 32];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    s_tri[i] = __ldg(g_tri_cases + i);
+    s_uses[i] = __ldg(g_edge_uses + i);
+  }
   const int64_t n = min((int64_t)*ws.ccount, ws.clist_cap);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const uint2 ent = ws.clist[i];
-    const ChunkDev ch = chunks[ent.x];
-    const int dim = ch.dim, zc = ch.zc;
-    const int lin = (int)ent.y;
-    const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
-    const int zb = z >> 5, lane = z & 31;
-    const uint32_t lt = lane_lt(lane);
-    const uint32_t* W = words + ch.words;
-    const uint32_t* vbase = ws.vcnt + ch.words;
-    const float* D = dens + ch.dens;
-    const int64_t wo = ((int64_t)x * dim + y) * zc + zb;
-    const uint32_t w00 = word_at(W, dim, zc, x, y, zb);
-    const uint32_t X = (x + 1 < dim) ? (w00 ^ word_at(W, dim, zc, x + 1, y, zb)) : 0u;
-    const uint32_t Y = (y + 1 < dim) ? (w00 ^ word_at(W, dim, zc, x, y + 1, zb)) : 0u;
-    const uint32_t Z = zcross_word(W, dim, zc, x, y, zb);
-    const uint32_t own = ((X >> lane) & 1u) | (((Y >> lane) & 1u) << 1) | (((Z >> lane) & 1u) << 2);
-    if (own) {
-      uint32_t vid = __ldg(vbase + wo) + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
-      for (int a = 0; a < 3; ++a) {
-        if (!((own >> a) & 1u)) continue;
-        const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
-        const int64_t gv = ch.vout + vid;
-        ++vid;
-        if (gv >= out.vcap) continue;
-        const float s0 = dens_at(D, dim, x, y, z), s1 = dens_at(D, dim, x1, y1, z1);
-        const float mu = (0.0f - s0) / (s1 - s0);
-        const float q0[3] = {(float)x, (float)y, (float)z};
-        const float dl[3] = {(float)(x1 - x), (float)(y1 - y), (float)(z1 - z)};
-        float* P = out.pos + 3 * gv;
+  const int tid = threadIdx.x, lane = tid & 31;
+  for (int64_t t0 = (int64_t)blockIdx.x * kTileWords; t0 < n; t0 += (int64_t)gridDim.x * kTileWords) {
+    const int nt = (int)min((int64_t)kTileWords, n - t0);
+    // 1. the tile's words
+    if (tid < nt) {
+      const uint2 e = ws.clist[t0 + tid];
+      const ChunkDev& ch = chunks[e.x];
+      const int dim = ch.dim, zc = ch.zc, wi = (int)e.y;
+      const int xy = wi / zc;
+      R.zb[tid] = wi - xy * zc;
+      R.y[tid] = xy % dim;
+      R.x[tid] = xy / dim;
+      R.dim[tid] = dim;
+      R.zc[tid] = zc;
+      R.w0[tid] = ch.words + wi;
+      R.dens[tid] = ch.dens;
+      R.vout[tid] = ch.vout;
+      R.iout[tid] = ch.iout;
+    }
+    __syncthreads();
+    // 2. stage the neighbourhoods (zeros outside the chunk)
+    for (int k = tid; k < nt * kTileSlots; k += blockDim.x) {
+      const int t = k / kTileSlots, sl = k - t * kTileSlots;
+      const int dim = R.dim[t], zc = R.zc[t], x = R.x[t], y = R.y[t], zb = R.zb[t];
+      const int64_t w0 = R.w0[t];
+      const int64_t cw = w0 - (((int64_t)x * dim + y) * zc + zb);  // chunk's first word
+      if (sl < 48) {
+        const int i = sl / 12, j = (sl / 3) & 3, b = sl % 3;
+        R.nb[t].w[sl] = word_at(words + cw, dim, zc, x - 1 + i, y - 1 + j, zb - 1 + b);
+      } else if (sl < 56) {
+        const int l = sl - 48;
+        const int xx = x + (l >> 2), yy = y + ((l >> 1) & 1), bb = zb + (l & 1);
+        R.nb[t].vb[l] = (xx < dim && yy < dim && bb < zc) ? __ldg(ws.vcnt + cw + ((int64_t)xx * dim + yy) * zc + bb)
+                                                         : 0u;
+      } else if (sl == 56) {
+        R.ib[t] = __ldg(ws.icnt + w0);
+      } else {
+        const uint32_t v = __ldg(ws.gpl + 3 * w0 + (sl - 57));
+        if (sl == 57) R.p0[t] = v;
+        else if (sl == 58) R.p1[t] = v;
+        else R.p2[t] = v;
+      }
+    }
+    __syncthreads();
+    // 3. active cells per word (owned crossings or triangles), flattened
+    if (tid < kTileWords) {
+      int cnt = 0;
+      if (tid < nt) {
+        const NbCache& nb = R.nb[tid];
+        const int dim = R.dim[tid], x = R.x[tid], y = R.y[tid], zb = R.zb[tid];
+        const uint32_t wc = nb.w[(1 * 4 + 1) * 3 + 1];
+        const uint32_t X = (x + 1 < dim) ? wc ^ nb.w[(2 * 4 + 1) * 3 + 1] : 0u;
+        const uint32_t Y = (y + 1 < dim) ? wc ^ nb.w[(1 * 4 + 2) * 3 + 1] : 0u;
+        uint32_t Z = wc ^ ((wc >> 1) | (nb.w[(1 * 4 + 1) * 3 + 2] << 31));
+        const int valid = dim - 1 - 32 * zb;
+        if (valid < 32) Z &= valid <= 0 ? 0u : ((1u << valid) - 1u);
+        const uint32_t act = R.p0[tid] | R.p1[tid] | R.p2[tid] | X | Y | Z;
+        R.X[tid] = X;
+        R.Y[tid] = Y;
+        R.Z[tid] = Z;
+        R.act[tid] = act;
+        cnt = __popc(act);
+      }
+      int incl = cnt;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const float dv = dl[k] * mu;
-          P[k] = dv + q0[k];
-        }
-        if (out.boundary)
-          out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
-                              x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
-        if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
-        if (out.vkey) out.vkey[gv] = ((uint32_t)lin << 2) | (uint32_t)a;
-        if (out.valence) {
-          int val = 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+      }
+      if (lane == 31) s_wsum[tid >> 5] = incl;
+      R.off[tid + 1] = incl;  // warp-local for now
+    }
+    if (tid == 0) R.off[0] = 0;
+    __syncthreads();
+    if (tid >= 32 && tid < kTileWords) R.off[tid + 1] += s_wsum[0];
+    __syncthreads();
+    const int total = R.off[nt];
+    // 4. one thread per active cell
+    for (int j = tid; j < total; j += blockDim.x) {
+      int lo = 0, hi = nt - 1;  // last t with off[t] <= j
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (R.off[mid] <= j) lo = mid; else hi = mid - 1;
+      }
+      const int t = lo;
+      const int l = nth_set_bit(R.act[t], j - R.off[t]);
+      const NbCache& nb = R.nb[t];
+      const int dim = R.dim[t], x = R.x[t], y = R.y[t], zb = R.zb[t];
+      const int z = 32 * zb + l;
+      const uint32_t lt = lane_lt(l);
+      const uint32_t X = R.X[t], Y = R.Y[t], Z = R.Z[t];
+      const uint32_t own = ((X >> l) & 1u) | (((Y >> l) & 1u) << 1) | (((Z >> l) & 1u) << 2);
+      const int64_t vout = R.vout[t];
+      if (own) {
+        const float* D = dens + R.dens[t];
+        uint32_t vid = nb.vb[0] + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
+        const uint32_t lin = (uint32_t)(((int64_t)x * dim + y) * dim + z);
+        for (int a = 0; a < 3; ++a) {
+          if (!((own >> a) & 1u)) continue;
+          const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+          const int64_t gv = vout + vid;
+          ++vid;
+          if (gv >= out.vcap) continue;
+          const float s0 = dens_at(D, dim, x, y, z), s1 = dens_at(D, dim, x1, y1, z1);
+          const float mu = (0.0f - s0) / (s1 - s0);
+          const float q0[3] = {(float)x, (float)y, (float)z};
+          const float dl[3] = {(float)(x1 - x), (float)(y1 - y), (float)(z1 - z)};
+          float* P = out.pos + 3 * gv;
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const int d1 = k >> 1, d2 = k & 1;
-            int cx = x, cy = y, cz = z, e;
-            if (a == 0) { cy -= d1; cz -= d2; e = 2 * d1 + d2; }
-            else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
-            else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
-            if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
-            val += tab_uses(T, cell_mask_at(W, dim, zc, cx, cy, cz), e);
+          for (int k = 0; k < 3; ++k) {
+            const float dv = dl[k] * mu;
+            P[k] = dv + q0[k];
           }
-          out.valence[gv] = (uint8_t)val;
+          if (out.boundary)
+            out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
+                                x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
+          if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
+          if (out.vkey) out.vkey[gv] = (lin << 2) | (uint32_t)a;
+          if (out.valence) {
+            // init_valence: uses of this edge by the (up to) four interior
+            // cells around it (polygonize skips far-face cells, DMCChunk.cpp:528)
+            int val = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int d1 = k >> 1, d2 = k & 1;
+              int cx = x, cy = y, cz = z, e;
+              if (a == 0) { cy -= d1; cz -= d2; e = 2 * d1 + d2; }
+              else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
+              else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
+              if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
+              const int m = nb_mask(nb, cx - x + 1, cy - y + 1, cz - 32 * (zb - 1));
+              val += (int)((s_uses[m] >> (4 * e)) & 0xF);
+            }
+            out.valence[gv] = (uint8_t)val;
+          }
+        }
+      }
+      // triangles: polygonize_cell order
+      if (x >= dim - 1 || y >= dim - 1 || z >= dim - 1) continue;
+      const uint64_t tw = s_tri[nb_mask(nb, 1, 1, l + 32)];
+      const int t3 = 3 * (int)(tw >> 60);
+      if (t3 == 0) continue;
+      const int before = __popc(R.p0[t] & lt) + 2 * __popc(R.p1[t] & lt) + 4 * __popc(R.p2[t] & lt);
+      int64_t gi = R.iout[t] + (int64_t)R.ib[t] + 3 * before;
+      for (int k = 0; k < t3; ++k, ++gi) {
+        const int e = tri_edge(tw, k);
+        // EDGE_V owner of edge e: axis e >> 2, offsets from its two low bits
+        const int ea = e >> 2, d1 = (e >> 1) & 1, d2 = e & 1;
+        const int ox = ea == 0 ? 0 : d1, oy = ea == 0 ? d1 : (ea == 1 ? 0 : d2), oz = ea == 2 ? 0 : d2;
+        const uint32_t vid = nb_vertex_id(nb, dim, x, y, zb, ox, oy, z + oz, ea);
+        if (gi < out.icap) {
+          out.idx[gi] = vid;
+          if (out.idx_global) out.idx_global[gi] = (uint32_t)(vout + vid);
         }
       }
     }
-    const bool interior = x < dim - 1 && y < dim - 1 && z < dim - 1;
-    const int mask = interior ? cell_mask_at(W, dim, zc, x, y, z) : 0;
-    const uint64_t tw = T.tri[mask];
-    const int t3 = 3 * (int)(tw >> 60);
-    if (t3 == 0) continue;
-    const uint32_t* pl = ws.gpl + 3 * (ch.words + wo);
-    const int before = __popc(__ldg(pl) & lt) + 2 * __popc(__ldg(pl + 1) & lt) + 4 * __popc(__ldg(pl + 2) & lt);
-    int64_t gi = ch.iout + (int64_t)__ldg(ws.icnt + ch.words + wo) + 3 * before;
-    for (int k = 0; k < t3; ++k, ++gi) {
-      const int e = tri_edge(tw, k);
-      const uint32_t vid = r_vertex_id(W, vbase, dim, zc, x + c_edge_owner[e][0], y + c_edge_owner[e][1],
-                                       z + c_edge_owner[e][2], c_edge_owner[e][3]);
-      if (gi < out.icap) {
-        out.idx[gi] = vid;
-        if (out.idx_global) out.idx_global[gi] = (uint32_t)(ch.vout + vid);
-      }
-    }
+    __syncthreads();  // the next tile overwrites the stage
   }
 }
 
@@ -990,7 +1187,7 @@ int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks,
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_emit_cells_r<<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+    k_emit_words_r<<<sms * 4, 256, 0, st>>>(d_chunks, words, dens, ws, out);
   } else if (mode == 0) {
     k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else if (ws.clist) {

@@ -31,11 +31,12 @@ struct WordScratch {
   uint32_t* vcnt;   // vertices hosted by the word's 32 cells; scanned in place to the chunk-local base
   uint32_t* icnt;   // indices emitted by the word's cells; scanned in place
   uint32_t* gpl;    // 3 bit-planes of the per-cell triangle (Mode R) / vertex-group (Mode Q) count
-  // Work list (nullable): every cell that owns a vertex or emits a primitive
-  // (Mode R: owned crossing or triangles; Mode Q: vertex groups or owned
-  // interior crossings), as {chunk, (x*dim + y)*dim + z}, in no particular
-  // order; *ccount (zeroed before the count kernel) entries, at most
-  // clist_cap kept.  Its size bound is vcap + icap / prim_size + 1.
+  // Work list (nullable), in no particular order; *ccount (zeroed before the
+  // count kernel) entries, at most clist_cap kept.  Mode R: every busy word
+  // (one whose cells own a crossing or emit triangles) as {chunk, word index
+  // in the chunk}; Mode Q: every cell that holds vertex groups or owns an
+  // interior crossing, as {chunk, (x*dim + y)*dim + z}.  Either way its size
+  // bound is vcap + icap / prim_size + 1.
   uint2* clist;
   uint32_t* ccount;
   int64_t clist_cap;
@@ -50,13 +51,13 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
 // Terrain FBM fill over line items {chunk, first line} (kFillLines lines
 // each; d_items null = chunk 0's items in order).  d_queue non-null: grid
 // persistent CTAs take items from the queue (reset here); else one CTA per item.
-// run = z-samples per step (4, 8 or 16).
+// run = z-samples per step (4, 8, 16 or 32).
 void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,
                          int grid, const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
                          cudaStream_t st);
 int fill_terrain_items(int dim);          // items of one chunk
 int fill_terrain_lines();                 // lines per item
-int fill_terrain_resident_ctas(int run);  // persistent grid: SMs x resident CTAs per SM
+int fill_terrain_resident_ctas(int run, int octaves);  // persistent grid: SMs x resident CTAs per SM
 void launch_cell_masks(int dim, const uint32_t* W, uint8_t* masks, cudaStream_t st);
 // contains_mesh flags of chunks whose words were produced elsewhere.
 void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, uint32_t* flags,
