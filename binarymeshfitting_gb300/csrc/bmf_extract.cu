@@ -708,48 +708,15 @@ __device__ __forceinline__ uint32_t line_bits3(const uint32_t* __restrict__ W, i
   return (uint32_t)(q >> (z0 & 31)) & 7u;
 }
 
-// Mode R adjacency of the vertex on the axis-A edge of sample (x, y, z): the
-// primitives of the (up to) four interior cells around the edge that use it,
-// cells in ascending linear order, triangles in list order.  The inside bits
-// of lines (x-1..x+1, y-1..y+1) at samples z-1..z+1 hold every corner of
-// those cells.
-template <int A>
-__device__ __forceinline__ int adj_edge_r(const SmemTabs& T, const uint32_t* __restrict__ W,
-                                          const uint32_t* __restrict__ pl, const uint32_t* __restrict__ ibase,
-                                          int64_t iout, int dim, int zc, int x, int y, int z, uint32_t* out, int room) {
-  uint32_t nb[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      nb[i][j] = (A == 0 ? i >= 1 : (A == 1 ? j >= 1 : true)) ? line_bits3(W, dim, zc, x - 1 + i, y - 1 + j, z - 1)
-                                                               : 0u;
-  int n = 0;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int d1 = (q >> 1) ^ 1, d2 = (q & 1) ^ 1;
-    // cell offsets from (x, y, z) and the edge's number in that cell
-    const int ox = A == 0 ? 0 : -d1, oy = A == 0 ? -d1 : (A == 1 ? 0 : -d2), oz = A == 2 ? 0 : -d2;
-    const int e = 4 * A + 2 * d1 + d2;
-    const int cx = x + ox, cy = y + oy, cz = z + oz;
-    if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
-    int m = 0;
-#pragma unroll
-    for (int cc = 0; cc < 8; ++cc)
-      m |= (int)((nb[1 + ox + ((cc >> 2) & 1)][1 + oy + ((cc >> 1) & 1)] >> (1 + oz + (cc & 1))) & 1u) << cc;
-    if (!tab_uses(T, m, e)) continue;
-    const uint64_t tw = T.tri[m];
-    const int nt = (int)(tw >> 60);
-    const int wi = (cx * dim + cy) * zc + (cz >> 5);
-    const uint32_t lt = lane_lt(cz & 31);
-    const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
-                         4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
-    const int64_t first = (iout + (int64_t)__ldg(ibase + wi)) / 3 + pre;
-    for (int t = 0; t < nt; ++t)
-      if ((tri_edge(tw, 3 * t) == e || tri_edge(tw, 3 * t + 1) == e || tri_edge(tw, 3 * t + 2) == e) && n < room)
-        out[n++] = (uint32_t)(first + t);
+// Which case tables a kernel stages in shared memory.
+template <bool TRI, bool USES, bool GRP>
+__device__ __forceinline__ void load_tabs_some(SmemTabs& t) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    if (TRI) t.tri[i] = __ldg(g_tri_cases + i);
+    if (USES) t.uses[i] = __ldg(g_edge_uses + i);
+    if (GRP) t.grp[i] = __ldg(g_group_cases + i);
   }
-  return n;
+  __syncthreads();
 }
 
 template <int MODE>
@@ -759,74 +726,91 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
                                                    uint32_t* __restrict__ adj) {
   __shared__ SmemTabs T;
-  __shared__ int s_crange[2];
-  load_tabs(T);
-  const int64_t nv = d_counts ? min(vcap, d_counts[0]) : vcap;
-  for (int64_t v0 = (int64_t)blockIdx.x * blockDim.x; v0 < nv; v0 += (int64_t)gridDim.x * blockDim.x) {
-    // the chunks this tile of vertices spans
-    __syncthreads();
-    if (threadIdx.x == 0) s_crange[0] = find_chunk_by_vertex(chunks, n_chunks, v0);
-    if (threadIdx.x == 32) s_crange[1] = find_chunk_by_vertex(chunks, n_chunks, min(v0 + (int64_t)blockDim.x, nv) - 1);
-    __syncthreads();
-    const int64_t v = v0 + threadIdx.x;
-    if (v >= nv) continue;
-    int c = s_crange[0];
-    for (int hi = s_crange[1]; c < hi;) {  // last chunk in range whose vout <= v
-      const int mid = (c + hi + 1) >> 1;
-      if (chunks[mid].vout <= v) c = mid; else hi = mid - 1;
+  load_tabs_some<MODE == 0, MODE == 0, MODE != 0>(T);
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
+  const int c = find_chunk_by_vertex(chunks, n_chunks, v);
+  const ChunkDev& ch = chunks[c];
+  const int dim = ch.dim, zc = ch.zc;
+  const int64_t iout = ch.iout;
+  const uint32_t* W = words + ch.words;
+  const uint32_t* ibase = ws.icnt + ch.words;
+  const uint32_t* pl = ws.gpl + 3 * ch.words;
+  const uint32_t key = vkey[v];
+  const int lin = (int)(key >> 2), k = (int)(key & 3u);
+  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+  uint32_t* out = adj + off[v];
+  // the vertex's CSR range (the exclusive scan of init_valence): never write past it
+  const int room = (int)(off[v + 1] - off[v]);
+  int n = 0;
+  if (MODE == 0) {
+    const int a = k;
+    // inside bits of lines (x-1+i, y-1+j), samples z-1..z+1, packed 3 bits per
+    // line at bit 3 (3i + j): every corner of the four cells around the edge
+    uint32_t nbits = 0u;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (a == 0 ? i >= 1 : (a == 1 ? j >= 1 : true))
+          nbits |= line_bits3(W, dim, zc, x - 1 + i, y - 1 + j, z - 1) << (3 * (3 * i + j));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {  // cells around the edge, ascending linear order
+      const int d1 = (q >> 1) ^ 1, d2 = (q & 1) ^ 1;
+      int ox = 0, oy = 0, oz = 0;
+      if (a == 0) { oy = -d1; oz = -d2; }
+      else if (a == 1) { ox = -d1; oz = -d2; }
+      else { ox = -d1; oy = -d2; }
+      const int e = 4 * a + 2 * d1 + d2;
+      const int cx = x + ox, cy = y + oy, cz = z + oz;
+      if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
+      // corner (dx, dy, dz): line (1 + ox + dx, 1 + oy + dy), bit 1 + oz + dz
+      const uint32_t base = nbits >> (3 * (3 * (1 + ox) + (1 + oy)) + 1 + oz);
+      const int m = (int)((base & 3u) | (((base >> 3) & 3u) << 2) | (((base >> 9) & 3u) << 4) |
+                          (((base >> 12) & 3u) << 6));
+      if (!tab_uses(T, m, e)) continue;
+      const uint64_t tw = T.tri[m];
+      const int nt = (int)(tw >> 60);
+      const int wi = (cx * dim + cy) * zc + (cz >> 5);
+      const uint32_t lt = lane_lt(cz & 31);
+      const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
+                           4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
+      const int64_t first = (iout + (int64_t)__ldg(ibase + wi)) / 3 + pre;
+      for (int t = 0; t < nt; ++t)
+        if ((tri_edge(tw, 3 * t) == e || tri_edge(tw, 3 * t + 1) == e || tri_edge(tw, 3 * t + 2) == e) && n < room)
+          out[n++] = (uint32_t)(first + t);
     }
-    const ChunkDev& ch = chunks[c];
-    const int dim = ch.dim, zc = ch.zc;
-    const int64_t iout = ch.iout;
-    const uint32_t* W = words + ch.words;
-    const uint32_t* ibase = ws.icnt + ch.words;
-    const uint32_t* pl = ws.gpl + 3 * ch.words;
-    const uint32_t key = vkey[v];
-    const int lin = (int)(key >> 2), k = (int)(key & 3u);
-    const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
-    uint32_t* out = adj + off[v];
-    // the vertex's CSR range (the exclusive scan of init_valence): never write past it
-    const int room = (int)(off[v + 1] - off[v]);
-    int n = 0;
-    if (MODE == 0) {
-      if (k == 0) n = adj_edge_r<0>(T, W, pl, ibase, iout, dim, zc, x, y, z, out, room);
-      else if (k == 1) n = adj_edge_r<1>(T, W, pl, ibase, iout, dim, zc, x, y, z, out, room);
-      else n = adj_edge_r<2>(T, W, pl, ibase, iout, dim, zc, x, y, z, out, room);
-    } else {
-      const int g = k;
-      const int m = cell_mask_at(W, dim, zc, x, y, z);
-      uint32_t ids[12];
-      const uint64_t gw = T.grp[m];
-      for (int e = 0; e < 12; ++e) {
-        if ((int)((gw >> (4 * e)) & 0xF) != g) continue;
-        const int c0 = edge_c0(e), a = e >> 2;
-        const int sx = x + ((c0 >> 2) & 1), sy = y + ((c0 >> 1) & 1), sz = z + (c0 & 1);
-        if (!q_edge_interior(dim, sx, sy, sz, a)) continue;
-        uint32_t Xi, Yi, Zi;
-        q_quad_words(W, dim, zc, sx, sy, sz >> 5, Xi, Yi, Zi);
-        const int l = sz & 31;
-        const uint32_t lt = lane_lt(l);
-        uint32_t pre = __popc(Xi & lt) + __popc(Yi & lt) + __popc(Zi & lt);
-        if (a >= 1) pre += (Xi >> l) & 1u;
-        if (a >= 2) pre += (Yi >> l) & 1u;
-        const int wi = (sx * dim + sy) * zc + (sz >> 5);
-        uint32_t id = (uint32_t)((iout + (int64_t)__ldg(ibase + wi)) / 4 + pre);
-        int j = n++;  // insertion into the sorted prefix
-        while (j > 0 && ids[j - 1] > id) { ids[j] = ids[j - 1]; --j; }
-        ids[j] = id;
-      }
-      for (int i = 0; i < n && i < room; ++i) out[i] = ids[i];
+  } else {
+    const int g = k;
+    const int m = cell_mask_at(W, dim, zc, x, y, z);
+    uint32_t ids[12];
+    const uint64_t gw = T.grp[m];
+    for (int e = 0; e < 12; ++e) {
+      if ((int)((gw >> (4 * e)) & 0xF) != g) continue;
+      const int c0 = edge_c0(e), a = e >> 2;
+      const int sx = x + ((c0 >> 2) & 1), sy = y + ((c0 >> 1) & 1), sz = z + (c0 & 1);
+      if (!q_edge_interior(dim, sx, sy, sz, a)) continue;
+      uint32_t Xi, Yi, Zi;
+      q_quad_words(W, dim, zc, sx, sy, sz >> 5, Xi, Yi, Zi);
+      const int l = sz & 31;
+      const uint32_t lt = lane_lt(l);
+      uint32_t pre = __popc(Xi & lt) + __popc(Yi & lt) + __popc(Zi & lt);
+      if (a >= 1) pre += (Xi >> l) & 1u;
+      if (a >= 2) pre += (Yi >> l) & 1u;
+      const int wi = (sx * dim + sy) * zc + (sz >> 5);
+      uint32_t id = (uint32_t)((iout + (int64_t)__ldg(ibase + wi)) / 4 + pre);
+      int j = n++;  // insertion into the sorted prefix
+      while (j > 0 && ids[j - 1] > id) { ids[j] = ids[j - 1]; --j; }
+      ids[j] = id;
     }
+    for (int i = 0; i < n && i < room; ++i) out[i] = ids[i];
   }
 }
 
 void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
                       const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,
                       uint32_t* adj, cudaStream_t st) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int blocks = (int)min((vcap + 255) / 256, (int64_t)sms * 8);
+  const int blocks = (int)((vcap + 255) / 256);
   if (blocks == 0) return;
   if (mode == 0) k_adj_build<0><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
   else k_adj_build<1><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
@@ -860,6 +844,15 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int k) {
   if (k >= c) { k -= c; m >>= 2; pos += 2; }
   if (k >= (int)(m & 1u)) pos += 1;
   return pos;
+}
+
+// Corner mask of the cell at offset (ox, oy, oz) in {-1, 0} from sample
+// (x, y, z), from the inside bits of lines (x-1+i, y-1+j) at samples z-1..z+1
+// packed 3 bits per line at bit 3 (3i + j): corner (dx, dy, dz) is bit
+// 3 (3 (1 + ox + dx) + 1 + oy + dy) + 1 + oz + dz.
+__device__ __forceinline__ int packed_mask(uint32_t nbits, int ox, int oy, int oz) {
+  const uint32_t b = nbits >> (3 * (3 * (1 + ox) + (1 + oy)) + 1 + oz);
+  return (int)((b & 3u) | (((b >> 3) & 3u) << 2) | (((b >> 9) & 3u) << 4) | (((b >> 12) & 3u) << 6));
 }
 
 // Mode R emission over the busy-word list.  A CTA takes kTileWords list
@@ -990,6 +983,17 @@ __global__ void __launch_bounds__(256) k_emit_words_r(const ChunkDev* __restrict
       const uint32_t X = R.X[t], Y = R.Y[t], Z = R.Z[t];
       const uint32_t own = ((X >> l) & 1u) | (((Y >> l) & 1u) << 1) | (((Z >> l) & 1u) << 2);
       const int64_t vout = R.vout[t];
+      // inside bits of lines (x-1..x+1, y-1..y+1) at samples z-1..z+1
+      uint32_t nbits = 0u;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int zr0 = l + 31, b = zr0 >> 5;  // z - 1 relative to block zb - 1
+          const uint32_t* w = nb.w + (i * 4 + j) * 3;
+          const uint64_t q = ((uint64_t)w[b + 1] << 32) | w[b];
+          nbits |= ((uint32_t)(q >> (zr0 & 31)) & 7u) << (3 * (3 * i + j));
+        }
       if (own) {
         const float* D = dens + R.dens[t];
         uint32_t vid = nb.vb[0] + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
@@ -1022,13 +1026,14 @@ __global__ void __launch_bounds__(256) k_emit_words_r(const ChunkDev* __restrict
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
               const int d1 = k >> 1, d2 = k & 1;
-              int cx = x, cy = y, cz = z, e;
-              if (a == 0) { cy -= d1; cz -= d2; e = 2 * d1 + d2; }
-              else if (a == 1) { cx -= d1; cz -= d2; e = 4 + 2 * d1 + d2; }
-              else { cx -= d1; cy -= d2; e = 8 + 2 * d1 + d2; }
+              int ox = 0, oy = 0, oz = 0;
+              if (a == 0) { oy = -d1; oz = -d2; }
+              else if (a == 1) { ox = -d1; oz = -d2; }
+              else { ox = -d1; oy = -d2; }
+              const int e = 4 * a + 2 * d1 + d2;
+              const int cx = x + ox, cy = y + oy, cz = z + oz;
               if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
-              const int m = nb_mask(nb, cx - x + 1, cy - y + 1, cz - 32 * (zb - 1));
-              val += (int)((s_uses[m] >> (4 * e)) & 0xF);
+              val += (int)((s_uses[packed_mask(nbits, ox, oy, oz)] >> (4 * e)) & 0xF);
             }
             out.valence[gv] = (uint8_t)val;
           }
@@ -1036,7 +1041,7 @@ __global__ void __launch_bounds__(256) k_emit_words_r(const ChunkDev* __restrict
       }
       // triangles: polygonize_cell order
       if (x >= dim - 1 || y >= dim - 1 || z >= dim - 1) continue;
-      const uint64_t tw = s_tri[nb_mask(nb, 1, 1, l + 32)];
+      const uint64_t tw = s_tri[packed_mask(nbits, 0, 0, 0)];
       const int t3 = 3 * (int)(tw >> 60);
       if (t3 == 0) continue;
       const int before = __popc(R.p0[t] & lt) + 2 * __popc(R.p1[t] & lt) + 4 * __popc(R.p2[t] & lt);
@@ -1184,10 +1189,22 @@ int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks,
                 int n_units, const uint32_t* words, const float* dens, const uint32_t* flags, WordScratch ws,
                 MeshOut out, const int64_t* d_counts, cudaStream_t st) {
   if (mode == 0 && ws.clist) {
-    int dev = 0, sms = 0;
+    // persistent: one wave of resident CTAs
+    static int grid[64] = {};
+    int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_emit_words_r<<<sms * 4, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+    if (dev < 0 || dev >= 64 || grid[dev] == 0) {
+      int sms = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_words_r, 256, 0);
+      const int g = sms * (per_sm > 0 ? per_sm : 1);
+      if (dev < 0 || dev >= 64) {
+        k_emit_words_r<<<g, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+        return 1;
+      }
+      grid[dev] = g;
+    }
+    k_emit_words_r<<<grid[dev], 256, 0, st>>>(d_chunks, words, dens, ws, out);
   } else if (mode == 0) {
     k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else if (ws.clist) {
