@@ -855,120 +855,122 @@ __device__ __forceinline__ int packed_mask(uint32_t nbits, int ox, int oy, int o
   return (int)((b & 3u) | (((b >> 3) & 3u) << 2) | (((b >> 9) & 3u) << 4) | (((b >> 12) & 3u) << 6));
 }
 
-// Mode R emission over the busy-word list.  A CTA takes kTileWords list
+// Mode R emission over the busy-word list.  Each warp takes kTileWords list
 // entries at a time and stages, per word, its neighbourhood (NbCache: the
 // occupancy words of lines (x-1..x+2, y-1..y+2) in blocks zb-1..zb+1 and the
 // scanned vertex bases of lines (x..x+1, y..y+1) in blocks zb..zb+1), its
-// index base and its triangle-count planes in shared memory.  Then one thread
+// index base and its triangle-count planes in shared memory.  Then one lane
 // per active cell of the tile (a flattened scan of the words' active-cell
 // counts) writes exactly what the reference writes for that cell: its owned
 // vertices (ids from the word base and the crossing words,
 // calculate_isovertex positions, boundary, key, init_valence) and its
 // triangles (slot from the word's index base and the count planes).  Every
 // mask, valence and neighbour vertex id is read from shared memory; only the
-// two endpoint densities of a vertex come from global memory.
-constexpr int kTileWords = 64;
+// two endpoint densities of a vertex come from global memory.  Warps work on
+// their own tiles with no block-wide barrier, so one warp's staging loads
+// overlap the others' cell work.
+constexpr int kTileWords = 8;
 constexpr int kTileSlots = 48 + 8 + 4;  // neighbour words, vertex bases, index base, 3 planes
+constexpr int kEmitWarps = 8;
 
 struct RTile {
   NbCache nb[kTileWords];
   uint32_t ib[kTileWords], p0[kTileWords], p1[kTileWords], p2[kTileWords];
   uint32_t X[kTileWords], Y[kTileWords], Z[kTileWords], act[kTileWords];
   int x[kTileWords], y[kTileWords], zb[kTileWords], dim[kTileWords], zc[kTileWords];
-  int64_t w0[kTileWords], dens[kTileWords], vout[kTileWords], iout[kTileWords];
+  int64_t cw[kTileWords], dens[kTileWords], vout[kTileWords], iout[kTileWords];
   int off[kTileWords + 1];
 };
 
-__global__ void __launch_bounds__(256) k_emit_words_r(const ChunkDev* __restrict__ chunks,
-                                                      const uint32_t* __restrict__ words,
-                                                      const float* __restrict__ dens, WordScratch ws, MeshOut out) {
+__global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const ChunkDev* __restrict__ chunks,
+                                                                 const uint32_t* __restrict__ words,
+                                                                 const float* __restrict__ dens, WordScratch ws,
+                                                                 MeshOut out) {
   __shared__ uint64_t s_tri[256], s_uses[256];
-  __shared__ RTile R;
-  __shared__ int s_wsum[kTileWords / 32];
+  __shared__ RTile s_tiles[kEmitWarps];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
     s_tri[i] = __ldg(g_tri_cases + i);
     s_uses[i] = __ldg(g_edge_uses + i);
   }
+  __syncthreads();
   const int64_t n = min((int64_t)*ws.ccount, ws.clist_cap);
-  const int tid = threadIdx.x, lane = tid & 31;
-  for (int64_t t0 = (int64_t)blockIdx.x * kTileWords; t0 < n; t0 += (int64_t)gridDim.x * kTileWords) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  RTile& R = s_tiles[warp];
+  const int64_t nwarps = (int64_t)gridDim.x * kEmitWarps;
+  for (int64_t t0 = ((int64_t)blockIdx.x * kEmitWarps + warp) * kTileWords; t0 < n; t0 += nwarps * kTileWords) {
     const int nt = (int)min((int64_t)kTileWords, n - t0);
     // 1. the tile's words
-    if (tid < nt) {
-      const uint2 e = ws.clist[t0 + tid];
+    if (lane < nt) {
+      const uint2 e = ws.clist[t0 + lane];
       const ChunkDev& ch = chunks[e.x];
       const int dim = ch.dim, zc = ch.zc, wi = (int)e.y;
       const int xy = wi / zc;
-      R.zb[tid] = wi - xy * zc;
-      R.y[tid] = xy % dim;
-      R.x[tid] = xy / dim;
-      R.dim[tid] = dim;
-      R.zc[tid] = zc;
-      R.w0[tid] = ch.words + wi;
-      R.dens[tid] = ch.dens;
-      R.vout[tid] = ch.vout;
-      R.iout[tid] = ch.iout;
+      R.zb[lane] = wi - xy * zc;
+      R.y[lane] = xy % dim;
+      R.x[lane] = xy / dim;
+      R.dim[lane] = dim;
+      R.zc[lane] = zc;
+      R.cw[lane] = ch.words;
+      R.dens[lane] = ch.dens;
+      R.vout[lane] = ch.vout;
+      R.iout[lane] = ch.iout;
     }
-    __syncthreads();
+    __syncwarp();
     // 2. stage the neighbourhoods (zeros outside the chunk)
-    for (int k = tid; k < nt * kTileSlots; k += blockDim.x) {
+    for (int k = lane; k < nt * kTileSlots; k += 32) {
       const int t = k / kTileSlots, sl = k - t * kTileSlots;
       const int dim = R.dim[t], zc = R.zc[t], x = R.x[t], y = R.y[t], zb = R.zb[t];
-      const int64_t w0 = R.w0[t];
-      const int64_t cw = w0 - (((int64_t)x * dim + y) * zc + zb);  // chunk's first word
+      const int64_t cw = R.cw[t];
+      const int wi = (x * dim + y) * zc + zb;
       if (sl < 48) {
         const int i = sl / 12, j = (sl / 3) & 3, b = sl % 3;
         R.nb[t].w[sl] = word_at(words + cw, dim, zc, x - 1 + i, y - 1 + j, zb - 1 + b);
       } else if (sl < 56) {
         const int l = sl - 48;
         const int xx = x + (l >> 2), yy = y + ((l >> 1) & 1), bb = zb + (l & 1);
-        R.nb[t].vb[l] = (xx < dim && yy < dim && bb < zc) ? __ldg(ws.vcnt + cw + ((int64_t)xx * dim + yy) * zc + bb)
-                                                         : 0u;
+        R.nb[t].vb[l] = (xx < dim && yy < dim && bb < zc) ? __ldg(ws.vcnt + cw + (xx * dim + yy) * zc + bb) : 0u;
       } else if (sl == 56) {
-        R.ib[t] = __ldg(ws.icnt + w0);
+        R.ib[t] = __ldg(ws.icnt + cw + wi);
       } else {
-        const uint32_t v = __ldg(ws.gpl + 3 * w0 + (sl - 57));
+        const uint32_t v = __ldg(ws.gpl + 3 * (cw + wi) + (sl - 57));
         if (sl == 57) R.p0[t] = v;
         else if (sl == 58) R.p1[t] = v;
         else R.p2[t] = v;
       }
     }
-    __syncthreads();
+    __syncwarp();
     // 3. active cells per word (owned crossings or triangles), flattened
-    if (tid < kTileWords) {
+    {
       int cnt = 0;
-      if (tid < nt) {
-        const NbCache& nb = R.nb[tid];
-        const int dim = R.dim[tid], x = R.x[tid], y = R.y[tid], zb = R.zb[tid];
+      if (lane < nt) {
+        const NbCache& nb = R.nb[lane];
+        const int dim = R.dim[lane], x = R.x[lane], y = R.y[lane], zb = R.zb[lane];
         const uint32_t wc = nb.w[(1 * 4 + 1) * 3 + 1];
         const uint32_t X = (x + 1 < dim) ? wc ^ nb.w[(2 * 4 + 1) * 3 + 1] : 0u;
         const uint32_t Y = (y + 1 < dim) ? wc ^ nb.w[(1 * 4 + 2) * 3 + 1] : 0u;
         uint32_t Z = wc ^ ((wc >> 1) | (nb.w[(1 * 4 + 1) * 3 + 2] << 31));
         const int valid = dim - 1 - 32 * zb;
         if (valid < 32) Z &= valid <= 0 ? 0u : ((1u << valid) - 1u);
-        const uint32_t act = R.p0[tid] | R.p1[tid] | R.p2[tid] | X | Y | Z;
-        R.X[tid] = X;
-        R.Y[tid] = Y;
-        R.Z[tid] = Z;
-        R.act[tid] = act;
+        const uint32_t act = R.p0[lane] | R.p1[lane] | R.p2[lane] | X | Y | Z;
+        R.X[lane] = X;
+        R.Y[lane] = Y;
+        R.Z[lane] = Z;
+        R.act[lane] = act;
         cnt = __popc(act);
       }
       int incl = cnt;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
+      for (int o = 1; o < kTileWords; o <<= 1) {
         const int v = __shfl_up_sync(kFull, incl, o);
         if (lane >= o) incl += v;
       }
-      if (lane == 31) s_wsum[tid >> 5] = incl;
-      R.off[tid + 1] = incl;  // warp-local for now
+      if (lane < kTileWords) R.off[lane + 1] = incl;
+      if (lane == 0) R.off[0] = 0;
     }
-    if (tid == 0) R.off[0] = 0;
-    __syncthreads();
-    if (tid >= 32 && tid < kTileWords) R.off[tid + 1] += s_wsum[0];
-    __syncthreads();
+    __syncwarp();
     const int total = R.off[nt];
-    // 4. one thread per active cell
-    for (int j = tid; j < total; j += blockDim.x) {
+    // 4. one lane per active cell
+    for (int j = lane; j < total; j += 32) {
       int lo = 0, hi = nt - 1;  // last t with off[t] <= j
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
@@ -1058,7 +1060,7 @@ __global__ void __launch_bounds__(256) k_emit_words_r(const ChunkDev* __restrict
         }
       }
     }
-    __syncthreads();  // the next tile overwrites the stage
+    __syncwarp();  // the next tile overwrites the stage
   }
 }
 
@@ -1196,15 +1198,15 @@ int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks,
     if (dev < 0 || dev >= 64 || grid[dev] == 0) {
       int sms = 0, per_sm = 0;
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_words_r, 256, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_words_r, 32 * kEmitWarps, 0);
       const int g = sms * (per_sm > 0 ? per_sm : 1);
       if (dev < 0 || dev >= 64) {
-        k_emit_words_r<<<g, 256, 0, st>>>(d_chunks, words, dens, ws, out);
+        k_emit_words_r<<<g, 32 * kEmitWarps, 0, st>>>(d_chunks, words, dens, ws, out);
         return 1;
       }
       grid[dev] = g;
     }
-    k_emit_words_r<<<grid[dev], 256, 0, st>>>(d_chunks, words, dens, ws, out);
+    k_emit_words_r<<<grid[dev], 32 * kEmitWarps, 0, st>>>(d_chunks, words, dens, ws, out);
   } else if (mode == 0) {
     k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else if (ws.clist) {
