@@ -571,7 +571,7 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
     if ((s = bail(cudaMemcpy(b->d_fill_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice),
                   "upload fill items")) != BMF_OK)
       return s;
-    b->fill_grid = fill_terrain_resident_ctas(b->fill_run);
+    b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5]);
     b->fill_mode = 2;
   }
   *out = b;
@@ -823,15 +823,15 @@ bmf_status bmf_batch_set_tuning(bmf_batch* b, const bmf_batch_tuning* t) {
   bmf_ctx* ctx = b->ctx;
   const bool terrain = b->field.kind == BMF_FIELD_TERRAIN_FBM;
   if (t->fill_mode < 0 || t->fill_mode > 2 || (!terrain && t->fill_mode != 0) ||
-      (t->fill_run != 4 && t->fill_run != 8 && t->fill_run != 16 && t->fill_run != 32) ||
+      (t->fill_run != 4 && t->fill_run != 8 && t->fill_run != 16) ||
       (t->sweep_block != 128 && t->sweep_block != 256 && t->sweep_block != 512))
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
-                "bmf_batch_set_tuning: fill_mode 0..2 (1, 2 for terrain fields only), fill_run 4/8/16/32, "
+                "bmf_batch_set_tuning: fill_mode 0..2 (1, 2 for terrain fields only), fill_run 4/8/16, "
                 "sweep_block 128/256/512");
   b->fill_mode = t->fill_mode;
   if (t->fill_run != b->fill_run) {
     b->fill_run = t->fill_run;
-    if (terrain) b->fill_grid = fill_terrain_resident_ctas(b->fill_run);
+    if (terrain) b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5]);
   }
   b->ps.block = t->sweep_block;
   if (b->exec) {
@@ -880,7 +880,7 @@ bmf_status bmf_batch_autotune(bmf_batch* b, bmf_batch_out* out, int32_t reps, vo
   };
   // stage 1: density fill + labels
   if (b->field.kind == BMF_FIELD_TERRAIN_FBM) {
-    const int cand[9][2] = {{0, 8}, {1, 4}, {1, 8}, {1, 16}, {1, 32}, {2, 4}, {2, 8}, {2, 16}, {2, 32}};
+    const int cand[7][2] = {{0, 8}, {1, 4}, {1, 8}, {1, 16}, {2, 4}, {2, 8}, {2, 16}};
     float best_ms = 1e30f;
     for (const auto& c : cand) {
       bmf_batch_tuning t = best;

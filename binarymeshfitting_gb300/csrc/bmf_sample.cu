@@ -122,15 +122,68 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
 // atomic ticket; the queue is ordered largest chunks first) or, with no queue,
 // one CTA per item.
 // ---------------------------------------------------------------------------
-// RUN (z-samples per step; 4, 8, 16 or 32, dividing 32 so that a run's inside
-// bits land in one word) is the tile height the batch autotuner picks.
+// RUN (z-samples per step; 4, 8 or 16, dividing 16 so that a run's inside
+// bits land in one word and its densities in one staged half block) is the
+// tile height the batch autotuner picks.
 constexpr int kFillLines = 256; // lines per item = threads per CTA
 constexpr int kMaxOctaves = 32;
-constexpr int kMaxFillRun = 32;
+constexpr int kMaxFillRun = 16;
 // z terms {zf, zf - 1, fade(zf), Z} per (octave, z): for every z of the
 // item's lines at once when octaves * dim fit, else per run
 constexpr int kZtEntries = 1024;
 static_assert(kZtEntries >= kMaxOctaves * kMaxFillRun, "per-run z terms fit");
+
+// Per (line, octave) state of the line walk: the x/y terms, the four hash
+// bases (bytes of p), and the alpha / beta pairs of the current z-lattice cell Zp.
+struct OctLine {
+  float xf, yf, u, v, a0, b0, a1, b1;
+  uint32_t p;
+  int Zp;
+};
+
+__device__ __forceinline__ void oct_line_init(OctLine& s, float px, float py, float fr,
+                                              const int* __restrict__ perm2) {
+  const float xs = px * fr, ys = py * fr;
+  const float fx = floorf(xs), fy = floorf(ys);
+  const int X = ((int)fx) & 255, Y = ((int)fy) & 255;
+  s.xf = xs - fx;
+  s.yf = ys - fy;
+  s.u = fade(s.xf);
+  s.v = fade(s.yf);
+  const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
+  s.p = (uint32_t)perm2[A] | ((uint32_t)perm2[A + 1] << 8) | ((uint32_t)perm2[B] << 16) |
+        ((uint32_t)perm2[B + 1] << 24);
+  s.Zp = -1;
+}
+
+// Enter z-lattice cell Z: when it is the next cell, the old layer-1 pair is
+// the new layer-0 pair; otherwise both layers are set up.
+__device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const uint4* __restrict__ gtab) {
+  const int pA = (int)(s.p & 255u), pA1 = (int)((s.p >> 8) & 255u), pB = (int)((s.p >> 16) & 255u),
+            pB1 = (int)(s.p >> 24);
+  const float x1 = s.xf - 1.0f, y1 = s.yf - 1.0f;
+  if (s.Zp >= 0 && Z == ((s.Zp + 1) & 255)) {
+    s.a0 = s.a1;
+    s.b0 = s.b1;
+  } else {
+    layer_coeffs(gtab, pA + Z, pB + Z, pA1 + Z, pB1 + Z, s.xf, s.yf, x1, y1, s.u, s.v, s.a0, s.b0);
+  }
+  const int Z1 = Z + 1;
+  layer_coeffs(gtab, pA + Z1, pB + Z1, pA1 + Z1, pB1 + Z1, s.xf, s.yf, x1, y1, s.u, s.v, s.a1, s.b1);
+  s.Zp = Z;
+}
+
+// Dynamic shared memory: the density stage (16-sample half blocks of the
+// CTA's lines, rows padded to 17 floats) and, for up to kCacheOctaves
+// octaves, each line's lattice-cell state (alpha / beta pairs and Zp) carried
+// from one run to the next, so a run re-enters a cell only when Z changes.
+constexpr int kStageRow = 17;
+constexpr int kCacheOctaves = 8;
+constexpr size_t kStageFloats = (size_t)kFillLines * kStageRow;
+__host__ __device__ constexpr size_t fill_smem_bytes(int octaves) {
+  return sizeof(float) * kStageFloats +
+         (octaves <= kCacheOctaves ? (size_t)octaves * kFillLines * (sizeof(float4) + sizeof(int)) : 0);
+}
 
 template <int kFillRun>
 __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __restrict__ chunks,
@@ -142,9 +195,10 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
   __shared__ int perm2[512];
   __shared__ uint4 gtab[512];
   __shared__ float4 zt[kZtEntries];
-  // density of the CTA's lines for one 32-sample word block, flushed with
-  // coalesced 128-byte row stores (rows padded to 33: conflict-free columns)
-  extern __shared__ float s_stage[];
+  // density of the CTA's lines for one 16-sample half block, flushed with
+  // coalesced 64-byte row stores (rows padded to 17: conflict-free columns)
+  extern __shared__ float4 s_dyn[];
+  float* s_stage = reinterpret_cast<float*>(s_dyn);
   __shared__ int s_item;
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
     perm2[i] = field.perm[i & 255];
@@ -152,6 +206,9 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
   }
   const int oct = min((int)field.p[5], kMaxOctaves);
   const float h0 = field.p[0], ampl = field.p[1], freq = field.p[2], lac = field.p[3], gain = field.p[4];
+  const bool cache = oct <= kCacheOctaves;
+  float4* s_ab = s_dyn + kStageFloats / 4;                      // [octave][line]: a0, b0, a1, b1
+  int* s_zp = reinterpret_cast<int*>(s_ab + (size_t)oct * kFillLines);  // [octave][line]: Zp
   for (int pass = 0;; ++pass) {
     __syncthreads();
     if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1) : (pass == 0 ? (int)blockIdx.x : n_items);
@@ -203,43 +260,38 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
 #pragma unroll
       for (int k = 0; k < kFillRun; ++k) sum[k] = 0.0f;
       float amp = 1.0f, fr = freq;
+#pragma unroll 1
       for (int o = 0; o < oct; ++o) {
-        const float xs = px * fr, ys = py * fr;
-        const float fx = floorf(xs), fy = floorf(ys);
-        const int X = ((int)fx) & 255, Y = ((int)fy) & 255;
-        const float xf = xs - fx, yf = ys - fy;
-        const float u = fade(xf), v = fade(yf);
-        const float x1 = xf - 1.0f, y1 = yf - 1.0f;
-        const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
-        const int pA = perm2[A], pA1 = perm2[A + 1], pB = perm2[B], pB1 = perm2[B + 1];
-        float a0 = 0.0f, b0 = 0.0f, a1 = 0.0f, b1 = 0.0f;
-        int Zp = -1;
+        OctLine L;
+        oct_line_init(L, px, py, fr, perm2);
+        const int si = o * kFillLines + (int)threadIdx.x;
+        if (cache && zr > 0) {  // the cell this line was in at the end of its previous run
+          const float4 ab = s_ab[si];
+          L.a0 = ab.x;
+          L.b0 = ab.y;
+          L.a1 = ab.z;
+          L.b1 = ab.w;
+          L.Zp = s_zp[si];
+        }
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) {
           if (k >= n) break;
           const float4 t = zt[o * zt_o + zt_k + k];
           const int Z = __float_as_int(t.w);
-          if (Z != Zp) {  // same for every lane of the CTA
-            const int Z1 = Z + 1;
-            if (Zp >= 0 && Z == ((Zp + 1) & 255)) {  // the next cell: its layer 0 is the old layer 1
-              a0 = a1;
-              b0 = b1;
-            } else {
-              layer_coeffs(gtab, pA + Z, pB + Z, pA1 + Z, pB1 + Z, xf, yf, x1, y1, u, v, a0, b0);
-            }
-            layer_coeffs(gtab, pA + Z1, pB + Z1, pA1 + Z1, pB1 + Z1, xf, yf, x1, y1, u, v, a1, b1);
-            Zp = Z;
-          }
-          const float zf = t.x, z1 = t.y, w = t.z;
-          const float l0 = a0 + b0 * zf;
-          const float l1 = a1 + b1 * z1;
-          sum[k] = sum[k] + amp * (l0 + w * (l1 - l0));
+          if (Z != L.Zp) oct_line_cell(L, Z, gtab);  // same for every lane of the CTA
+          const float l0 = L.a0 + L.b0 * t.x;
+          const float l1 = L.a1 + L.b1 * t.y;
+          sum[k] = sum[k] + amp * (l0 + t.z * (l1 - l0));
+        }
+        if (cache) {
+          s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
+          s_zp[si] = L.Zp;
         }
         fr = fr * lac;
         amp = amp * gain;
       }
       uint32_t bits = 0u;
-      float* row = s_stage + threadIdx.x * 33 + (z0 & 31);
+      float* row = s_stage + threadIdx.x * kStageRow + (z0 & 15);
 #pragma unroll
       for (int k = 0; k < kFillRun; ++k) {
         if (k >= n) break;
@@ -254,18 +306,19 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         wacc = 0u;
       }
       }  // active
-      if (dens_out && (((z0 + kFillRun) & 31) == 0 || zr == nruns - 1)) {
-        // flush the word block: warp w writes rows [32w, 32w + 32), one
-        // 32-sample segment per row per instruction
+      if (dens_out && (((z0 + kFillRun) & 15) == 0 || zr == nruns - 1)) {
+        // flush the half block: warp w writes rows [32w, 32w + 32), two
+        // 16-sample row segments per instruction
         __syncthreads();
-        const int zb0 = z0 & ~31, nz = min(32, dim - zb0);
-        const int lane = threadIdx.x & 31, w0 = threadIdx.x & ~31;
-        for (int j = 0; j < 32; ++j) {
-          const int l = w0 + j;
-          if (item.y + l < dim * dim && lane < nz)
-            dens_out[ch.dens + (int64_t)(item.y + l) * dim + zb0 + lane] = s_stage[l * 33 + lane];
+        const int zh0 = z0 & ~15, nz = min(16, dim - zh0);
+        const int lane = threadIdx.x & 31, w0 = threadIdx.x & ~31, col = lane & 15;
+#pragma unroll 1
+        for (int j = 0; j < 32; j += 2) {
+          const int l = w0 + j + (lane >> 4);
+          if (item.y + l < dim * dim && col < nz)
+            dens_out[ch.dens + (int64_t)(item.y + l) * dim + zh0 + col] = s_stage[l * kStageRow + col];
         }
-        __syncthreads();  // the next word block's rows overwrite the stage
+        __syncthreads();  // the next half block's rows overwrite the stage
       }
     }
     fl = __reduce_or_sync(kFull, fl);
@@ -274,7 +327,6 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
   }
 }
 
-constexpr size_t kStageBytes = sizeof(float) * kFillLines * 33;
 
 // The kernels' static + staging shared memory exceeds the 48 KB default: opt
 // in once per device.
@@ -283,10 +335,10 @@ static void fill_terrain_smem_optin() {
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && done[dev]) return;
-  cudaFuncSetAttribute(k_fill_terrain<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
-  cudaFuncSetAttribute(k_fill_terrain<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
-  cudaFuncSetAttribute(k_fill_terrain<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
-  cudaFuncSetAttribute(k_fill_terrain<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageBytes);
+  const int mx = (int)fill_smem_bytes(kCacheOctaves);
+  cudaFuncSetAttribute(k_fill_terrain<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_fill_terrain<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_fill_terrain<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   if (dev >= 0 && dev < 64) done[dev] = true;
 }
 
@@ -297,32 +349,29 @@ void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items,
   if (d_queue) cudaMemsetAsync(d_queue, 0, sizeof(int), st);
   const int g = d_queue ? grid : n_items;
   fill_terrain_smem_optin();
-  const size_t sm = kStageBytes;
+  const size_t sm = fill_smem_bytes(min((int)field.p[5], kMaxOctaves));
   if (run == 4)
     k_fill_terrain<4><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
   else if (run == 16)
     k_fill_terrain<16><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
-  else if (run == 32)
-    k_fill_terrain<32><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
   else
     k_fill_terrain<8><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
 }
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
 int fill_terrain_lines() { return kFillLines; }
-int fill_terrain_resident_ctas(int run) {
+int fill_terrain_resident_ctas(int run, int octaves) {
+  const size_t sm = fill_smem_bytes(min(octaves, kMaxOctaves));
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   fill_terrain_smem_optin();
   if (run == 4)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4>, kFillLines, kStageBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4>, kFillLines, sm);
   else if (run == 16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16>, kFillLines, kStageBytes);
-  else if (run == 32)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<32>, kFillLines, kStageBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16>, kFillLines, sm);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8>, kFillLines, kStageBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8>, kFillLines, sm);
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 

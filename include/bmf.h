@@ -257,7 +257,7 @@ BMF_API bmf_status bmf_batch_format(bmf_batch* b, const bmf_batch_out* out, int3
 typedef struct {
   int32_t fill_mode;   /* terrain fill: 0 x-plane kernel, 1 one CTA per line item, 2 persistent CTAs taking
                           line items (largest chunks first) from a device work queue */
-  int32_t fill_run;    /* line kernel tile height: z-samples per thread step, 4, 8, 16 or 32 */
+  int32_t fill_run;    /* line kernel tile height: z-samples per thread step, 4, 8 or 16 */
   int32_t sweep_block; /* threads per CTA of the dual / primal sweeps: 128, 256 or 512 */
   int32_t reserved[5];
 } bmf_batch_tuning;

@@ -276,8 +276,7 @@ def test_batch_tunings_give_identical_results(ctx):
     assert b.tuning() == dict(fill_mode=2, fill_run=8, sweep_block=256)
     nv, ni = b.run(use_graph=True)
     ref = [bufs[k][:n].clone() for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"].clone()]
-    for fm, fr, sb in [(0, 8, 256), (1, 4, 128), (1, 16, 512), (2, 4, 256), (2, 16, 128), (1, 8, 512), (1, 32, 256),
-                       (2, 32, 512)]:
+    for fm, fr, sb in [(0, 8, 256), (1, 4, 128), (1, 16, 512), (2, 4, 256), (2, 16, 128), (1, 8, 512)]:
         b.set_tuning(fill_mode=fm, fill_run=fr, sweep_block=sb)
         for use_graph in (False, True):
             assert b.run(use_graph=use_graph) == (nv, ni)
@@ -286,7 +285,7 @@ def test_batch_tunings_give_identical_results(ctx):
                 assert torch.equal(r.view(torch.int32) if r.is_floating_point() else r,
                                    g_.view(torch.int32) if g_.is_floating_point() else g_), (fm, fr, sb)
     chosen, ms = b.autotune(reps=2)
-    assert len(ms) == 12 and all(m > 0 for m in ms)
+    assert len(ms) == 10 and all(m > 0 for m in ms)
     assert chosen["fill_mode"] in (0, 1, 2) and chosen["sweep_block"] in (128, 256, 512)
     assert b.tuning() == chosen
     got = [bufs[k][:n] for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"]]
