@@ -16,6 +16,7 @@ FIELD_TORUS_Z, FIELD_SPHERE, FIELD_CUBOID, FIELD_PLANE_Y = 3, 4, 5, 6
 MODE_R, MODE_Q = 0, 1
 PLACE_CENTER, PLACE_MASSPOINT, PLACE_QEF = 0, 1, 2
 FIT_ADJOINT_F64 = 1
+FIT_ADJOINT_DF = 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "output capacity exceeded", 4: "device wait timed out",
           5: "out of device memory", 6: "not supported"}

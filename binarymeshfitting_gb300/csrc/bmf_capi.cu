@@ -980,7 +980,8 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
   if (!ctx || !out) return BMF_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   if (n_chunks <= 0 || !dim_ok(dim) || (placement != BMF_PLACE_MASSPOINT && placement != BMF_PLACE_QEF) ||
-      iters < 0 || vcap <= 0 || icap <= 0 || (flags & ~BMF_FIT_ADJOINT_F64))
+      iters < 0 || vcap <= 0 || icap <= 0 || (flags & ~(BMF_FIT_ADJOINT_F64 | BMF_FIT_ADJOINT_DF)) ||
+      (flags & BMF_FIT_ADJOINT_F64 && flags & BMF_FIT_ADJOINT_DF))
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
                 "bmf_fit_create: bad count, dim, placement, iters, capacity or flags");
   bmf_fit* f = new bmf_fit();
@@ -1090,10 +1091,10 @@ bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_
   int k = launch_process_bwd(4, f->vcap, f->icap / 4, f->d_totals, f->d_boundary, f->d_valence, f->d_idxg, f->iters,
                              0, f->ps, f->d_g, st);
   BMF_CUDA(ctx, cudaMemsetAsync(d_grad_density, 0, sizeof(float) * (size_t)f->n * f->dim * f->dim * f->dim, st));
-  const bool f64 = (f->flags & BMF_FIT_ADJOINT_F64) != 0;
-  launch_place_bwd(f->placement, f64, f->d_chunks, f->n, f->d_words, f->last_density, f->d_vkey, f->d_totals,
+  const int wide = (f->flags & BMF_FIT_ADJOINT_F64) ? 1 : ((f->flags & BMF_FIT_ADJOINT_DF) ? 2 : 0);
+  launch_place_bwd(f->placement, wide, f->d_chunks, f->n, f->d_words, f->last_density, f->d_vkey, f->d_totals,
                    f->vcap, f->d_g, d_grad_density, f->d_qlist, f->d_qlist + f->vcap, st);
-  BMF_LAUNCHED(ctx, k + (f64 && f->placement == BMF_PLACE_QEF ? 2 : 1));
+  BMF_LAUNCHED(ctx, k + (wide && f->placement == BMF_PLACE_QEF ? 2 : 1));
   return BMF_OK;
 }
 

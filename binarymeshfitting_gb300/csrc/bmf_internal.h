@@ -132,13 +132,16 @@ int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_coun
 // Adjoint of Mode Q placement (placement 1 mass point, 2 QEF; f64: the QEF
 // derivative from an FP64 re-solve); accumulates into grad_dens (the caller
 // clears it).
-// The FP64 list pass of launch_place_bwd (bmf_adjoint64.cu).
-void launch_place_bwd_f64_list(const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, const float* dens,
-                               const uint32_t* vkey, const int64_t* d_counts, int64_t vcap, const float* grad_pos,
-                               float* grad_dens, uint32_t* qlist, uint32_t* qcount, cudaStream_t st);
-// qlist (vcap entries) + qcount: scratch of the two-pass FP64 form (nullable:
-// one pass, idle lanes in the FP64 code).
-void launch_place_bwd(int placement, int f64, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
+// The wide list pass of launch_place_bwd (bmf_adjoint64.cu): wide 1 = FP64,
+// 2 = double-float.
+void launch_place_bwd_wide_list(int wide, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
+                                const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
+                                const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount,
+                                cudaStream_t st);
+// qlist (vcap entries) + qcount: scratch of the two-pass wide form (nullable:
+// one pass, idle lanes in the wide code).  wide: 0 FP32 adjoint, 1 the QEF
+// derivative from an FP64 re-solve, 2 from a double-float re-solve.
+void launch_place_bwd(int placement, int wide, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
                       const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount,
                       cudaStream_t st);

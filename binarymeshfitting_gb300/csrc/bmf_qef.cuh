@@ -3,6 +3,7 @@
 #pragma once
 
 #include "bmf_device.cuh"
+#include "bmf_df.cuh"
 #include "bmf_internal.h"
 
 namespace bmf {
@@ -334,29 +335,41 @@ __device__ __forceinline__ void hermite_t(const float* D, int dim, int x, int y,
   }
 }
 
-// Symmetric 3x3 eigen decomposition in FP64, A = V diag(w) V^T, refined from
-// the forward's FP32 eigenvectors: V0 is re-orthonormalised (Gram-Schmidt),
-// A is rotated into that basis (nearly diagonal, off-diagonals ~1e-6 |A|)
-// and cyclic Jacobi rotations finish it; convergence is quadratic, so one or
-// two sweeps reach the 1e-17 |A| stopping point instead of five or six from
+// Symmetric 3x3 eigen decomposition in a wide type R (FP64 or double-float),
+// A = V diag(w) V^T, refined from the forward's FP32 eigenvectors: V0 is
+// re-orthonormalised (Gram-Schmidt), A is rotated into that basis (nearly
+// diagonal, off-diagonals ~1e-6 |A|) and cyclic Jacobi rotations finish it;
+// convergence is quadratic, so one or two sweeps reach the stopping point
+// (1e-17 |A| in FP64, 3e-14 |A| in double-float) instead of five or six from
 // the identity.
-static __device__ void eig3_refine(const double A[3][3], const float V0[3][3], double w[3], double V[3][3]) {
+// Stopping point of the refinement: 1e-17 |A| in FP64, 3e-14 |A| in
+// double-float (about its resolution).
+template <typename R>
+struct EigTol {
+  static constexpr double scale = 1e-17;
+};
+template <>
+struct EigTol<DF> {
+  static constexpr double scale = 3e-14;
+};
+template <typename R>
+__device__ void eig3_refine(const R A[3][3], const float V0[3][3], R w[3], R V[3][3]) {
   // columns of V0, orthonormalised
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    double v[3] = {(double)V0[0][c], (double)V0[1][c], (double)V0[2][c]};
+    R v[3] = {R(V0[0][c]), R(V0[1][c]), R(V0[2][c])};
 #pragma unroll
     for (int k = 0; k < c; ++k) {
-      const double d = v[0] * V[0][k] + v[1] * V[1][k] + v[2] * V[2][k];
+      const R d = v[0] * V[0][k] + v[1] * V[1][k] + v[2] * V[2][k];
 #pragma unroll
       for (int r = 0; r < 3; ++r) v[r] -= d * V[r][k];
     }
-    const double il = 1.0 / sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const R il = R(1.0f) / sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
 #pragma unroll
     for (int r = 0; r < 3; ++r) V[r][c] = v[r] * il;
   }
   // B = V^T A V
-  double AV[3][3], B[3][3];
+  R AV[3][3], B[3][3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
 #pragma unroll
@@ -370,9 +383,9 @@ static __device__ void eig3_refine(const double A[3][3], const float V0[3][3], d
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
 #pragma unroll
-    for (int c = 0; c < r; ++c) B[r][c] = B[c][r] = 0.5 * (B[r][c] + B[c][r]);
+    for (int c = 0; c < r; ++c) B[r][c] = B[c][r] = R(0.5f) * (B[r][c] + B[c][r]);
   }
-  const double tol = 1e-17 * (fabs(B[0][0]) + fabs(B[1][1]) + fabs(B[2][2]));
+  const R tol = R(EigTol<R>::scale) * (fabs(B[0][0]) + fabs(B[1][1]) + fabs(B[2][2]));
 #pragma unroll 1
   for (int sweep = 0; sweep < 16; ++sweep) {
     if (fabs(B[0][1]) + fabs(B[0][2]) + fabs(B[1][2]) <= tol) break;
@@ -380,24 +393,24 @@ static __device__ void eig3_refine(const double A[3][3], const float V0[3][3], d
     for (int q = 0; q < 3; ++q) {
       const int p = q == 2 ? 1 : 0, r = q == 0 ? 1 : 2;
       if (fabs(B[p][r]) <= tol) continue;
-      const double tau = (B[r][r] - B[p][p]) / (2.0 * B[p][r]);
-      const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-      const double c = 1.0 / sqrt(1.0 + t * t), s = t * c;
+      const R tau = (B[r][r] - B[p][p]) / (R(2.0f) * B[p][r]);
+      const R t = (tau >= R(0.0f) ? R(1.0f) : R(-1.0f)) / (fabs(tau) + sqrt(R(1.0f) + tau * tau));
+      const R c = R(1.0f) / sqrt(R(1.0f) + t * t), s = t * c;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const double bkp = B[k][p], bkr = B[k][r];
+        const R bkp = B[k][p], bkr = B[k][r];
         B[k][p] = c * bkp - s * bkr;
         B[k][r] = s * bkp + c * bkr;
       }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const double bpk = B[p][k], brk = B[r][k];
+        const R bpk = B[p][k], brk = B[r][k];
         B[p][k] = c * bpk - s * brk;
         B[r][k] = s * bpk + c * brk;
       }
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const double vkp = V[k][p], vkr = V[k][r];
+        const R vkp = V[k][p], vkr = V[k][r];
         V[k][p] = c * vkp - s * vkr;
         V[k][r] = s * vkp + c * vkr;
       }
@@ -461,7 +474,7 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
     // decided it); here the replay only seeds the FP64 eigenvectors
     if (LIST == 2) use_qef = true;
     if (use_qef) {
-      if (sizeof(T) == sizeof(float)) {
+      if constexpr (sizeof(T) == sizeof(float)) {
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
 #pragma unroll
@@ -475,13 +488,15 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
           Q.r[r] = (T)info.r[r];
         }
       } else {
-        // the same QEF in FP64: ATA, ATb, mass point, converged eigen pairs
-        double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, b[3] = {0, 0, 0}, m[3] = {0, 0, 0};
+        // the same QEF in the wide type (FP64 or double-float): ATA, ATb, mass
+        // point, converged eigen pairs
+        T A[3][3] = {{T(0.0f), T(0.0f), T(0.0f)}, {T(0.0f), T(0.0f), T(0.0f)}, {T(0.0f), T(0.0f), T(0.0f)}};
+        T b[3] = {T(0.0f), T(0.0f), T(0.0f)}, m[3] = {T(0.0f), T(0.0f), T(0.0f)};
         for (int e = 0; e < 12; ++e) {
           if (group_of(mask, e) != g) continue;
-          HermiteT<double> h;
-          hermite_t<double>(D, dim, x, y, z, e, true, h);
-          const double d = h.n[0] * h.p[0] + h.n[1] * h.p[1] + h.n[2] * h.p[2];
+          HermiteT<T> h;
+          hermite_t<T>(D, dim, x, y, z, e, true, h);
+          const T d = h.n[0] * h.p[0] + h.n[1] * h.p[1] + h.n[2] * h.p[2];
 #pragma unroll
           for (int r = 0; r < 3; ++r) {
 #pragma unroll
@@ -492,25 +507,25 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
         }
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          m[r] /= (double)cnt;
+          m[r] /= T(cnt);
 #pragma unroll
-          for (int k = 0; k < 3; ++k) Q.A[r][k] = (T)A[r][k];
+          for (int k = 0; k < 3; ++k) Q.A[r][k] = A[r][k];
         }
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-          Q.mp[r] = (T)m[r];
-          Q.r[r] = (T)(b[r] - (A[r][0] * m[0] + A[r][1] * m[1] + A[r][2] * m[2]));
+          Q.mp[r] = m[r];
+          Q.r[r] = b[r] - (A[r][0] * m[0] + A[r][1] * m[1] + A[r][2] * m[2]);
         }
-        double w[3], V[3][3];
-        eig3_refine(A, info.V, w, V);
+        T w[3], V[3][3];
+        eig3_refine<T>(A, info.V, w, V);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          const double oo = 1.0 / w[i];
-          const double mn = fabs(w[i]) < fabs(oo) ? fabs(w[i]) : fabs(oo);
-          Q.sigma[i] = (T)w[i];
-          Q.inv[i] = (T)(mn >= 0.001 ? oo : 0.0);
+          const T oo = T(1.0f) / w[i];
+          const T mn = fabs(w[i]) < fabs(oo) ? fabs(w[i]) : fabs(oo);
+          Q.sigma[i] = w[i];
+          Q.inv[i] = mn >= T(0.001f) ? oo : T(0.0f);
 #pragma unroll
-          for (int k = 0; k < 3; ++k) Q.V[k][i] = (T)V[k][i];
+          for (int k = 0; k < 3; ++k) Q.V[k][i] = V[k][i];
         }
       }
     }

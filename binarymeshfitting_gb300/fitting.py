@@ -14,18 +14,23 @@ from .engine import Context, _stream
 
 
 class FitPlan:
-    """n_chunks learnable grids of dim^3 samples (bmf_fit).  adjoint_f64: the
-    QEF adjoint from an FP64 re-solve (the derivative of the exact-arithmetic
-    placement); False differentiates the forward's own FP32 eigen pairs."""
+    """n_chunks learnable grids of dim^3 samples (bmf_fit).  adjoint: "df" (the
+    default) or "f64" take the QEF derivative from a re-solve of the hermite
+    data and eigen pairs in double-float or FP64 arithmetic (the derivative of
+    the exact-arithmetic placement; double-float gives FP64's accuracy here at
+    a fraction of the cost); "f32" differentiates the forward's own FP32 eigen
+    pairs.  adjoint_f64 (True / False) is the older spelling of "f64" / "f32"."""
 
     def __init__(self, ctx: Context, n_chunks, dim, placement=L.PLACE_QEF, iters=8, vcap=None, icap=None,
-                 adjoint_f64=True):
+                 adjoint="df", adjoint_f64=None):
         self.ctx = ctx
         self.n, self.dim, self.iters = n_chunks, dim, iters
         self.vcap = vcap or n_chunks * dim * dim * 4
         self.icap = icap or 4 * self.vcap
         h = ctypes.c_void_p()
-        flags = L.FIT_ADJOINT_F64 if adjoint_f64 else 0
+        if adjoint_f64 is not None:
+            adjoint = "f64" if adjoint_f64 else "f32"
+        flags = {"df": L.FIT_ADJOINT_DF, "f64": L.FIT_ADJOINT_F64, "f32": 0}[adjoint]
         ctx._check(ctx.lib.bmf_fit_create(ctx.h, n_chunks, dim, placement, iters, self.vcap, self.icap, flags,
                                           ctypes.byref(h)))
         self.h = h

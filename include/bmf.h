@@ -285,6 +285,10 @@ BMF_API bmf_status bmf_batch_autotune(bmf_batch* b, bmf_batch_out* out, int32_t 
 typedef struct bmf_fit bmf_fit;
 /* flags of bmf_fit_create */
 #define BMF_FIT_ADJOINT_F64 1 /* QEF adjoint from an FP64 re-solve of the hermite data and eigen pairs */
+/* QEF adjoint from a double-float re-solve (pairs of floats, ~48-bit
+ * significands; FP64's accuracy for this adjoint at a fraction of its cost on
+ * GPUs with a reduced FP64 rate).  Exclusive with BMF_FIT_ADJOINT_F64. */
+#define BMF_FIT_ADJOINT_DF 2
 BMF_API bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t placement, int32_t iters,
                                   int64_t vcap, int64_t icap, int32_t flags, bmf_fit** out);
 /* Positions (vcap*3) and chunk-local quad indices (icap) of all chunks, with

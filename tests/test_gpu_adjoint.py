@@ -78,8 +78,8 @@ def test_fit_forward_bit_exact(ctx):
     plan.close()
 
 
-def gpu_grad(ctx, d, reduce="mean", adjoint_f64=True):
-    plan = FitPlan(ctx, 1, DIM, L.PLACE_QEF, ITERS, adjoint_f64=adjoint_f64)
+def gpu_grad(ctx, d, reduce="mean", adjoint="df"):
+    plan = FitPlan(ctx, 1, DIM, L.PLACE_QEF, ITERS, adjoint=adjoint)
     dens = torch.from_numpy(d).cuda().requires_grad_(True)
     pos = ExtractFit.apply(dens, plan)
     loss = box_loss(pos, reduce)
@@ -101,7 +101,7 @@ def compare_kept(g, g64, near_branch):
 
 def test_fit_gradient_fp32_adjoint(ctx):
     d = sphere_noise()
-    _, g = gpu_grad(ctx, d, adjoint_f64=False)
+    _, g = gpu_grad(ctx, d, adjoint="f32")
     nb = np.zeros(DIM ** 3, np.uint8)
     _, g64, _, _ = cpu.fit_loss_f64(DIM, d.astype(np.float64), ITERS, BOX, want_grad=True, near_branch=nb)
     rel_l2, ok, _, _ = compare_kept(g, g64, nb)
@@ -109,19 +109,32 @@ def test_fit_gradient_fp32_adjoint(ctx):
     assert rel_l2 <= 1e-2
 
 
-def test_fit_gradient_matches_fp64_adjoint(ctx):
+@pytest.mark.parametrize("adjoint", ["df", "f64"])
+def test_fit_gradient_matches_fp64_adjoint(ctx, adjoint):
+    """The double-float and the FP64 re-solve against the FP64 oracle gradient."""
     d = sphere_noise()
-    loss, g = gpu_grad(ctx, d)
+    loss, g = gpu_grad(ctx, d, adjoint=adjoint)
     nb = np.zeros(DIM ** 3, np.uint8)
     loss64, g64, counts, _ = cpu.fit_loss_f64(DIM, d.astype(np.float64), ITERS, BOX, want_grad=True,
                                               near_branch=nb)
     assert abs(loss - loss64) <= 1e-4 * abs(loss64), (loss, loss64)
     rel_l2, ok, kept, nsup = compare_kept(g, g64, nb)
-    print("loss %.9g vs %.9g  rel_l2 %.3g  entries within tol %.5f of %d (samples kept %.4f; vertices %d, "
-          "QEF-placed %d)" % (loss, loss64, rel_l2, ok, nsup, kept, counts[0], counts[2]))
+    print("%s: loss %.9g vs %.9g  rel_l2 %.3g  entries within tol %.5f of %d (samples kept %.4f; vertices %d, "
+          "QEF-placed %d)" % (adjoint, loss, loss64, rel_l2, ok, nsup, kept, counts[0], counts[2]))
     assert rel_l2 <= 2e-4
     assert ok >= 0.999
     assert kept >= 0.98
+
+
+def test_df_adjoint_matches_f64_adjoint(ctx):
+    """Double-float and FP64 re-solves give the same gradient to well below the
+    oracle tolerance (both differentiate the exact-arithmetic placement)."""
+    d = sphere_noise(seed=5)
+    _, g_df = gpu_grad(ctx, d, adjoint="df")
+    _, g_64 = gpu_grad(ctx, d, adjoint="f64")
+    rel = np.linalg.norm(g_df - g_64) / np.linalg.norm(g_64)
+    print("df vs f64 adjoint: rel_l2 %.3g" % rel)
+    assert rel <= 2e-5
 
 
 def test_fit_batched_equals_single(ctx):
