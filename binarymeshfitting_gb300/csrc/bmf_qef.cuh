@@ -542,23 +542,23 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
     }
 #pragma unroll
     for (int r = 0; r < 3; ++r) gr[r] = Pm[r][0] * gx[0] + Pm[r][1] * gx[1] + Pm[r][2] * gx[2];
-    T Gs[3][3], M[3][3], F[3][3];
+    T Gs[3][3], M[3][3], F[3][3], W[3][3];
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) Gs[r][k] = (T)0.5 * (gx[r] * Q.r[k] + gx[k] * Q.r[r]);
     }
+    // M = V^T Gs V as two 3x3 products (W = Gs V, then V^T W)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b) W[r][b] = Gs[r][0] * Q.V[0][b] + Gs[r][1] * Q.V[1][b] + Gs[r][2] * Q.V[2][b];
+    }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        T s = (T)0;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) s += Q.V[r][a] * Gs[r][k] * Q.V[k][b];
-        }
-        M[a][b] = s;
+        M[a][b] = Q.V[0][a] * W[0][b] + Q.V[1][a] * W[1][b] + Q.V[2][a] * W[2][b];
         // f(s) = 1/s: (f_a - f_b) / (s_a - s_b) = -f_a f_b (no cancellation for
         // close eigenvalues) and f'(s) = -f^2; a truncated eigenvalue (f = 0)
         // beside a kept one takes the quotient
@@ -569,48 +569,63 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
           F[a][b] = (T)0;
         else
           F[a][b] = (fa - fb) / (sa - sb);
+        F[a][b] = F[a][b] * M[a][b];
       }
+    }
+    // gA = V (F o M) V^T - sym(gr mp^T), again as two products
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int b = 0; b < 3; ++b) W[r][b] = Q.V[r][0] * F[0][b] + Q.V[r][1] * F[1][b] + Q.V[r][2] * F[2][b];
     }
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        T s = (T)0;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-#pragma unroll
-          for (int b = 0; b < 3; ++b) s += Q.V[r][a] * F[a][b] * M[a][b] * Q.V[k][b];
-        }
+        const T s = W[r][0] * Q.V[k][0] + W[r][1] * Q.V[k][1] + W[r][2] * Q.V[k][2];
         gA[r][k] = s - (T)0.5 * (gr[r] * Q.mp[k] + gr[k] * Q.mp[r]);
       }
     }
 #pragma unroll
     for (int r = 0; r < 3; ++r) gm[r] -= Q.A[r][0] * gr[0] + Q.A[r][1] * gr[1] + Q.A[r][2] * gr[2];
   }
-  const T inv_cnt = (T)1 / (T)cnt;
+  // The chain rule into the density runs in FP32 on the forward's own hermite
+  // data, whatever T is: the ill-conditioned part -- the eigen pairs of A, the
+  // residual r and gm = gx - A gr -- is done in T; what remains is a product of
+  // well-conditioned factors.
+  float fA[3][3], fr[3], fm[3], fx[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) fA[r][k] = (float)gA[r][k];
+    fr[r] = (float)gr[r];
+    fm[r] = (float)gm[r];
+    fx[r] = (float)gx[r];
+  }
+  const float inv_cnt = 1.0f / (float)cnt;
   // per hermite pair: g_p, g_n, then into the density
   for (int e = 0; e < 12; ++e) {
     if (group_of(mask, e) != g) continue;
-    HermiteT<T> h;
-    hermite_t<T>(D, dim, x, y, z, e, PLACE == 2, h);
+    HermiteT<float> h;
+    hermite_t<float>(D, dim, x, y, z, e, PLACE == 2, h);
     const int ax = e >> 2;
-    T gp[3], gn[3] = {(T)0, (T)0, (T)0};
+    float gp[3], gn[3] = {0.0f, 0.0f, 0.0f};
     if (!use_qef) {
 #pragma unroll
-      for (int k = 0; k < 3; ++k) gp[k] = gx[k] * inv_cnt;
+      for (int k = 0; k < 3; ++k) gp[k] = fx[k] * inv_cnt;
     } else {
-      const T d = h.n[0] * h.p[0] + h.n[1] * h.p[1] + h.n[2] * h.p[2];
-      const T gd = gr[0] * h.n[0] + gr[1] * h.n[1] + gr[2] * h.n[2];
+      const float d = h.n[0] * h.p[0] + h.n[1] * h.p[1] + h.n[2] * h.p[2];
+      const float gd = fr[0] * h.n[0] + fr[1] * h.n[1] + fr[2] * h.n[2];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        gn[k] = (T)2 * (gA[k][0] * h.n[0] + gA[k][1] * h.n[1] + gA[k][2] * h.n[2]) + d * gr[k] + gd * h.p[k];
-        gp[k] = gd * h.n[k] + gm[k] * inv_cnt;
+        gn[k] = 2.0f * (fA[k][0] * h.n[0] + fA[k][1] * h.n[1] + fA[k][2] * h.n[2]) + d * fr[k] + gd * h.p[k];
+        gp[k] = gd * h.n[k] + fm[k] * inv_cnt;
       }
     }
-    T gmu = gp[ax];
+    float gmu = gp[ax];
     if (use_qef) {
-      const T nd = h.n[0] * gn[0] + h.n[1] * gn[1] + h.n[2] * gn[2];
-      T gG[3];
+      const float nd = h.n[0] * gn[0] + h.n[1] * gn[1] + h.n[2] * gn[2];
+      float gG[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         gG[k] = (gn[k] - h.n[k] * nd) * h.iglen;
@@ -622,19 +637,19 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
 #pragma unroll
         for (int end = 0; end < 2; ++end) {
           const int* q0 = end ? h.a1 : h.a0;
-          const T w = gG[a] * (end ? h.mu : (T)1 - h.mu);
+          const float w = gG[a] * (end ? h.mu : 1.0f - h.mu);
           int lo[3] = {q0[0], q0[1], q0[2]}, hi[3] = {q0[0], q0[1], q0[2]};
-          T hh = (T)0.5;
-          if (q0[a] > 0) lo[a]--; else hh = (T)1;
-          if (q0[a] < dim - 1) hi[a]++; else hh = (T)1;
-          atomicAdd(GD + ((int64_t)hi[0] * dim + hi[1]) * dim + hi[2], (float)(w * hh));
-          atomicAdd(GD + ((int64_t)lo[0] * dim + lo[1]) * dim + lo[2], (float)(-w * hh));
+          float hh = 0.5f;
+          if (q0[a] > 0) lo[a]--; else hh = 1.0f;
+          if (q0[a] < dim - 1) hi[a]++; else hh = 1.0f;
+          atomicAdd(GD + ((int64_t)hi[0] * dim + hi[1]) * dim + hi[2], w * hh);
+          atomicAdd(GD + ((int64_t)lo[0] * dim + lo[1]) * dim + lo[2], -w * hh);
         }
       }
     }
-    const T iden = (T)1 / ((h.s1 - h.s0) * (h.s1 - h.s0));
-    atomicAdd(GD + ((int64_t)h.a0[0] * dim + h.a0[1]) * dim + h.a0[2], (float)(gmu * (-h.s1 * iden)));
-    atomicAdd(GD + ((int64_t)h.a1[0] * dim + h.a1[1]) * dim + h.a1[2], (float)(gmu * (h.s0 * iden)));
+    const float iden = 1.0f / ((h.s1 - h.s0) * (h.s1 - h.s0));
+    atomicAdd(GD + ((int64_t)h.a0[0] * dim + h.a0[1]) * dim + h.a0[2], gmu * (-h.s1 * iden));
+    atomicAdd(GD + ((int64_t)h.a1[0] * dim + h.a1[1]) * dim + h.a1[2], gmu * (h.s0 * iden));
   }
 }
 
