@@ -4,7 +4,7 @@
 // FP32 rate.  Algorithms: Dekker / Knuth error-free transformations (TwoSum,
 // FastTwoSum, the product error from one fused multiply-add), as in D. H.
 // Bailey's double-double and Hida-Li-Bailey's QD library papers; division and
-// square root take one Newton correction of the float quotient / root.
+// square root refine the float quotient / root with the exact residual.
 //
 // Must be compiled with FMA available (the error-free product uses fmaf); the
 // sums use plain adds, which contraction never touches.
@@ -61,12 +61,17 @@ __device__ __forceinline__ DF operator*(DF a, DF b) {
   e = fmaf(a.lo, b.hi, e);
   return df_fast_two_sum(p, e);
 }
-__device__ __forceinline__ DF operator/(DF a, DF b) {
-  const float q1 = a.hi / b.hi;
+// Division and square root are out of line: inlined at every use they made
+// the adjoint kernel too large for the instruction cache.
+// The three partial quotients use the fast float reciprocal: each only has to
+// be within a few ulps, the residuals carry the rest.
+static __device__ __noinline__ DF operator/(DF a, DF b) {
+  const float ib = __frcp_rn(b.hi);
+  const float q1 = a.hi * ib;
   const DF r = a - b * DF(q1, 0.0f);
-  const float q2 = r.hi / b.hi;
+  const float q2 = r.hi * ib;
   const DF r2 = r - b * DF(q2, 0.0f);
-  const float q3 = r2.hi / b.hi;
+  const float q3 = r2.hi * ib;
   return df_fast_two_sum(q1, q2) + DF(q3, 0.0f);
 }
 __device__ __forceinline__ DF& operator+=(DF& a, DF b) { return a = a + b; }
@@ -82,7 +87,7 @@ __device__ __forceinline__ bool operator==(DF a, DF b) { return a.hi == b.hi && 
 __device__ __forceinline__ bool operator!=(DF a, DF b) { return !(a == b); }
 
 __device__ __forceinline__ DF fabs(DF a) { return a.hi < 0.0f ? -a : a; }
-__device__ __forceinline__ DF sqrt(DF a) {
+static __device__ __noinline__ DF sqrt(DF a) {
   if (a.hi <= 0.0f) return DF(0.0f, 0.0f);
   const float s = sqrtf(a.hi);
   const DF r = a - DF(s, 0.0f) * DF(s, 0.0f);  // exact residual of the float root
