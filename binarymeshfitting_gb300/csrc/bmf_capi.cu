@@ -72,7 +72,7 @@ struct bmf_batch {
   int* d_queue = nullptr;
   int fill_grid = 0;
   int fill_mode = 0;
-  int fill_run = 8;
+  int fill_run = 16;  // the tile height the autotuner picks on the mixed-LOD update
   // Mode R work list, sized by the output capacity (vcap + icap / 3 + 1)
   uint2* d_clist = nullptr;
   int64_t clist_cap = 0;

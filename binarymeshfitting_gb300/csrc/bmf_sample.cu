@@ -411,7 +411,7 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
                          const FieldDev& field, const float* dens_in, float* dens_out, uint32_t* words,
                          uint32_t* flags, cudaStream_t st) {
   if (field.kind == BMF_FIELD_TERRAIN_FBM && n_chunks == 1) {
-    launch_fill_terrain(8, d_chunks, nullptr, fill_terrain_items(max_dim), nullptr, 0, field, dens_out, words, flags,
+    launch_fill_terrain(16, d_chunks, nullptr, fill_terrain_items(max_dim), nullptr, 0, field, dens_out, words, flags,
                         st);
     return;
   }

@@ -273,7 +273,7 @@ def test_batch_tunings_give_identical_results(ctx):
     descs, rows = _small_batch()
     b = Batch(ctx, descs, workloads.terrain_field(), mode=L.MODE_R, iters=4, smooth_normals=True)
     bufs = b.allocate(400000, 2400000, normals=True)
-    assert b.tuning() == dict(fill_mode=2, fill_run=8, sweep_block=256)
+    assert b.tuning() == dict(fill_mode=2, fill_run=16, sweep_block=256)
     nv, ni = b.run(use_graph=True)
     ref = [bufs[k][:n].clone() for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"].clone()]
     for fm, fr, sb in [(0, 8, 256), (1, 4, 128), (1, 16, 512), (2, 4, 256), (2, 16, 128), (1, 8, 512)]:
