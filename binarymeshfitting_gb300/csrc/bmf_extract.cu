@@ -870,7 +870,6 @@ __device__ __forceinline__ int packed_mask(uint32_t nbits, int ox, int oy, int o
 // their own tiles with no block-wide barrier, so one warp's staging loads
 // overlap the others' cell work.
 constexpr int kTileWords = 8;
-constexpr int kTileSlots = 48 + 8 + 4;  // neighbour words, vertex bases, index base, 3 planes
 constexpr int kEmitWarps = 8;
 
 struct RTile {
@@ -916,26 +915,43 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
       R.iout[lane] = ch.iout;
     }
     __syncwarp();
-    // 2. stage the neighbourhoods (zeros outside the chunk)
-    for (int k = lane; k < nt * kTileSlots; k += 32) {
-      const int t = k / kTileSlots, sl = k - t * kTileSlots;
+    // 2. stage the neighbourhoods (zeros outside the chunk): one item per
+    // (word, neighbour line) loads the line's blocks zb-1..zb+1; one item per
+    // (word, owner line) its vertex bases in blocks zb, zb+1; one per word its
+    // index base and count planes
+    for (int k = lane; k < nt * 21; k += 32) {
+      const int t = k / 21, it = k - t * 21;
       const int dim = R.dim[t], zc = R.zc[t], x = R.x[t], y = R.y[t], zb = R.zb[t];
       const int64_t cw = R.cw[t];
-      const int wi = (x * dim + y) * zc + zb;
-      if (sl < 48) {
-        const int i = sl / 12, j = (sl / 3) & 3, b = sl % 3;
-        R.nb[t].w[sl] = word_at(words + cw, dim, zc, x - 1 + i, y - 1 + j, zb - 1 + b);
-      } else if (sl < 56) {
-        const int l = sl - 48;
-        const int xx = x + (l >> 2), yy = y + ((l >> 1) & 1), bb = zb + (l & 1);
-        R.nb[t].vb[l] = (xx < dim && yy < dim && bb < zc) ? __ldg(ws.vcnt + cw + (xx * dim + yy) * zc + bb) : 0u;
-      } else if (sl == 56) {
-        R.ib[t] = __ldg(ws.icnt + cw + wi);
+      if (it < 16) {
+        const int i = it >> 2, j = it & 3;
+        const int xx = x - 1 + i, yy = y - 1 + j;
+        uint32_t* dst = R.nb[t].w + (i * 4 + j) * 3;
+        if (xx < 0 || yy < 0 || xx >= dim || yy >= dim) {
+          dst[0] = dst[1] = dst[2] = 0u;
+        } else {
+          const uint32_t* L = words + cw + (xx * dim + yy) * zc + zb;
+          dst[0] = zb > 0 ? __ldg(L - 1) : 0u;
+          dst[1] = __ldg(L);
+          dst[2] = zb + 1 < zc ? __ldg(L + 1) : 0u;
+        }
+      } else if (it < 20) {
+        const int l = it - 16;
+        const int xx = x + (l >> 1), yy = y + (l & 1);
+        uint32_t* dst = R.nb[t].vb + (l >> 1) * 4 + (l & 1) * 2;
+        if (xx < dim && yy < dim) {
+          const uint32_t* V = ws.vcnt + cw + (xx * dim + yy) * zc + zb;
+          dst[0] = __ldg(V);
+          dst[1] = zb + 1 < zc ? __ldg(V + 1) : 0u;
+        } else {
+          dst[0] = dst[1] = 0u;
+        }
       } else {
-        const uint32_t v = __ldg(ws.gpl + 3 * (cw + wi) + (sl - 57));
-        if (sl == 57) R.p0[t] = v;
-        else if (sl == 58) R.p1[t] = v;
-        else R.p2[t] = v;
+        const int64_t wi = cw + (x * dim + y) * zc + zb;
+        R.ib[t] = __ldg(ws.icnt + wi);
+        R.p0[t] = __ldg(ws.gpl + 3 * wi);
+        R.p1[t] = __ldg(ws.gpl + 3 * wi + 1);
+        R.p2[t] = __ldg(ws.gpl + 3 * wi + 2);
       }
     }
     __syncwarp();
