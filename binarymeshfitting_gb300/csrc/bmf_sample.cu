@@ -256,48 +256,86 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
       // z terms of (octave o, sample k of this run)
       const int zt_o = whole ? dim : kFillRun, zt_k = whole ? z0 : 0;
       if (active) {
-      float sum[kFillRun];
+      uint32_t bits = 0u;
+      float* row = s_stage + threadIdx.x * kStageRow + (z0 & 15);
+      if (n == kFillRun) {
+        // a full run: RUN samples per octave, unrolled, no tail guards
+        float sum[kFillRun];
 #pragma unroll
-      for (int k = 0; k < kFillRun; ++k) sum[k] = 0.0f;
-      float amp = 1.0f, fr = freq;
+        for (int k = 0; k < kFillRun; ++k) sum[k] = 0.0f;
+        float amp = 1.0f, fr = freq;
 #pragma unroll 1
-      for (int o = 0; o < oct; ++o) {
-        OctLine L;
-        oct_line_init(L, px, py, fr, perm2);
-        const int si = o * kFillLines + (int)threadIdx.x;
-        if (cache && zr > 0) {  // the cell this line was in at the end of its previous run
-          const float4 ab = s_ab[si];
-          L.a0 = ab.x;
-          L.b0 = ab.y;
-          L.a1 = ab.z;
-          L.b1 = ab.w;
-          L.Zp = s_zp[si];
+        for (int o = 0; o < oct; ++o) {
+          OctLine L;
+          oct_line_init(L, px, py, fr, perm2);
+          const int si = o * kFillLines + (int)threadIdx.x;
+          if (cache && zr > 0) {  // the cell this line was in at the end of its previous run
+            const float4 ab = s_ab[si];
+            L.a0 = ab.x;
+            L.b0 = ab.y;
+            L.a1 = ab.z;
+            L.b1 = ab.w;
+            L.Zp = s_zp[si];
+          }
+          const float4* zo = zt + o * zt_o + zt_k;
+#pragma unroll
+          for (int k = 0; k < kFillRun; ++k) {
+            const float4 t = zo[k];
+            const int Z = __float_as_int(t.w);
+            if (Z != L.Zp) oct_line_cell(L, Z, gtab);  // same for every lane of the CTA
+            const float l0 = L.a0 + L.b0 * t.x;
+            const float l1 = L.a1 + L.b1 * t.y;
+            sum[k] = sum[k] + amp * (l0 + t.z * (l1 - l0));
+          }
+          if (cache) {
+            s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
+            s_zp[si] = L.Zp;
+          }
+          fr = fr * lac;
+          amp = amp * gain;
         }
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) {
-          if (k >= n) break;
-          const float4 t = zt[o * zt_o + zt_k + k];
-          const int Z = __float_as_int(t.w);
-          if (Z != L.Zp) oct_line_cell(L, Z, gtab);  // same for every lane of the CTA
-          const float l0 = L.a0 + L.b0 * t.x;
-          const float l1 = L.a1 + L.b1 * t.y;
-          sum[k] = sum[k] + amp * (l0 + t.z * (l1 - l0));
+          const float d = (py - h0) - ampl * sum[k];
+          row[k] = d;
+          if (d < 0.0f) bits |= 1u << k;
         }
-        if (cache) {
-          s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
-          s_zp[si] = L.Zp;
+      } else {
+        // the line's last, partial run: one sample at a time (same operations
+        // in the same order per sample; its cell state is not needed after it)
+#pragma unroll 1
+        for (int k = 0; k < n; ++k) {
+          float sum = 0.0f, amp = 1.0f, fr = freq;
+#pragma unroll 1
+          for (int o = 0; o < oct; ++o) {
+            OctLine L;
+            oct_line_init(L, px, py, fr, perm2);
+            const int si = o * kFillLines + (int)threadIdx.x;
+            if (cache && (zr > 0 || k > 0)) {
+              const float4 ab = s_ab[si];
+              L.a0 = ab.x;
+              L.b0 = ab.y;
+              L.a1 = ab.z;
+              L.b1 = ab.w;
+              L.Zp = s_zp[si];
+            }
+            const float4 t = zt[o * zt_o + zt_k + k];
+            const int Z = __float_as_int(t.w);
+            if (Z != L.Zp) oct_line_cell(L, Z, gtab);
+            const float l0 = L.a0 + L.b0 * t.x;
+            const float l1 = L.a1 + L.b1 * t.y;
+            sum = sum + amp * (l0 + t.z * (l1 - l0));
+            if (cache && k + 1 < n) {
+              s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
+              s_zp[si] = L.Zp;
+            }
+            fr = fr * lac;
+            amp = amp * gain;
+          }
+          const float d = (py - h0) - ampl * sum;
+          row[k] = d;
+          if (d < 0.0f) bits |= 1u << k;
         }
-        fr = fr * lac;
-        amp = amp * gain;
-      }
-      uint32_t bits = 0u;
-      float* row = s_stage + threadIdx.x * kStageRow + (z0 & 15);
-#pragma unroll
-      for (int k = 0; k < kFillRun; ++k) {
-        if (k >= n) break;
-        const float d = (py - h0) - ampl * sum[k];
-        row[k] = d;
-        if (d < 0.0f) bits |= 1u << k;
       }
       wacc |= bits << (z0 & 31);
       if (((z0 + kFillRun) & 31) == 0 || zr == nruns - 1) {
