@@ -329,6 +329,19 @@ __device__ __forceinline__ uint32_t ycross_word(const uint32_t* __restrict__ W, 
 
 __device__ __forceinline__ uint32_t lane_lt(int lane) { return (1u << lane) - 1u; }
 
+// Vertex key: where a vertex came from, as the sample (x, y, z) that owns it
+// (9 bits each: chunks have at most 512 samples per axis) and k, the crossing
+// axis (Mode R) or vertex group (Mode Q).
+__device__ __forceinline__ uint32_t vertex_key(int x, int y, int z, int k) {
+  return ((uint32_t)x << 20) | ((uint32_t)y << 11) | ((uint32_t)z << 2) | (uint32_t)k;
+}
+__device__ __forceinline__ void vertex_key_decode(uint32_t key, int& x, int& y, int& z, int& k) {
+  x = (int)(key >> 20);
+  y = (int)((key >> 11) & 511u);
+  z = (int)((key >> 2) & 511u);
+  k = (int)(key & 3u);
+}
+
 // Warp-inclusive scan of an int.
 __device__ __forceinline__ int warp_incl_scan(int v) {
   const int lane = threadIdx.x & 31;

@@ -542,7 +542,7 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
             out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
                                 x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
           if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
-          if (out.vkey) out.vkey[gv] = ((uint32_t)(((int64_t)x * dim + y) * dim + z) << 2) | (uint32_t)a;
+          if (out.vkey) out.vkey[gv] = vertex_key(x, y, z, a);
           if (out.valence) {
             // init_valence: uses of this edge by the (up to) four interior
             // cells around it (polygonize skips far-face cells, DMCChunk.cpp:528).
@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
           }
           if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
           if (out.boundary) out.boundary[gv] = bnd;
-          if (out.vkey) out.vkey[gv] = ((uint32_t)(((int64_t)x * dim + y) * dim + z) << 2) | (uint32_t)g;
+          if (out.vkey) out.vkey[gv] = vertex_key(x, y, z, g);
           if (out.valence) {
             int val = 0;
             for (int e = 0; e < 12; ++e) {
@@ -736,9 +736,11 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
   const uint32_t* W = words + ch.words;
   const uint32_t* ibase = ws.icnt + ch.words;
   const uint32_t* pl = ws.gpl + 3 * ch.words;
-  const uint32_t key = vkey[v];
-  const int lin = (int)(key >> 2), k = (int)(key & 3u);
-  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+  int x, y, z, k;
+  vertex_key_decode(vkey[v], x, y, z, k);
+  // the chunk's first primitive (its index offset and word bases are
+  // multiples of the primitive size)
+  const int64_t pbase = iout / (MODE == 0 ? 3 : 4);
   uint32_t* out = adj + off[v];
   // the vertex's CSR range (the exclusive scan of init_valence): never write past it
   const int room = (int)(off[v + 1] - off[v]);
@@ -775,7 +777,7 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
       const uint32_t lt = lane_lt(cz & 31);
       const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
                            4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
-      const int64_t first = (iout + (int64_t)__ldg(ibase + wi)) / 3 + pre;
+      const int64_t first = pbase + __ldg(ibase + wi) / 3u + pre;
       for (int t = 0; t < nt; ++t)
         if ((tri_edge(tw, 3 * t) == e || tri_edge(tw, 3 * t + 1) == e || tri_edge(tw, 3 * t + 2) == e) && n < room)
           out[n++] = (uint32_t)(first + t);
@@ -798,7 +800,7 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
       if (a >= 1) pre += (Xi >> l) & 1u;
       if (a >= 2) pre += (Yi >> l) & 1u;
       const int wi = (sx * dim + sy) * zc + (sz >> 5);
-      uint32_t id = (uint32_t)((iout + (int64_t)__ldg(ibase + wi)) / 4 + pre);
+      uint32_t id = (uint32_t)(pbase + __ldg(ibase + wi) / 4u + pre);
       int j = n++;  // insertion into the sorted prefix
       while (j > 0 && ids[j - 1] > id) { ids[j] = ids[j - 1]; --j; }
       ids[j] = id;
@@ -1015,7 +1017,6 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
       if (own) {
         const float* D = dens + R.dens[t];
         uint32_t vid = nb.vb[0] + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
-        const uint32_t lin = (uint32_t)(((int64_t)x * dim + y) * dim + z);
         for (int a = 0; a < 3; ++a) {
           if (!((own >> a) & 1u)) continue;
           const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
@@ -1036,7 +1037,7 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
             out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
                                 x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
           if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
-          if (out.vkey) out.vkey[gv] = (lin << 2) | (uint32_t)a;
+          if (out.vkey) out.vkey[gv] = vertex_key(x, y, z, a);
           if (out.valence) {
             // init_valence: uses of this edge by the (up to) four interior
             // cells around it (polygonize skips far-face cells, DMCChunk.cpp:528)
@@ -1127,7 +1128,7 @@ __global__ void __launch_bounds__(256, 3) k_emit_cells_q(const ChunkDev* __restr
         }
         if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
         if (out.boundary) out.boundary[gv] = bnd;
-        if (out.vkey) out.vkey[gv] = ((uint32_t)lin << 2) | (uint32_t)g;
+        if (out.vkey) out.vkey[gv] = vertex_key(x, y, z, g);
         if (out.valence) {
           int val = 0;
           for (int e = 0; e < 12; ++e) {
@@ -1192,9 +1193,8 @@ __global__ void __launch_bounds__(128) k_place_qef(const ChunkDev* __restrict__ 
   const int c = find_chunk_by_vertex(chunks, n_chunks, v);
   const ChunkDev ch = chunks[c];
   const int dim = ch.dim;
-  const uint32_t key = vkey[v];
-  const int lin = (int)(key >> 2), g = (int)(key & 3u);
-  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+  int x, y, z, g;
+  vertex_key_decode(vkey[v], x, y, z, g);
   const int mask = cell_mask_at(words + ch.words, dim, ch.zc, x, y, z);
   float P[3];
   q_place<2>(dens + ch.dens, dim, x, y, z, mask, g, P);

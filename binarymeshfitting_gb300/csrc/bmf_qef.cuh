@@ -441,9 +441,8 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
   const uint32_t* W = words + ch.words;
   const float* D = dens + ch.dens;
   float* GD = grad_dens + ch.dens;
-  const uint32_t key = vkey[v];
-  const int lin = (int)(key >> 2), g = (int)(key & 3u);
-  const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+  int x, y, z, g;
+  vertex_key_decode(vkey[v], x, y, z, g);
   const int mask = cell_mask_at(W, dim, zc, x, y, z);
   const T gx[3] = {(T)grad_pos[3 * v], (T)grad_pos[3 * v + 1], (T)grad_pos[3 * v + 2]};
   // the forward's branch: replay of q_place in FP32
