@@ -38,9 +38,11 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
   const int x = u - __ldg(unit_start + c);
   const int dim = ch.dim, zc = ch.zc;
   const int nw = dim * zc;
-  for (int i = threadIdx.x; i < 512; i += blockDim.x) {
-    perm2[i] = field.perm[i & 255];
-    gtab[i] = seg_grad_code(field.perm[i & 255]);
+  if (field.kind == BMF_FIELD_TERRAIN_FBM) {  // the noise tables; no other field reads them
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+      perm2[i] = field.perm[i & 255];
+      gtab[i] = seg_grad_code(field.perm[i & 255]);
+    }
   }
   for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = 0u;
   __syncthreads();

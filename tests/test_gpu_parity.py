@@ -84,10 +84,12 @@ def test_field_fill_bit_exact(ctx, kind, params, dim, origin, scale):
     assert_float_exact(g, o, "density")
 
 
-@pytest.mark.parametrize("dim", [2, 3, 17, 32, 129])
-@pytest.mark.parametrize("octaves", [0, 1, 5, 7])
+@pytest.mark.parametrize("dim", [2, 3, 17, 30, 32, 47, 129])
+@pytest.mark.parametrize("octaves", [0, 1, 5, 7, 9])
 def test_terrain_fill_line_kernel_sizes(ctx, dim, octaves):
-    """The line-mapped terrain kernel: ragged runs, word ends, octave counts."""
+    """The line-mapped terrain kernel: ragged runs (partial last runs of 1 to
+    15 samples), word ends, octave counts with and without the cell-state cache
+    (more than 8 octaves rebuild it every run)."""
     params = list(workloads.TERRAIN_PARAMS)
     params[5] = octaves
     desc = L.ChunkDesc.make((37.0, -20.0, 1000.25), 2.0, dim)
