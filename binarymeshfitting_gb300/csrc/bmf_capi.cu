@@ -955,7 +955,8 @@ struct bmf_fit {
   uint32_t *d_idxg = nullptr, *d_vkey = nullptr;
   uint8_t *d_valence = nullptr, *d_boundary = nullptr;
   float* d_g = nullptr;           // position-gradient work buffer
-  uint32_t* d_qlist = nullptr;    // QEF-placed vertices of the FP64 backward (+ counter at [vcap])
+  uint32_t* d_qlist = nullptr;    // QEF-placed vertices of the wide backward (+ counter at [vcap])
+  float* d_qseed = nullptr;       // their FP32 eigenvectors from the first backward pass (9 per entry)
   uint2* d_clist = nullptr;       // work list of active cells (+ counter after it)
   const float* last_density = nullptr;
   int64_t* h_pinned = nullptr;
@@ -967,7 +968,7 @@ bmf_status bmf_fit_destroy(bmf_fit* f) {
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   void* ptrs[] = {f->d_chunks, f->d_units, f->d_flags, f->d_tot, f->d_words, f->d_totals, f->ws.vcnt, f->ws.icnt,
                   f->ws.gpl, f->ps.off, f->ps.cursor, f->ps.adj, f->ps.dual_p, f->ps.dual_n, f->ps.tmp, f->d_idxg,
-                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist, f->d_clist};
+                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist, f->d_qseed, f->d_clist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (f->h_pinned) cudaFreeHost(f->h_pinned);
@@ -1027,6 +1028,8 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
             cudaMalloc(&f->d_valence, vcap + 1) == cudaSuccess && cudaMalloc(&f->d_boundary, vcap + 1) == cudaSuccess &&
             cudaMalloc(&f->d_g, sizeof(float) * 3 * (vcap + 1)) == cudaSuccess &&
             cudaMalloc(&f->d_qlist, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
+            (!(flags & (BMF_FIT_ADJOINT_F64 | BMF_FIT_ADJOINT_DF)) ||
+             cudaMalloc(&f->d_qseed, sizeof(float) * 9 * (vcap + 1)) == cudaSuccess) &&
             cudaMalloc(&f->d_clist, sizeof(uint2) * (vcap + icap / 4 + 2)) == cudaSuccess &&
             cudaMallocHost(&f->h_pinned, sizeof(int64_t) * 4) == cudaSuccess &&
             cudaMemcpy(f->d_chunks, hc.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -1093,7 +1096,7 @@ bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_
   BMF_CUDA(ctx, cudaMemsetAsync(d_grad_density, 0, sizeof(float) * (size_t)f->n * f->dim * f->dim * f->dim, st));
   const int wide = (f->flags & BMF_FIT_ADJOINT_F64) ? 1 : ((f->flags & BMF_FIT_ADJOINT_DF) ? 2 : 0);
   launch_place_bwd(f->placement, wide, f->d_chunks, f->n, f->d_words, f->last_density, f->d_vkey, f->d_totals,
-                   f->vcap, f->d_g, d_grad_density, f->d_qlist, f->d_qlist + f->vcap, st);
+                   f->vcap, f->d_g, d_grad_density, f->d_qlist, f->d_qlist + f->vcap, f->d_qseed, st);
   BMF_LAUNCHED(ctx, k + (wide && f->placement == BMF_PLACE_QEF ? 2 : 1));
   return BMF_OK;
 }

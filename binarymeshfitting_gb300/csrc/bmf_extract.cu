@@ -662,20 +662,21 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
 
 void launch_place_bwd(int placement, int wide, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
-                      const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount, cudaStream_t st) {
+                      const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount, float* qseed,
+                      cudaStream_t st) {
   const int blocks = (int)((vcap + 127) / 128);
   if (blocks == 0) return;
 #define BMF_PLACE_BWD(P, T, L)                                                                                     \
   k_place_bwd<P, T, L><<<blocks, 128, 0, st>>>(d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos, \
-                                               grad_dens, qlist, qcount)
-  if (placement == 2 && wide && qlist && qcount) {
+                                               grad_dens, qlist, qcount, qseed)
+  if (placement == 2 && wide && qlist && qcount && qseed) {
     // float pass for the mass-point vertices, then the wide QEF adjoint over
     // the compacted list of QEF-placed ones (no idle lanes in the wide code;
     // its own translation unit, compiled with FMA contraction)
     cudaMemsetAsync(qcount, 0, sizeof(uint32_t), st);
     BMF_PLACE_BWD(2, float, 1);
     launch_place_bwd_wide_list(wide, d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos, grad_dens,
-                               qlist, qcount, st);
+                               qlist, qcount, qseed, st);
   } else if (placement == 2) {
     if (wide) BMF_PLACE_BWD(2, double, 0); else BMF_PLACE_BWD(2, float, 0);
   } else {

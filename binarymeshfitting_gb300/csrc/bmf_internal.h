@@ -137,13 +137,14 @@ int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_coun
 void launch_place_bwd_wide_list(int wide, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                                 const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
                                 const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount,
-                                cudaStream_t st);
-// qlist (vcap entries) + qcount: scratch of the two-pass wide form (nullable:
-// one pass, idle lanes in the wide code).  wide: 0 FP32 adjoint, 1 the QEF
+                                float* qseed, cudaStream_t st);
+// qlist (vcap entries) + qcount + qseed (9 floats per entry: the first pass's
+// FP32 eigenvectors of the listed vertex): scratch of the two-pass wide form
+// (nullable: one pass, idle lanes in the wide code).  wide: 0 FP32 adjoint, 1 the QEF
 // derivative from an FP64 re-solve, 2 from a double-float re-solve.
 void launch_place_bwd(int placement, int wide, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
-                      const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount,
+                      const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount, float* qseed,
                       cudaStream_t st);
 void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n, const int64_t* d_n,
                                      uint32_t* block_tmp, cudaStream_t st);

@@ -428,8 +428,10 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
                                                    const uint32_t* __restrict__ vkey,
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
                                                    const float* __restrict__ grad_pos, float* __restrict__ grad_dens,
-                                                   uint32_t* __restrict__ qlist, uint32_t* __restrict__ qcount) {
+                                                   uint32_t* __restrict__ qlist, uint32_t* __restrict__ qcount,
+                                                   float* __restrict__ qseed) {
   int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t slot = v;  // LIST == 2: the list entry
   if (LIST == 2) {
     if (v >= (int64_t)*qcount) return;
     v = qlist[v];
@@ -445,33 +447,52 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
   vertex_key_decode(vkey[v], x, y, z, g);
   const int mask = cell_mask_at(W, dim, zc, x, y, z);
   const T gx[3] = {(T)grad_pos[3 * v], (T)grad_pos[3 * v + 1], (T)grad_pos[3 * v + 2]};
-  // the forward's branch: replay of q_place in FP32
   int cnt = 0;
-  QefAccum q;
-  if (PLACE == 2) q.init();
-  for (int e = 0; e < 12; ++e) {
-    if (group_of(mask, e) != g) continue;
-    float p[3], n[3];
-    hermite(D, dim, x, y, z, e, PLACE == 2, p, n);
-    ++cnt;
-    if (PLACE == 2) q.add(p, n);
-  }
-  if (cnt == 0) return;
   bool use_qef = false;
   QefAdj<T> Q;
-  if (PLACE == 2) {
-    float s[3];
-    QefSolveInfo info;
-    if (q.solve(s, &info))
-      use_qef = s[0] >= (float)x && s[0] <= (float)(x + 1) && s[1] >= (float)y && s[1] <= (float)(y + 1) &&
-                s[2] >= (float)z && s[2] <= (float)(z + 1);
-    if (LIST == 1 && use_qef) {
-      qlist[atomicAdd(qcount, 1u)] = (uint32_t)v;
-      return;
+  QefAccum q;
+  QefSolveInfo info;
+  if constexpr (LIST == 2) {
+    // a listed vertex is QEF-placed (the first pass's exact FP32 replay
+    // decided it) and its FP32 eigenvectors, which seed the wide re-solve, were
+    // kept by that pass
+    for (int e = 0; e < 12; ++e) cnt += group_of(mask, e) == g;
+    if (cnt == 0) return;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) info.V[r][k] = qseed[9 * slot + 3 * r + k];
     }
-    // listed vertices are QEF-placed (the exact FP32 replay of the first pass
-    // decided it); here the replay only seeds the FP64 eigenvectors
-    if (LIST == 2) use_qef = true;
+    use_qef = true;
+  } else {
+    // the forward's branch: replay of q_place in FP32
+    if (PLACE == 2) q.init();
+    for (int e = 0; e < 12; ++e) {
+      if (group_of(mask, e) != g) continue;
+      float p[3], n[3];
+      hermite(D, dim, x, y, z, e, PLACE == 2, p, n);
+      ++cnt;
+      if (PLACE == 2) q.add(p, n);
+    }
+    if (cnt == 0) return;
+    if (PLACE == 2) {
+      float s[3];
+      if (q.solve(s, &info))
+        use_qef = s[0] >= (float)x && s[0] <= (float)(x + 1) && s[1] >= (float)y && s[1] <= (float)(y + 1) &&
+                  s[2] >= (float)z && s[2] <= (float)(z + 1);
+      if (LIST == 1 && use_qef) {
+        const uint32_t k = atomicAdd(qcount, 1u);
+        qlist[k] = (uint32_t)v;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+#pragma unroll
+          for (int c3 = 0; c3 < 3; ++c3) qseed[9 * (int64_t)k + 3 * r + c3] = info.V[r][c3];
+        }
+        return;
+      }
+    }
+  }
+  if (PLACE == 2) {
     if (use_qef) {
       if constexpr (sizeof(T) == sizeof(float)) {
 #pragma unroll
