@@ -300,11 +300,35 @@ __device__ __forceinline__ int inside_at(const uint32_t* __restrict__ W, int dim
   if (z < 0 || z >= dim) return 0;
   return (int)((word_at(W, dim, zc, x, y, z >> 5) >> (z & 31)) & 1u);
 }
-// Reference cell mask (DMCChunk.cpp:202-438): corners outside the chunk are 0.
+// Inside bits of samples z and z + 1 of one line L (bit 0: z); 0 for samples
+// outside [0, dim).
+__device__ __forceinline__ uint32_t line_bits2(const uint32_t* __restrict__ L, int dim, int z) {
+  if (z >= dim) return 0u;
+  uint32_t r;
+  if (z >= 0 && (z & 31) != 31) {
+    r = (__ldg(L + (z >> 5)) >> (z & 31)) & 3u;
+  } else {  // z and z + 1 straddle two words (or z == -1)
+    r = 0u;
+    if (z >= 0 && z < dim) r = (__ldg(L + (z >> 5)) >> 31) & 1u;
+    if (z + 1 >= 0 && z + 1 < dim) r |= (__ldg(L + ((z + 1) >> 5)) & 1u) << 1;
+  }
+  if (z + 1 >= dim) r &= 1u;
+  return r;
+}
+
+// Reference cell mask (DMCChunk.cpp:202-438): bit 4dx + 2dy + dz is corner
+// (x+dx, y+dy, z+dz); corners outside the chunk are 0.  Two bits per line.
 __device__ __forceinline__ int cell_mask_at(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int z) {
   int m = 0;
 #pragma unroll
-  for (int c = 0; c < 8; ++c) m |= inside_at(W, dim, zc, x + ((c >> 2) & 1), y + ((c >> 1) & 1), z + (c & 1)) << c;
+  for (int i = 0; i < 2; ++i) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int xx = x + i, yy = y + j;
+      if (xx < 0 || yy < 0 || xx >= dim || yy >= dim) continue;
+      m |= (int)line_bits2(W + (xx * dim + yy) * zc, dim, z) << (4 * i + 2 * j);
+    }
+  }
   return m;
 }
 
