@@ -263,9 +263,10 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
           if (slot < ws.clist_cap) ws.clist[slot] = make_uint2((uint32_t)c, (uint32_t)(x * nw + wi));
         } else {
           const int y = wi / zc, zb = wi - y * zc;
-          const uint32_t lin0 = (uint32_t)((((int64_t)x * dim + y) * dim) + 32 * zb);
+          const uint32_t key0 = vertex_key(x, y, 32 * zb, 0);  // the cell as a vertex key (k = 0)
           for (uint32_t m = act; m; m &= m - 1u, ++slot)
-            if (slot < ws.clist_cap) ws.clist[slot] = make_uint2((uint32_t)c, lin0 + (uint32_t)(__ffs(m) - 1));
+            if (slot < ws.clist_cap)
+              ws.clist[slot] = make_uint2((uint32_t)c, key0 + ((uint32_t)(__ffs(m) - 1) << 2));
         }
       }
     }
@@ -1099,8 +1100,8 @@ __global__ void __launch_bounds__(256, 3) k_emit_cells_q(const ChunkDev* __restr
     const uint2 ent = ws.clist[i];
     const ChunkDev ch = chunks[ent.x];
     const int dim = ch.dim, zc = ch.zc;
-    const int lin = (int)ent.y;
-    const int z = lin % dim, y = (lin / dim) % dim, x = lin / (dim * dim);
+    int x, y, z, k0;
+    vertex_key_decode(ent.y, x, y, z, k0);
     const int zb = z >> 5, lane = z & 31;
     const uint32_t lt = lane_lt(lane);
     const uint32_t* W = words + ch.words;

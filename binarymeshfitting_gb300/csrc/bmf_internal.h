@@ -35,7 +35,7 @@ struct WordScratch {
   // count kernel) entries, at most clist_cap kept.  Mode R: every busy word
   // (one whose cells own a crossing or emit triangles) as {chunk, word index
   // in the chunk}; Mode Q: every cell that holds vertex groups or owns an
-  // interior crossing, as {chunk, (x*dim + y)*dim + z}.  Either way its size
+  // interior crossing, as {chunk, vertex_key(x, y, z, 0)}.  Either way its size
   // bound is vcap + icap / prim_size + 1.
   uint2* clist;
   uint32_t* ccount;

@@ -198,3 +198,12 @@ def test_batched_fit_spheres_fp64_spot_check(ctx):
             print("chunk %d: rel_l2 %.3g, entries within tol %.5f, samples kept %.4f" % (k, rel_l2, ok, kept))
             assert rel_l2 <= 2e-4 and ok >= 0.999, k
     assert abs(float(loss) - loss64) <= 1e-4 * abs(loss64), (float(loss), loss64)
+
+
+def test_fit_create_rejects_two_wide_adjoints(ctx):
+    """BMF_FIT_ADJOINT_F64 and BMF_FIT_ADJOINT_DF are exclusive."""
+    import ctypes
+    h = ctypes.c_void_p()
+    st = ctx.lib.bmf_fit_create(ctx.h, 1, DIM, L.PLACE_QEF, ITERS, 100000, 400000,
+                                L.FIT_ADJOINT_F64 | L.FIT_ADJOINT_DF, ctypes.byref(h))
+    assert st == L.ERR_INVALID_ARGUMENT and not h.value

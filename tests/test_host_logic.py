@@ -38,3 +38,25 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.Mesh) == 80
     assert ctypes.sizeof(_lib.BatchOut) == 72
     assert ctypes.sizeof(_lib.BatchTuning) == 32
+
+
+def test_fill_fp32_op_count():
+    """The bench's algorithmic FP32 count of the line-separable FBM: per sample
+    9 per octave + 2, plus per-line and per-layer set-up terms; on the
+    mixed-LOD update about 68 per sample, and a single 1-octave chunk inside one
+    z-lattice cell matches the closed form exactly."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), ".."))
+    import bench
+    _, rows = workloads.lod_update()
+    ops = bench.fill_fp32_ops(rows, workloads.TERRAIN_PARAMS)
+    per_sample = ops / (rows[:, 4] ** 3).sum()
+    assert 60.0 < per_sample < 75.0, per_sample
+    # one 33^3 chunk, one octave at a frequency that keeps every line in one cell
+    params = (64.0, 40.0, 1e-4, 2.0, 0.5, 1, 1337)
+    one = np.array([[0.0, 0.0, 0.0, 1.0, 33, 0]])
+    dim = 33
+    want = (dim ** 3 * (bench.OPS_PER_SAMPLE_OCTAVE + bench.OPS_PER_SAMPLE)
+            + dim ** 2 * (bench.OPS_PER_LINE_OCTAVE + bench.OPS_PER_LINE) + dim ** 2 * 2 * bench.OPS_PER_LAYER)
+    assert bench.fill_fp32_ops(one, params) == want
