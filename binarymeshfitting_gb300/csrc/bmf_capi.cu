@@ -20,6 +20,10 @@ enum Slot {
 };
 
 constexpr int kMaxDim = 512;
+// below this many chunks the sweeps run as whole-mesh kernels: one CTA per
+// chunk needs several chunks per resident CTA (~450 on a GB300) to balance
+// (measured: 4096 mixed chunks gain 3 %, 512 equal chunks lose 3 %)
+constexpr int kChunkSweepMinChunks = 2048;
 
 struct DevBuf {
   void* p = nullptr;
@@ -70,6 +74,9 @@ struct bmf_batch {
   int2* d_fill_items = nullptr;
   int n_fill_items = 0;
   int* d_queue = nullptr;
+  // the chunk-by-chunk sweeps: chunk indices by size, largest first, and their queue
+  int* d_order = nullptr;
+  int* d_pqueue = nullptr;
   int fill_grid = 0;
   int fill_mode = 0;
   int fill_run = 16;  // the tile height the autotuner picks on the mixed-LOD update
@@ -554,12 +561,19 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
   if ((s = bail(cudaMemcpy(b->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice),
                 "upload units")) != BMF_OK)
     return s;
+  // chunks by size, largest first (longest-processing-time order for the
+  // work queues of the fill and of the chunk-by-chunk sweeps)
+  std::vector<int> order(n_chunks);
+  for (int i = 0; i < n_chunks; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int c) { return b->h_chunks[a].dim > b->h_chunks[c].dim; });
+  if ((s = bail(cudaMalloc(&b->d_order, sizeof(int) * n_chunks), "chunk order")) != BMF_OK) return s;
+  if ((s = bail(cudaMalloc(&b->d_pqueue, sizeof(int)), "sweep queue")) != BMF_OK) return s;
+  if ((s = bail(cudaMemcpy(b->d_order, order.data(), sizeof(int) * n_chunks, cudaMemcpyHostToDevice),
+                "upload chunk order")) != BMF_OK)
+    return s;
   if (b->field.kind == BMF_FIELD_TERRAIN_FBM) {
-    // line items, largest chunks first (longest-processing-time order for the queue)
-    std::vector<int> order(n_chunks);
-    for (int i = 0; i < n_chunks; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int c) { return b->h_chunks[a].dim > b->h_chunks[c].dim; });
+    // line items in that order
     std::vector<int2> items;
     for (int i : order) {
       const int n_it = fill_terrain_items(b->h_chunks[i].dim);
@@ -637,6 +651,18 @@ bmf_status batch_proc_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   return BMF_OK;
 }
 
+// The structured adjacency of a batch; with enough chunks to fill the GPU
+// the sweeps run chunk by chunk (one CTA per chunk, largest chunks first).
+StructuredAdj batch_adj(const bmf_batch* b) {
+  StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
+  if (b->n >= kChunkSweepMinChunks) {
+    sa.tot = b->d_tot;
+    sa.order = b->d_order;
+    sa.queue = b->d_pqueue;
+  }
+  return sa;
+}
+
 // Enqueues one whole update on st (captured into the graph, or run directly).
 bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st, int64_t* kernels) {
   bmf_ctx* ctx = b->ctx;
@@ -653,7 +679,7 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
                               b->d_words, b->d_dens, b->d_flags, b->ws, mo, b->d_totals, st);
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
-    const StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
+    const StructuredAdj sa = batch_adj(b);
     k += launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary,
                         b->d_valence, b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals,
                         b->ps, &sa, st);
@@ -779,7 +805,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   int pk = 0;
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
-    const StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
+    const StructuredAdj sa = batch_adj(b);
     pk = launch_process(N, out->vcap, out->icap / N, b->d_totals, out->d_pos, out->d_nrm, b->d_boundary,
                         b->d_valence, b->d_idxg, b->opts.iters, b->opts.process_boundary, b->opts.smooth_normals,
                         b->ps, &sa, st);
@@ -906,7 +932,7 @@ bmf_status bmf_batch_autotune(bmf_batch* b, bmf_batch_out* out, int32_t reps, vo
   if (b->opts.iters > 0) {
     if ((s = bmf_batch_run(b, out, 0, 1, stream)) != BMF_OK) return s;
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
-    const StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
+    const StructuredAdj sa = batch_adj(b);
     const int blocks[3] = {128, 256, 512};
     float best_ms = 1e30f;
     for (int bs : blocks) {
@@ -955,6 +981,8 @@ struct bmf_fit {
   uint32_t *d_idxg = nullptr, *d_vkey = nullptr;
   uint8_t *d_valence = nullptr, *d_boundary = nullptr;
   float* d_g = nullptr;           // position-gradient work buffer
+  int* d_order = nullptr;         // chunk order of the chunk-by-chunk sweeps (identity) and its queue
+  int* d_pqueue = nullptr;
   uint32_t* d_qlist = nullptr;    // QEF-placed vertices of the wide backward (+ counter at [vcap])
   float* d_qseed = nullptr;       // their FP32 eigenvectors from the first backward pass (9 per entry)
   uint2* d_clist = nullptr;       // work list of active cells (+ counter after it)
@@ -968,7 +996,8 @@ bmf_status bmf_fit_destroy(bmf_fit* f) {
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   void* ptrs[] = {f->d_chunks, f->d_units, f->d_flags, f->d_tot, f->d_words, f->d_totals, f->ws.vcnt, f->ws.icnt,
                   f->ws.gpl, f->ps.off, f->ps.cursor, f->ps.adj, f->ps.dual_p, f->ps.dual_n, f->ps.tmp, f->d_idxg,
-                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist, f->d_qseed, f->d_clist};
+                  f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist, f->d_qseed, f->d_clist, f->d_order,
+                  f->d_pqueue};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (f->h_pinned) cudaFreeHost(f->h_pinned);
@@ -1028,12 +1057,19 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
             cudaMalloc(&f->d_valence, vcap + 1) == cudaSuccess && cudaMalloc(&f->d_boundary, vcap + 1) == cudaSuccess &&
             cudaMalloc(&f->d_g, sizeof(float) * 3 * (vcap + 1)) == cudaSuccess &&
             cudaMalloc(&f->d_qlist, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
+            cudaMalloc(&f->d_order, sizeof(int) * n_chunks) == cudaSuccess &&
+            cudaMalloc(&f->d_pqueue, sizeof(int)) == cudaSuccess &&
             (!(flags & (BMF_FIT_ADJOINT_F64 | BMF_FIT_ADJOINT_DF)) ||
              cudaMalloc(&f->d_qseed, sizeof(float) * 9 * (vcap + 1)) == cudaSuccess) &&
             cudaMalloc(&f->d_clist, sizeof(uint2) * (vcap + icap / 4 + 2)) == cudaSuccess &&
             cudaMallocHost(&f->h_pinned, sizeof(int64_t) * 4) == cudaSuccess &&
             cudaMemcpy(f->d_chunks, hc.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(f->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok) {  // every chunk has the same size: the sweep queue takes them in index order
+    std::vector<int> order(n_chunks);
+    for (int i = 0; i < n_chunks; ++i) order[i] = i;
+    ok = cudaMemcpy(f->d_order, order.data(), sizeof(int) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess;
+  }
   if (!ok) {
     bmf_fit_destroy(f);
     return fail(ctx, BMF_ERR_OUT_OF_MEMORY, "bmf_fit_create: device allocation failed");
@@ -1063,7 +1099,12 @@ bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uin
   int k = 4 + launch_emit(BMF_MODE_Q, f->placement, f->d_chunks, f->n, f->d_units, f->n * f->dim, f->d_words,
                           d_density, f->d_flags, f->ws, mo, f->d_totals, st);
   if (f->iters > 0) {
-    const StructuredAdj sa{BMF_MODE_Q, f->d_chunks, f->n, f->d_words, f->ws, f->d_vkey};
+    StructuredAdj sa{BMF_MODE_Q, f->d_chunks, f->n, f->d_words, f->ws, f->d_vkey};
+    if (f->n >= kChunkSweepMinChunks) {
+      sa.tot = f->d_tot;
+      sa.order = f->d_order;
+      sa.queue = f->d_pqueue;
+    }
     k += launch_process(4, f->vcap, f->icap / 4, f->d_totals, d_pos, nullptr, f->d_boundary, f->d_valence, f->d_idxg,
                         f->iters, 0, 0, f->ps, &sa, st);
   }
@@ -1107,7 +1148,7 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
                   b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
                   b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey,
-                  b->d_fill_items, b->d_queue, b->d_clist};
+                  b->d_fill_items, b->d_queue, b->d_order, b->d_pqueue, b->d_clist};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);

@@ -29,7 +29,6 @@ static __device__ uint64_t g_tri_cases[256] = BMF_TRI_CASES_INIT;
 static __device__ uint64_t g_group_cases[256] = BMF_GROUP_CASES_INIT;
 static __device__ uint64_t g_edge_uses[256] = BMF_EDGE_USES_INIT;
 
-__device__ __forceinline__ int tri_count(int mask) { return (int)(c_tri_cases[mask] >> 60); }
 __device__ __forceinline__ int tri_edge(uint64_t w, int i) { return (int)((w >> (4 * i)) & 0xF); }
 __device__ __forceinline__ int group_count(int mask) { return (int)((c_group_cases[mask] >> 48) & 0xF); }
 __device__ __forceinline__ int group_of(int mask, int e) { return (int)((c_group_cases[mask] >> (4 * e)) & 0xF); }
@@ -294,11 +293,6 @@ __device__ __forceinline__ float eval_field(const FieldDev& f, const int* __rest
 __device__ __forceinline__ uint32_t word_at(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int zb) {
   if (x < 0 || y < 0 || x >= dim || y >= dim || zb < 0 || zb >= zc) return 0u;
   return __ldg(W + ((int64_t)x * dim + y) * zc + zb);
-}
-// Inside bit of sample (x, y, z); 0 outside the chunk.
-__device__ __forceinline__ int inside_at(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int z) {
-  if (z < 0 || z >= dim) return 0;
-  return (int)((word_at(W, dim, zc, x, y, z >> 5) >> (z & 31)) & 1u);
 }
 // Inside bits of samples z and z + 1 of one line L (bit 0: z); 0 for samples
 // outside [0, dim).

@@ -103,6 +103,11 @@ struct StructuredAdj {
   const uint32_t* words;
   WordScratch ws;            // scanned counts + per-word bit-planes
   const uint32_t* vkey;      // per-vertex keys written by the emit kernel
+  // optional (all three or none): the sweeps run chunk by chunk, one CTA per
+  // chunk, taking chunks from queue in the given order
+  const uint32_t* tot = nullptr;  // per chunk {vertices, indices}
+  const int* order = nullptr;     // chunk indices, largest first
+  int* queue = nullptr;           // one int, reset by launch_process
 };
 void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
                       const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,

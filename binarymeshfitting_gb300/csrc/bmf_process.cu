@@ -147,13 +147,12 @@ __device__ __forceinline__ void cross3(const float a[3], const float b[3], float
 
 // optimize_dual_grid body (MeshProcessor.cpp:142-227).  normal_mode: 0 none,
 // 1 face normal, 2 sum of vertex normals.
+constexpr int kChunkSweepThreads = 512;
+
 template <int N>
-__global__ void k_dual(int64_t n_prims, int64_t nv, const int64_t* __restrict__ d_counts,
-                       const uint32_t* __restrict__ idx, const float* __restrict__ pos, const float* __restrict__ nrm,
-                       float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (d_counts ? min(n_prims, d_counts[1] / N) : n_prims)) return;
-  const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
+__device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t* __restrict__ idx,
+                                          const float* __restrict__ pos, const float* __restrict__ nrm,
+                                          float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
   uint32_t v[N];
 #pragma unroll
   for (int k = 0; k < N; ++k) {
@@ -226,15 +225,23 @@ __global__ void k_dual(int64_t n_prims, int64_t nv, const int64_t* __restrict__ 
   for (int c = 0; c < 3; ++c) dual_n[3 * t + c] = o[c];
 }
 
+template <int N>
+__global__ void k_dual(int64_t n_prims, int64_t nv, const int64_t* __restrict__ d_counts,
+                       const uint32_t* __restrict__ idx, const float* __restrict__ pos, const float* __restrict__ nrm,
+                       float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (d_counts ? min(n_prims, d_counts[1] / N) : n_prims)) return;
+  dual_prim<N>(t, d_counts ? min(nv, d_counts[0]) : nv, idx, pos, nrm, dual_p, dual_n, normal_mode);
+}
+
 // optimize_primal_grid (MeshProcessor.cpp:238-306).
-__global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int64_t* __restrict__ d_counts,
-                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
-                         const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
-                         const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
-                         const float* __restrict__ dual_n, float* __restrict__ pos, float* __restrict__ nrm,
-                         int process_boundary, int smooth_normals, int set_colors) {
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
+__device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t adj_cap,
+                                              const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
+                                              const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
+                                              const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
+                                              const float* __restrict__ dual_n, float* __restrict__ pos,
+                                              float* __restrict__ nrm, int process_boundary, int smooth_normals,
+                                              int set_colors) {
   // list length: adj_next (MeshProcessor.cpp:247); with a prebuilt adjacency it equals init_valence
   const int64_t room = adj_cap - (int64_t)off[v];
   const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)(cursor ? min(cursor[v], (uint32_t)valence[v])
@@ -269,6 +276,60 @@ __global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int6
   if (nrm && nn[1] != 0.0f) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) nrm[3 * v + c] = nn[c];
+  }
+}
+
+__global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int64_t* __restrict__ d_counts,
+                         const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
+                         const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
+                         const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
+                         const float* __restrict__ dual_n, float* __restrict__ pos, float* __restrict__ nrm,
+                         int process_boundary, int smooth_normals, int set_colors) {
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
+  primal_vertex(v, np_lim, adj_cap, off, cursor, valence, adj, boundary, dual_p, dual_n, pos, nrm, process_boundary,
+                smooth_normals, set_colors);
+}
+
+// The whole sweep sequence chunk by chunk: a chunk's vertices only ever
+// touch its own primitives, so one CTA can run every dual and primal step of
+// a chunk with block barriers in between, while the chunk's positions, dual
+// values and adjacency stay in L2.  The operations per primitive and vertex
+// are those of k_dual / k_primal, so results are identical.  CTAs take chunks
+// from a queue ordered largest first.
+template <int N>
+__global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
+    const ChunkDev* __restrict__ chunks, const uint32_t* __restrict__ tot, const int* __restrict__ order, int n_chunks,
+    int* __restrict__ queue, int64_t nv, int64_t n_prims, int64_t adj_cap, const int64_t* __restrict__ d_counts,
+    const uint32_t* __restrict__ off, const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
+    const uint8_t* __restrict__ boundary, const uint32_t* __restrict__ idx, float* __restrict__ pos,
+    float* __restrict__ nrm, float* __restrict__ dual_p, float* __restrict__ dual_n, int iters, int process_boundary,
+    int sn) {
+  __shared__ int s_item;
+  const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
+  const int64_t npb = d_counts ? min(n_prims, d_counts[1] / N) : n_prims;
+  const int hard_norm_max = 10;
+  const int max_norms = (iters / 2 - 3 < hard_norm_max ? iters / 2 - 3 : hard_norm_max);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();  // everyone has read s_item before thread 0 takes the next
+    if (it >= n_chunks) break;
+    const int c = order[it];
+    const int64_t v0 = chunks[c].vout, v1 = min(v0 + (int64_t)tot[2 * c], nvb);
+    const int64_t p0 = chunks[c].iout / N, p1 = min((chunks[c].iout + (int64_t)tot[2 * c + 1]) / N, npb);
+    for (int m = 0; m < iters; ++m) {
+      const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
+      const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
+      for (int64_t t = p0 + threadIdx.x; t < p1; t += blockDim.x)
+        dual_prim<N>(t, nvb, idx, pos, nrm, dual_p, dual_n, normal_mode);
+      __syncthreads();
+      for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+        primal_vertex(v, n_prims, adj_cap, off, nullptr, valence, adj, boundary, dual_p, dual_n, pos, nrm,
+                      process_boundary, sn, set_colors);
+      __syncthreads();
+    }
   }
 }
 
@@ -487,6 +548,31 @@ int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, 
   const int hard_norm_max = 10;
   const int max_norms = (iters / 2 - 3 < hard_norm_max ? iters / 2 - 3 : hard_norm_max);
   const bool sn = smooth_normals != 0 && nrm != nullptr;
+  if (sa && sa->tot && sa->order && sa->queue) {
+    static int grid[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int gi = dev >= 0 && dev < 64 ? dev : 0;
+    if (grid[gi] == 0) {
+      int sms = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (N == 3)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<3>, kChunkSweepThreads, 0);
+      else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<4>, kChunkSweepThreads, 0);
+      grid[gi] = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    cudaMemsetAsync(sa->queue, 0, sizeof(int), st);
+    if (N == 3)
+      k_sweep_chunks<3><<<grid[gi], kChunkSweepThreads, 0, st>>>(
+          sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_slots, d_counts, s.off, valence,
+          s.adj, boundary, idx, pos, nrm, s.dual_p, s.dual_n, iters, process_boundary, sn ? 1 : 0);
+    else
+      k_sweep_chunks<4><<<grid[gi], kChunkSweepThreads, 0, st>>>(
+          sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_slots, d_counts, s.off, valence,
+          s.adj, boundary, idx, pos, nrm, s.dual_p, s.dual_n, iters, process_boundary, sn ? 1 : 0);
+    return launched + 1;
+  }
   for (int m = 0; m < iters; ++m) {
     const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
     if (N == 3)

@@ -268,6 +268,50 @@ def test_batch_matches_oracle_per_chunk(ctx, mode, placement, iters, use_graph):
     b.close()
 
 
+@pytest.mark.parametrize("mode", [L.MODE_R, L.MODE_Q])
+def test_chunk_sweeps_match_whole_mesh_sweeps(ctx, mode):
+    """A batch of 2048 chunks or more runs its sweeps chunk by chunk (one CTA
+    per chunk); smaller batches run them as whole-mesh kernels.  Split in two
+    small batches, the same chunks give bit-identical positions, normals and
+    indices; a sample of chunks also matches the oracle."""
+    from binarymeshfitting_gb300.engine import Batch
+    descs, rows = workloads.lod_update(n=2100, seed=9)
+    for dsc, r in zip(descs, rows):  # small chunks keep the test quick
+        dsc.dim = 17
+        r[4] = 17
+    kw = dict(mode=mode, placement=L.PLACE_MASSPOINT, iters=4, smooth_normals=True)
+    big = Batch(ctx, descs, workloads.terrain_field(), **kw)
+    big.allocate(3000000, 12000000, normals=True)
+    nv, ni = big.run(use_graph=True)
+    parts = [(0, 1000), (1000, 2100)]
+    got_v = 0
+    checked = 0
+    for lo, hi in parts:
+        sub = Batch(ctx, descs[lo:hi], workloads.terrain_field(), **kw)
+        sub.allocate(1500000, 6000000, normals=True)
+        sv, si = sub.run(use_graph=True)
+        got_v += sv
+        for i in range(hi - lo):
+            a, b_ = big.chunk_mesh(lo + i), sub.chunk_mesh(i)
+            for k in ("pos", "nrm", "idx"):
+                assert torch.equal(a[k].view(torch.int32) if a[k].is_floating_point() else a[k],
+                                   b_[k].view(torch.int32) if b_[k].is_floating_point() else b_[k]), (lo + i, k)
+            if a["contains_mesh"] and checked < 8 and len(a["pos"]) > 0:
+                r = rows[lo + i]
+                d = cpu.fill_field(2, list(workloads.TERRAIN_PARAMS), 17, r[:3], r[3])
+                w, _ = cpu.label_grid(17, d)
+                if mode == L.MODE_R:
+                    O, N = cpu.extract_r(17, d, cpu.cell_masks(17, w)), 3
+                else:
+                    O, N = cpu.extract_q(17, d, w, L.PLACE_MASSPOINT), 4
+                op, _ = cpu.process(N, O["pos"], O["boundary"], O["valence"], O["idx"], 4, False, True)
+                assert_float_exact(a["pos"].cpu().numpy(), op, "chunk %d positions" % (lo + i))
+                checked += 1
+        sub.close()
+    assert got_v == nv and checked == 8
+    big.close()
+
+
 def test_batch_tunings_give_identical_results(ctx):
     """Every launch tuning (fill kernel form, tile height, sweep block) changes
     speed only: the whole arena is bit-identical to the default's."""
