@@ -401,7 +401,9 @@ def run_gb300(args):
                 "extraction_hbm": {"kernels": "count+scan+offsets+emit", "achieved": ext_gbs, "peak": hbm_peak,
                                    "unit": "GB/s", "frac": ext_gbs / hbm_peak, "bytes": ext_bytes,
                                    "ms": ext_ms, "peak_kind": peak_kind},
-                "processing_hbm": {"kernels": "scan+adj_build+%d x (dual, primal)" % args.iters,
+                "processing_hbm": {"kernels": ("k_sweep_chunks (CSR scan, adjacency, %d x (dual, primal), chunk by chunk)"
+                                               if args.chunks >= 2048 else "scan+adj_build+%d x (dual, primal)")
+                                              % args.iters,
                                    "achieved": proc_gbs, "peak": hbm_peak, "unit": "GB/s",
                                    "frac": proc_gbs / hbm_peak, "bytes": proc_bytes, "ms": st_ms[5],
                                    "peak_kind": peak_kind},

@@ -19,6 +19,7 @@
 #include "bmf_device.cuh"
 #include "bmf_internal.h"
 #include "bmf_qef.cuh"
+#include "bmf_sweep.cuh"
 
 namespace bmf {
 
@@ -721,31 +722,22 @@ __device__ __forceinline__ void load_tabs_some(SmemTabs& t) {
   __syncthreads();
 }
 
+// The adjacency list of one vertex (key: its packed grid position) of chunk
+// ch, at most room entries, into out.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ chunks, int n_chunks,
-                                                   const uint32_t* __restrict__ words, WordScratch ws,
-                                                   const uint32_t* __restrict__ vkey, const uint32_t* __restrict__ off,
-                                                   const int64_t* __restrict__ d_counts, int64_t vcap,
-                                                   uint32_t* __restrict__ adj) {
-  __shared__ SmemTabs T;
-  load_tabs_some<MODE == 0, MODE == 0, MODE != 0>(T);
-  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
-  const int c = find_chunk_by_vertex(chunks, n_chunks, v);
-  const ChunkDev& ch = chunks[c];
+__device__ __forceinline__ void adj_vertex(const SmemTabs& T, const ChunkDev& ch, const uint32_t* __restrict__ words,
+                                           const WordScratch& ws, uint32_t key, uint32_t* __restrict__ out,
+                                           int room) {
   const int dim = ch.dim, zc = ch.zc;
   const int64_t iout = ch.iout;
   const uint32_t* W = words + ch.words;
   const uint32_t* ibase = ws.icnt + ch.words;
   const uint32_t* pl = ws.gpl + 3 * ch.words;
   int x, y, z, k;
-  vertex_key_decode(vkey[v], x, y, z, k);
+  vertex_key_decode(key, x, y, z, k);
   // the chunk's first primitive (its index offset and word bases are
   // multiples of the primitive size)
   const int64_t pbase = iout / (MODE == 0 ? 3 : 4);
-  uint32_t* out = adj + off[v];
-  // the vertex's CSR range (the exclusive scan of init_valence): never write past it
-  const int room = (int)(off[v + 1] - off[v]);
   int n = 0;
   if (MODE == 0) {
     const int a = k;
@@ -811,6 +803,21 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
   }
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ chunks, int n_chunks,
+                                                   const uint32_t* __restrict__ words, WordScratch ws,
+                                                   const uint32_t* __restrict__ vkey, const uint32_t* __restrict__ off,
+                                                   const int64_t* __restrict__ d_counts, int64_t vcap,
+                                                   uint32_t* __restrict__ adj) {
+  __shared__ SmemTabs T;
+  load_tabs_some<MODE == 0, MODE == 0, MODE != 0>(T);
+  const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
+  const int c = find_chunk_by_vertex(chunks, n_chunks, v);
+  // the vertex's CSR range (the exclusive scan of init_valence): never write past it
+  adj_vertex<MODE>(T, chunks[c], words, ws, vkey[v], adj + off[v], (int)(off[v + 1] - off[v]));
+}
+
 void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
                       const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,
                       uint32_t* adj, cudaStream_t st) {
@@ -818,6 +825,131 @@ void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const ui
   if (blocks == 0) return;
   if (mode == 0) k_adj_build<0><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
   else k_adj_build<1><<<blocks, 256, 0, st>>>(d_chunks, n_chunks, words, ws, vkey, off, d_counts, vcap, adj);
+}
+
+// ---------------------------------------------------------------------------
+// K5+K6 chunk by chunk (batches): one CTA per chunk, from a queue ordered
+// largest first, runs the chunk's CSR offsets, its adjacency and every
+// dual / primal sweep with block barriers in between.  A chunk's vertices
+// only touch its own primitives, and the sum of its vertices' valences is its
+// index count, so the chunk's offsets are its index offset plus the exclusive
+// scan of its own valences -- the global scan's values.  Per primitive and
+// vertex the operations are those of k_adj_build, k_dual and k_primal, so
+// the results are identical.
+// ---------------------------------------------------------------------------
+template <int MODE, int N>
+__global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
+    const ChunkDev* __restrict__ chunks, const uint32_t* __restrict__ tot, const int* __restrict__ order,
+    int n_chunks, int* __restrict__ queue, const uint32_t* __restrict__ words, WordScratch ws,
+    const uint32_t* __restrict__ vkey, int64_t nv, int64_t n_prims, int64_t adj_cap,
+    const int64_t* __restrict__ d_counts, uint32_t* __restrict__ off, const uint8_t* __restrict__ valence,
+    uint32_t* __restrict__ adj, const uint8_t* __restrict__ boundary, const uint32_t* __restrict__ idx,
+    float* __restrict__ pos, float* __restrict__ nrm, float* __restrict__ dual_p, float* __restrict__ dual_n,
+    int iters, int process_boundary, int sn) {
+  constexpr int kWarps = kChunkSweepThreads / 32;
+  __shared__ SmemTabs T;
+  __shared__ uint32_t s_warp[kWarps];
+  __shared__ uint32_t s_total;
+  __shared__ int s_item;
+  load_tabs_some<MODE == 0, MODE == 0, MODE != 0>(T);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
+  const int64_t npb = d_counts ? min(n_prims, d_counts[1] / N) : n_prims;
+  const int hard_norm_max = 10;
+  const int max_norms = (iters / 2 - 3 < hard_norm_max ? iters / 2 - 3 : hard_norm_max);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();  // everyone has read s_item before thread 0 takes the next
+    if (it >= n_chunks) break;
+    const int c = order[it];
+    const ChunkDev& ch = chunks[c];
+    const int64_t v0 = ch.vout, v1 = min(v0 + (int64_t)tot[2 * c], nvb);
+    const int64_t p0 = ch.iout / N, p1 = min((ch.iout + (int64_t)tot[2 * c + 1]) / N, npb);
+    // CSR offsets (MeshProcessor.cpp:32-40), blockDim vertices per pass;
+    // vertex v is always handled by the same thread below
+    uint32_t carry = (uint32_t)ch.iout;
+    for (int64_t b = v0; b < v1; b += kChunkSweepThreads) {
+      const int64_t v = b + threadIdx.x;
+      const uint32_t x = v < v1 ? (uint32_t)__ldg(valence + v) : 0u;
+      uint32_t incl = x;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+      }
+      if (lane == 31) s_warp[warp] = incl;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t w = lane < kWarps ? s_warp[lane] : 0u;
+        uint32_t wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, wi, d);
+          if (lane >= d) wi += y;
+        }
+        if (lane < kWarps) s_warp[lane] = wi - w;  // exclusive over warps
+        if (lane == kWarps - 1) s_total = wi;
+      }
+      __syncthreads();
+      if (v < v1) off[v] = carry + s_warp[warp] + incl - x;
+      carry += s_total;
+      __syncthreads();
+    }
+    // adjacency, in each vertex's own CSR range and inside adj
+    for (int64_t v = v0 + threadIdx.x; v < v1; v += kChunkSweepThreads) {
+      const uint32_t o = off[v];
+      const int room = (int)max((int64_t)0, min((int64_t)__ldg(valence + v), adj_cap - (int64_t)o));
+      adj_vertex<MODE>(T, ch, words, ws, __ldg(vkey + v), adj + o, room);
+    }
+    __syncthreads();
+    for (int m = 0; m < iters; ++m) {
+      const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
+      const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
+      for (int64_t t = p0 + threadIdx.x; t < p1; t += kChunkSweepThreads)
+        dual_prim<N, true>(t, nvb, idx, pos, nrm, dual_p, dual_n, normal_mode);
+      __syncthreads();
+      for (int64_t v = v0 + threadIdx.x; v < v1; v += kChunkSweepThreads)
+        primal_vertex<true>(v, n_prims, adj_cap, off, nullptr, valence, adj, boundary, dual_p, dual_n, pos, nrm,
+                            process_boundary, sn, set_colors);
+      __syncthreads();
+    }
+  }
+}
+
+template <int MODE, int N>
+static int sweep_chunks_grid() {
+  static int grid[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int gi = dev >= 0 && dev < 64 ? dev : 0;
+  if (grid[gi] == 0) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<MODE, N>, kChunkSweepThreads, 0);
+    grid[gi] = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  return grid[gi];
+}
+
+void launch_sweep_chunks(const StructuredAdj& sa, int N, int64_t nv, int64_t n_prims, const int64_t* d_counts,
+                         float* pos, float* nrm, const uint8_t* boundary, const uint8_t* valence,
+                         const uint32_t* idx, int iters, int process_boundary, int smooth_normals,
+                         const ProcessScratch& s, cudaStream_t st) {
+  cudaMemsetAsync(sa.queue, 0, sizeof(int), st);
+  const int64_t adj_cap = n_prims * N;
+#define BMF_SWEEP_CHUNKS(M, NN)                                                                                 \
+  k_sweep_chunks<M, NN><<<sweep_chunks_grid<M, NN>(), kChunkSweepThreads, 0, st>>>(                              \
+      sa.chunks, sa.tot, sa.order, sa.n_chunks, sa.queue, sa.words, sa.ws, sa.vkey, nv, n_prims, adj_cap,        \
+      d_counts, s.off, valence, s.adj, boundary, idx, pos, nrm, s.dual_p, s.dual_n, iters, process_boundary,      \
+      smooth_normals)
+  if (sa.mode == 0) {
+    if (N == 3) BMF_SWEEP_CHUNKS(0, 3); else BMF_SWEEP_CHUNKS(0, 4);
+  } else {
+    if (N == 3) BMF_SWEEP_CHUNKS(1, 3); else BMF_SWEEP_CHUNKS(1, 4);
+  }
+#undef BMF_SWEEP_CHUNKS
 }
 
 void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,

@@ -112,6 +112,12 @@ struct StructuredAdj {
 void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
                       const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,
                       uint32_t* adj, cudaStream_t st);
+// The chunk-by-chunk form of launch_process for StructuredAdj with tot /
+// order / queue set: CSR offsets, adjacency and all sweeps in one launch.
+void launch_sweep_chunks(const StructuredAdj& sa, int N, int64_t nv, int64_t n_prims, const int64_t* d_counts,
+                         float* pos, float* nrm, const uint8_t* boundary, const uint8_t* valence,
+                         const uint32_t* idx, int iters, int process_boundary, int smooth_normals,
+                         const ProcessScratch& s, cudaStream_t st);
 // Returns the number of kernels launched.
 int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, float* pos, float* nrm,
                    const uint8_t* boundary, const uint8_t* valence, const uint32_t* idx, int iters,

@@ -11,6 +11,7 @@
 // fill uses atomic cursors and then sorts each (short) list.
 #include "bmf_device.cuh"
 #include "bmf_internal.h"
+#include "bmf_sweep.cuh"
 
 namespace bmf {
 
@@ -132,99 +133,6 @@ __global__ void k_sort_adj(int64_t nv, int64_t adj_cap, const int64_t* __restric
   }
 }
 
-__device__ __forceinline__ void nrm3(const float v[3], float o[3]) {
-  const float l2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
-  const float inv = 1.0f / sqrtf(l2);
-  o[0] = v[0] * inv;
-  o[1] = v[1] * inv;
-  o[2] = v[2] * inv;
-}
-__device__ __forceinline__ void cross3(const float a[3], const float b[3], float o[3]) {
-  o[0] = a[1] * b[2] - b[1] * a[2];
-  o[1] = a[2] * b[0] - b[2] * a[0];
-  o[2] = a[0] * b[1] - b[0] * a[1];
-}
-
-// optimize_dual_grid body (MeshProcessor.cpp:142-227).  normal_mode: 0 none,
-// 1 face normal, 2 sum of vertex normals.
-constexpr int kChunkSweepThreads = 512;
-
-template <int N>
-__device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t* __restrict__ idx,
-                                          const float* __restrict__ pos, const float* __restrict__ nrm,
-                                          float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
-  uint32_t v[N];
-#pragma unroll
-  for (int k = 0; k < N; ++k) {
-    v[k] = __ldg(idx + N * t + k);
-    if ((int64_t)v[k] >= nvb) v[k] = 0;  // an index outside the mesh reads vertex 0 instead of faulting
-  }
-  float p[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-  for (int k = 0; k < N; ++k) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) p[c] = p[c] + __ldg(pos + 3 * v[k] + c);
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) dual_p[3 * t + c] = p[c] / (float)N;
-  if (normal_mode == 0) return;
-  float o[3];
-  if (normal_mode == 1) {
-    if (N == 3) {
-      float a[3] = {0.0f, 0.0f, 0.0f}, b[3] = {0.0f, 0.0f, 0.0f}, na[3], nb[3];
-      if (v[0] != v[1] && v[1] != v[2] && v[0] != v[2]) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          a[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[1] + c);
-          b[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[2] + c);
-        }
-      }
-      nrm3(a, na);
-      nrm3(b, nb);
-      cross3(na, nb, o);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) o[c] = -o[c];
-    } else {
-      float a[3], b[3], na[3], nb[3], n1[3], n2[3];
-      const uint32_t v3 = v[N - 1];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        a[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[1] + c);
-        b[c] = __ldg(pos + 3 * v[0] + c) - __ldg(pos + 3 * v[2] + c);
-      }
-      nrm3(a, na);
-      nrm3(b, nb);
-      cross3(na, nb, n1);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        a[c] = __ldg(pos + 3 * v[2] + c) - __ldg(pos + 3 * v3 + c);
-        b[c] = __ldg(pos + 3 * v[2] + c) - __ldg(pos + 3 * v[0] + c);
-      }
-      nrm3(a, na);
-      nrm3(b, nb);
-      cross3(na, nb, n2);
-      if (isnan(n1[0])) {
-        n1[0] = n2[0]; n1[1] = n2[1]; n1[2] = n2[2];
-        if (isnan(n1[0])) { n1[0] = 0.0f; n1[1] = 1.0f; n1[2] = 0.0f; }
-      }
-      if (isnan(n2[0])) { n2[0] = n1[0]; n2[1] = n1[1]; n2[2] = n1[2]; }
-      const float h[3] = {(n1[0] + n2[0]) * 0.5f, (n1[1] + n2[1]) * 0.5f, (n1[2] + n2[2]) * 0.5f};
-      nrm3(h, o);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) o[c] = -o[c];
-    }
-  } else {
-    o[0] = o[1] = o[2] = 0.0f;
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) o[c] = o[c] + __ldg(nrm + 3 * v[k] + c);
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) dual_n[3 * t + c] = o[c];
-}
-
 template <int N>
 __global__ void k_dual(int64_t n_prims, int64_t nv, const int64_t* __restrict__ d_counts,
                        const uint32_t* __restrict__ idx, const float* __restrict__ pos, const float* __restrict__ nrm,
@@ -235,50 +143,6 @@ __global__ void k_dual(int64_t n_prims, int64_t nv, const int64_t* __restrict__ 
 }
 
 // optimize_primal_grid (MeshProcessor.cpp:238-306).
-__device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t adj_cap,
-                                              const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
-                                              const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
-                                              const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
-                                              const float* __restrict__ dual_n, float* __restrict__ pos,
-                                              float* __restrict__ nrm, int process_boundary, int smooth_normals,
-                                              int set_colors) {
-  // list length: adj_next (MeshProcessor.cpp:247); with a prebuilt adjacency it equals init_valence
-  const int64_t room = adj_cap - (int64_t)off[v];
-  const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)(cursor ? min(cursor[v], (uint32_t)valence[v])
-                                                                    : (uint32_t)valence[v]), room));
-  if (n == 0 || (!process_boundary && boundary[v])) return;
-  const uint32_t* a = adj + off[v];
-  float p[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
-  for (uint32_t k = 0; k < n; ++k) {
-    const uint32_t t = __ldg(a + k);
-    if ((int64_t)t >= np_lim) continue;  // never read past the dual points
-#pragma unroll
-    for (int c = 0; c < 3; ++c) p[c] = p[c] + __ldg(dual_p + 3 * t + c);
-    if (smooth_normals) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) nn[c] = nn[c] + __ldg(dual_n + 3 * t + c);
-    }
-  }
-  const float cnt = (float)n;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) p[c] = p[c] / cnt;
-  if (smooth_normals) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) nn[c] = nn[c] / cnt;
-  }
-  if (set_colors) {
-    float o[3];
-    nrm3(nn, o);
-    nn[0] = o[0]; nn[1] = o[1]; nn[2] = o[2];
-  }
-#pragma unroll
-  for (int c = 0; c < 3; ++c) pos[3 * v + c] = p[c];
-  if (nrm && nn[1] != 0.0f) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) nrm[3 * v + c] = nn[c];
-  }
-}
-
 __global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int64_t* __restrict__ d_counts,
                          const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
                          const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
@@ -289,48 +153,6 @@ __global__ void k_primal(int64_t nv, int64_t np_lim, int64_t adj_cap, const int6
   if (v >= (d_counts ? min(nv, d_counts[0]) : nv)) return;
   primal_vertex(v, np_lim, adj_cap, off, cursor, valence, adj, boundary, dual_p, dual_n, pos, nrm, process_boundary,
                 smooth_normals, set_colors);
-}
-
-// The whole sweep sequence chunk by chunk: a chunk's vertices only ever
-// touch its own primitives, so one CTA can run every dual and primal step of
-// a chunk with block barriers in between, while the chunk's positions, dual
-// values and adjacency stay in L2.  The operations per primitive and vertex
-// are those of k_dual / k_primal, so results are identical.  CTAs take chunks
-// from a queue ordered largest first.
-template <int N>
-__global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
-    const ChunkDev* __restrict__ chunks, const uint32_t* __restrict__ tot, const int* __restrict__ order, int n_chunks,
-    int* __restrict__ queue, int64_t nv, int64_t n_prims, int64_t adj_cap, const int64_t* __restrict__ d_counts,
-    const uint32_t* __restrict__ off, const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
-    const uint8_t* __restrict__ boundary, const uint32_t* __restrict__ idx, float* __restrict__ pos,
-    float* __restrict__ nrm, float* __restrict__ dual_p, float* __restrict__ dual_n, int iters, int process_boundary,
-    int sn) {
-  __shared__ int s_item;
-  const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
-  const int64_t npb = d_counts ? min(n_prims, d_counts[1] / N) : n_prims;
-  const int hard_norm_max = 10;
-  const int max_norms = (iters / 2 - 3 < hard_norm_max ? iters / 2 - 3 : hard_norm_max);
-  for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
-    __syncthreads();
-    const int it = s_item;
-    __syncthreads();  // everyone has read s_item before thread 0 takes the next
-    if (it >= n_chunks) break;
-    const int c = order[it];
-    const int64_t v0 = chunks[c].vout, v1 = min(v0 + (int64_t)tot[2 * c], nvb);
-    const int64_t p0 = chunks[c].iout / N, p1 = min((chunks[c].iout + (int64_t)tot[2 * c + 1]) / N, npb);
-    for (int m = 0; m < iters; ++m) {
-      const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
-      const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
-      for (int64_t t = p0 + threadIdx.x; t < p1; t += blockDim.x)
-        dual_prim<N>(t, nvb, idx, pos, nrm, dual_p, dual_n, normal_mode);
-      __syncthreads();
-      for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x)
-        primal_vertex(v, n_prims, adj_cap, off, nullptr, valence, adj, boundary, dual_p, dual_n, pos, nrm,
-                      process_boundary, sn, set_colors);
-      __syncthreads();
-    }
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -527,6 +349,12 @@ int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, 
                    cudaStream_t st) {
   if (nv == 0 || n_prims == 0 || iters <= 0) return 0;
   const int64_t n_slots = n_prims * N;
+  const bool sn = smooth_normals != 0 && nrm != nullptr;
+  if (sa && sa->tot && sa->order && sa->queue) {
+    launch_sweep_chunks(*sa, N, nv, n_prims, d_counts, pos, nrm, boundary, valence, idx, iters, process_boundary,
+                        sn ? 1 : 0, s, st);
+    return 1;
+  }
   int launched = 3;
   // CSR offsets: exclusive scan of init_valence (MeshProcessor.cpp:32-40)
   launch_exclusive_scan_u8_to_u32(valence, s.off, nv, d_counts, s.tmp, st);
@@ -547,32 +375,6 @@ int launch_process(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, 
   }
   const int hard_norm_max = 10;
   const int max_norms = (iters / 2 - 3 < hard_norm_max ? iters / 2 - 3 : hard_norm_max);
-  const bool sn = smooth_normals != 0 && nrm != nullptr;
-  if (sa && sa->tot && sa->order && sa->queue) {
-    static int grid[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const int gi = dev >= 0 && dev < 64 ? dev : 0;
-    if (grid[gi] == 0) {
-      int sms = 0, per_sm = 0;
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      if (N == 3)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<3>, kChunkSweepThreads, 0);
-      else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<4>, kChunkSweepThreads, 0);
-      grid[gi] = sms * (per_sm > 0 ? per_sm : 1);
-    }
-    cudaMemsetAsync(sa->queue, 0, sizeof(int), st);
-    if (N == 3)
-      k_sweep_chunks<3><<<grid[gi], kChunkSweepThreads, 0, st>>>(
-          sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_slots, d_counts, s.off, valence,
-          s.adj, boundary, idx, pos, nrm, s.dual_p, s.dual_n, iters, process_boundary, sn ? 1 : 0);
-    else
-      k_sweep_chunks<4><<<grid[gi], kChunkSweepThreads, 0, st>>>(
-          sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_slots, d_counts, s.off, valence,
-          s.adj, boundary, idx, pos, nrm, s.dual_p, s.dual_n, iters, process_boundary, sn ? 1 : 0);
-    return launched + 1;
-  }
   for (int m = 0; m < iters; ++m) {
     const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
     if (N == 3)

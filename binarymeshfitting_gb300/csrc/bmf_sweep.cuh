@@ -1,0 +1,160 @@
+// The MeshProcessor sweep steps for one primitive (dual) and one vertex
+// (primal), shared by the whole-mesh kernels (bmf_process.cu) and the
+// chunk-by-chunk kernel (bmf_extract.cu).  MeshProcessor.cpp:130-306.
+#pragma once
+
+#include "bmf_device.cuh"
+
+namespace bmf {
+
+// threads of the chunk-by-chunk sweep kernel's CTA
+constexpr int kChunkSweepThreads = 512;
+
+// COH selects the load for data that the same kernel also writes (positions,
+// normals and dual values in the chunk-by-chunk kernel, which runs every
+// sweep in one launch, and its adjacency): a plain L1-cached load, which
+// block barriers order.  Otherwise the read-only path.
+template <bool COH, typename T>
+__device__ __forceinline__ T sweep_ld(const T* p) {
+  if (COH) return __ldca(p);
+  return __ldg(p);
+}
+
+__device__ __forceinline__ void nrm3(const float v[3], float o[3]) {
+  const float l2 = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+  const float inv = 1.0f / sqrtf(l2);
+  o[0] = v[0] * inv;
+  o[1] = v[1] * inv;
+  o[2] = v[2] * inv;
+}
+__device__ __forceinline__ void cross3(const float a[3], const float b[3], float o[3]) {
+  o[0] = a[1] * b[2] - b[1] * a[2];
+  o[1] = a[2] * b[0] - b[2] * a[0];
+  o[2] = a[0] * b[1] - b[0] * a[1];
+}
+
+// optimize_dual_grid body (MeshProcessor.cpp:142-227).  normal_mode: 0 none,
+// 1 face normal, 2 sum of vertex normals.
+template <int N, bool COH = false>
+__device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t* __restrict__ idx,
+                                          const float* __restrict__ pos, const float* __restrict__ nrm,
+                                          float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
+  uint32_t v[N];
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    v[k] = __ldg(idx + N * t + k);
+    if ((int64_t)v[k] >= nvb) v[k] = 0;  // an index outside the mesh reads vertex 0 instead of faulting
+  }
+  float p[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p[c] = p[c] + sweep_ld<COH>(pos + 3 * v[k] + c);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) dual_p[3 * t + c] = p[c] / (float)N;
+  if (normal_mode == 0) return;
+  float o[3];
+  if (normal_mode == 1) {
+    if (N == 3) {
+      float a[3] = {0.0f, 0.0f, 0.0f}, b[3] = {0.0f, 0.0f, 0.0f}, na[3], nb[3];
+      if (v[0] != v[1] && v[1] != v[2] && v[0] != v[2]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          a[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[1] + c);
+          b[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[2] + c);
+        }
+      }
+      nrm3(a, na);
+      nrm3(b, nb);
+      cross3(na, nb, o);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c] = -o[c];
+    } else {
+      float a[3], b[3], na[3], nb[3], n1[3], n2[3];
+      const uint32_t v3 = v[N - 1];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[1] + c);
+        b[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[2] + c);
+      }
+      nrm3(a, na);
+      nrm3(b, nb);
+      cross3(na, nb, n1);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a[c] = sweep_ld<COH>(pos + 3 * v[2] + c) - sweep_ld<COH>(pos + 3 * v3 + c);
+        b[c] = sweep_ld<COH>(pos + 3 * v[2] + c) - sweep_ld<COH>(pos + 3 * v[0] + c);
+      }
+      nrm3(a, na);
+      nrm3(b, nb);
+      cross3(na, nb, n2);
+      if (isnan(n1[0])) {
+        n1[0] = n2[0]; n1[1] = n2[1]; n1[2] = n2[2];
+        if (isnan(n1[0])) { n1[0] = 0.0f; n1[1] = 1.0f; n1[2] = 0.0f; }
+      }
+      if (isnan(n2[0])) { n2[0] = n1[0]; n2[1] = n1[1]; n2[2] = n1[2]; }
+      const float h[3] = {(n1[0] + n2[0]) * 0.5f, (n1[1] + n2[1]) * 0.5f, (n1[2] + n2[2]) * 0.5f};
+      nrm3(h, o);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c] = -o[c];
+    }
+  } else {
+    o[0] = o[1] = o[2] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c] = o[c] + sweep_ld<COH>(nrm + 3 * v[k] + c);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) dual_n[3 * t + c] = o[c];
+}
+
+template <bool COH = false>
+__device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t adj_cap,
+                                              const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
+                                              const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
+                                              const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
+                                              const float* __restrict__ dual_n, float* __restrict__ pos,
+                                              float* __restrict__ nrm, int process_boundary, int smooth_normals,
+                                              int set_colors) {
+  // list length: adj_next (MeshProcessor.cpp:247); with a prebuilt adjacency it equals init_valence
+  const uint32_t ov = sweep_ld<COH>(off + v);
+  const int64_t room = adj_cap - (int64_t)ov;
+  const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)(cursor ? min(cursor[v], (uint32_t)valence[v])
+                                                                    : (uint32_t)valence[v]), room));
+  if (n == 0 || (!process_boundary && boundary[v])) return;
+  const uint32_t* a = adj + ov;
+  float p[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
+  for (uint32_t k = 0; k < n; ++k) {
+    const uint32_t t = sweep_ld<COH>(a + k);
+    if ((int64_t)t >= np_lim) continue;  // never read past the dual points
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p[c] = p[c] + sweep_ld<COH>(dual_p + 3 * t + c);
+    if (smooth_normals) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) nn[c] = nn[c] + sweep_ld<COH>(dual_n + 3 * t + c);
+    }
+  }
+  const float cnt = (float)n;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) p[c] = p[c] / cnt;
+  if (smooth_normals) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nn[c] = nn[c] / cnt;
+  }
+  if (set_colors) {
+    float o[3];
+    nrm3(nn, o);
+    nn[0] = o[0]; nn[1] = o[1]; nn[2] = o[2];
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) pos[3 * v + c] = p[c];
+  if (nrm && nn[1] != 0.0f) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nrm[3 * v + c] = nn[c];
+  }
+}
+
+}  // namespace bmf
