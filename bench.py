@@ -29,13 +29,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "chunks/s (mixed-LOD batch vs per-chunk, same GB300, exact topology)"
-# FP32 operations of the line-separable FBM (counted from the kernel source,
-# mul and add separately since contraction is off)
-OPS_PER_SAMPLE_OCTAVE = 9   # l0, l1 (2 each), l1 - l0, w * (.), + l0, amp * n, sum +
-OPS_PER_SAMPLE = 2          # (py - h) - a * sum: the product and the difference
-OPS_PER_LINE_OCTAVE = 24    # xs, ys, 2 floor, xf, yf, 2 fade (7 each), x1, y1, fr, amp
+# FP32 instructions of the line-separable FBM, counted from the kernel source
+# (a fused multiply-add is one instruction; the denominator is the FP32
+# instruction rate)
+OPS_PER_SAMPLE_OCTAVE = 5   # l0, l1 (one fma each), l1 - l0, fma(w, ., l0), fma(amp, n, sum)
+OPS_PER_SAMPLE = 1          # fma(-a, sum, py - h)
+OPS_PER_LINE_OCTAVE = 20    # xs, ys, 2 floor, xf, yf, 2 fade (5 each), x1, y1, fr, amp
 OPS_PER_LINE = 1            # py - h
-OPS_PER_LAYER = 22          # 4 corner sums s, alpha and beta (3 lerps of 3 operations each)
+OPS_PER_LAYER = 20          # 4 corners (mul + fma), alpha and beta (3 lerps of 2 each)
 # DRAM bytes (read + write) per sample of k_fill_terrain from one ncu capture on
 # the 256-chunk update (110,890,368 samples, 80.08 MB read + 479.36 MB written):
 # traffic grows with the samples, so a full launch is scaled from it

@@ -96,65 +96,60 @@ __device__ __forceinline__ float det_sin(float x) {
   return (q & 2) ? -v : v;
 }
 
+// Noise arithmetic: fused multiply-adds (one rounding each) at fixed places --
+// fade's two inner steps, every lerp a + t (b - a) = fma(t, b - a, a), a
+// corner's s = fma(gy, y, gx * x), l = fma(beta, zk, alpha) and the FBM sums.
+// The oracle calls fmaf at exactly these places (and rounds every other
+// operation separately), so the two agree bit for bit.
 __device__ __forceinline__ float fade(float t) {
-  float a = t * 6.0f;
-  a = a - 15.0f;
-  a = t * a;
-  a = a + 10.0f;
+  float a = __fmaf_rn(t, 6.0f, -15.0f);
+  a = __fmaf_rn(t, a, 10.0f);
   float t3 = t * t;
   t3 = t3 * t;
   return t3 * a;
 }
-__device__ __forceinline__ float lerp_t(float t, float a, float b) { return a + t * (b - a); }
+__device__ __forceinline__ float lerp_t(float t, float a, float b) { return __fmaf_rn(t, b - a, a); }
 
 // ---------------------------------------------------------------------------
 // Improved gradient noise (K. Perlin, SIGGRAPH 2002) in line-separable form.
 //
 // A corner gradient grad(h, x, y, z) = (+/-u) + (+/-v) with u in {x, y} and v in
-// {x, y, z} is written s + c * z: s = (+/-u) + (+/-v) and c = +0 when v is x or
-// y; s = +/-u and c = +/-1 when v is z.  lerp is linear, so a z-layer's x/y
-// interpolant of the four corners is alpha + beta * zk exactly, with
+// {x, y, z} (never the same axis as u) is written gx * x + gy * y + c * z with
+// gx, gy, c in {0, +1, -1}: s = fma(gy, y, gx * x) is the textbook x/y part
+// with one rounding.  lerp is linear, so a z-layer's x/y interpolant of the
+// four corners is alpha + beta * zk exactly, with
 //     alpha = lerp(v, lerp(u, s00, s10), lerp(u, s01, s11))   (beta: the c's),
 // and the noise value is  l0 = alpha0 + beta0 * zf,  l1 = alpha1 + beta1 * (zf - 1),
 // l0 + w (l1 - l0).  In exact arithmetic this is the textbook value; in float it
 // differs from the textbook order by rounding only, and the CPU oracle evaluates
-// exactly these operations (compiled without contraction), so samples agree
-// bit for bit.  alpha and beta depend on x, y and the lattice cell Z, not on the
-// sample's own z: a z-line sets them up once per lattice cell, and the layer-1
-// pair of cell Z is the layer-0 pair of cell Z + 1 (same hashes, same operations).
+// exactly these operations, so samples agree bit for bit.  alpha and beta
+// depend on x, y and the lattice cell Z, not on the sample's own z: a z-line
+// sets them up once per lattice cell, and the layer-1 pair of cell Z is the
+// layer-0 pair of cell Z + 1 (same hashes, same operations).
 //
-// Per hash h the gradient is coded for byte permutes (seg_grad_code):
-//   x = selector of u (x or y) | sign of u << 31
-//   y = selector of v (x or y) | (v == z ? 1 : sign of v) << 31
-//   z = 0 when v == z (drops v, leaving the -0.0 that keeps s = +/-u exactly), else all ones
-//   w = the bits of c: +/-1.0f when v == z, else +0.0f
-// Tables are 512 entries, entry i coding perm[i & 255], so hash chains index
-// them without masks.
+// Tables are 512 entries {gx, gy, c, 0}, entry i coding perm[i & 255], so hash
+// chains index them without masks.
 // ---------------------------------------------------------------------------
-__host__ __device__ inline uint4 seg_grad_code(int h) {
+__host__ __device__ inline float4 grad_coeffs(int h) {
   h &= 15;
-  const bool vz = (h & 12) != 0 && (h & 13) != 12;
-  const uint32_t sel_x = 0x3210u, sel_y = 0x7654u;
-  uint4 t;
-  t.x = ((h & 8) ? sel_y : sel_x) | ((uint32_t)(h & 1) << 31);
-  t.y = ((h & 12) == 0 ? sel_y : sel_x) | ((vz ? 1u : (uint32_t)((h >> 1) & 1)) << 31);
-  t.z = vz ? 0u : 0xFFFFFFFFu;
-  t.w = vz ? (0x3F800000u | ((uint32_t)((h >> 1) & 1) << 31)) : 0u;
+  const float su = (h & 1) ? -1.0f : 1.0f, sv = (h & 2) ? -1.0f : 1.0f;
+  float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (h < 8) t.x = su; else t.y = su;
+  if (h < 4) t.y = sv;
+  else if (h == 12 || h == 14) t.x = sv;
+  else t.z = sv;
   return t;
 }
 
 // s and c of one corner at lattice offsets (xc, yc).
-__device__ __forceinline__ void seg_corner(uint4 t, float xc, float yc, float& s, float& c) {
-  const uint32_t xb = __float_as_uint(xc), yb = __float_as_uint(yc);
-  const float su = __uint_as_float(__byte_perm(xb, yb, t.x) ^ (t.x & 0x80000000u));
-  const float sv = __uint_as_float((__byte_perm(xb, yb, t.y) & t.z) ^ (t.y & 0x80000000u));
-  s = su + sv;
-  c = __uint_as_float(t.w);
+__device__ __forceinline__ void seg_corner(float4 t, float xc, float yc, float& s, float& c) {
+  s = __fmaf_rn(t.y, yc, t.x * xc);
+  c = t.z;
 }
 
 // alpha / beta of one z-layer from the hashes of its four corners
 // (h00 = AA + k, h10 = BA + k, h01 = AB + k, h11 = BB + k).
-__device__ __forceinline__ void layer_coeffs(const uint4* __restrict__ gtab, int h00, int h10, int h01, int h11,
+__device__ __forceinline__ void layer_coeffs(const float4* __restrict__ gtab, int h00, int h10, int h01, int h11,
                                              float xf, float yf, float x1, float y1, float u, float v, float& a,
                                              float& b) {
   float s00, c00, s10, c10, s01, c01, s11, c11;
@@ -169,7 +164,7 @@ __device__ __forceinline__ void layer_coeffs(const uint4* __restrict__ gtab, int
 }
 
 // One noise value (perm2: the permutation duplicated to 512 entries).
-__device__ __forceinline__ float perlin(const int* __restrict__ perm2, const uint4* __restrict__ gtab, float x, float y,
+__device__ __forceinline__ float perlin(const int* __restrict__ perm2, const float4* __restrict__ gtab, float x, float y,
                                         float z) {
   const float fx = floorf(x), fy = floorf(y), fz = floorf(z);
   const int X = ((int)fx) & 255, Y = ((int)fy) & 255, Z = ((int)fz) & 255;
@@ -183,9 +178,9 @@ __device__ __forceinline__ float perlin(const int* __restrict__ perm2, const uin
   float a0, b0, a1, b1;
   layer_coeffs(gtab, AA, BA, AB, BB, x, y, x1, y1, u, v, a0, b0);
   layer_coeffs(gtab, AA + 1, BA + 1, AB + 1, BB + 1, x, y, x1, y1, u, v, a1, b1);
-  const float l0 = a0 + b0 * z;
-  const float l1 = a1 + b1 * z1;
-  return l0 + w * (l1 - l0);
+  const float l0 = __fmaf_rn(b0, z, a0);
+  const float l1 = __fmaf_rn(b1, z1, a1);
+  return __fmaf_rn(w, l1 - l0, l0);
 }
 
 constexpr int kRun = 4;
@@ -194,7 +189,7 @@ constexpr int kRun = 4;
 // z-coordinates pz[k]; px, py are the line's world x, y.  Every x/y-dependent
 // term is computed once per octave, and alpha / beta once per lattice cell.
 __device__ __forceinline__ void terrain_run(const FieldDev& f, const int* __restrict__ perm2,
-                                            const uint4* __restrict__ gtab, float px, float py, const float* pz,
+                                            const float4* __restrict__ gtab, float px, float py, const float* pz,
                                             int n, float* out) {
   float sum[kRun];
 #pragma unroll
@@ -226,17 +221,17 @@ __device__ __forceinline__ void terrain_run(const FieldDev& f, const int* __rest
         layer_coeffs(gtab, pA + Z, pB + Z, pA1 + Z, pB1 + Z, xf, yf, x1, y1, u, v, a0, b0);
         layer_coeffs(gtab, pA + Z + 1, pB + Z + 1, pA1 + Z + 1, pB1 + Z + 1, xf, yf, x1, y1, u, v, a1, b1);
       }
-      const float l0 = a0 + b0 * zf;
-      const float l1 = a1 + b1 * z1;
-      const float nv = l0 + w * (l1 - l0);
-      sum[k] = sum[k] + amp * nv;
+      const float l0 = __fmaf_rn(b0, zf, a0);
+      const float l1 = __fmaf_rn(b1, z1, a1);
+      const float nv = __fmaf_rn(w, l1 - l0, l0);
+      sum[k] = __fmaf_rn(amp, nv, sum[k]);
     }
     fr = fr * f.p[3];
     amp = amp * f.p[4];
   }
 #pragma unroll
   for (int k = 0; k < kRun; ++k)
-    if (k < n) out[k] = (py - f.p[0]) - f.p[1] * sum[k];
+    if (k < n) out[k] = __fmaf_rn(-f.p[1], sum[k], py - f.p[0]);
 }
 
 __device__ __forceinline__ float len3(float x, float y, float z) {
@@ -246,7 +241,7 @@ __device__ __forceinline__ float len3(float x, float y, float z) {
 
 // Evaluates a density field at world position (px, py, pz).
 __device__ __forceinline__ float eval_field(const FieldDev& f, const int* __restrict__ perm,
-                                            const uint4* __restrict__ gtab, float px, float py,
+                                            const float4* __restrict__ gtab, float px, float py,
                                             float pz) {
   switch (f.kind) {
     case BMF_FIELD_SPHERE_WAVE: {
@@ -260,11 +255,11 @@ __device__ __forceinline__ float eval_field(const FieldDev& f, const int* __rest
       float sum = 0.0f, amp = 1.0f, fr = f.p[2];
       for (int o = 0; o < oct; ++o) {
         const float n = perlin(perm, gtab, px * fr, py * fr, pz * fr);
-        sum = sum + amp * n;
+        sum = __fmaf_rn(amp, n, sum);
         fr = fr * f.p[3];
         amp = amp * f.p[4];
       }
-      return (py - f.p[0]) - f.p[1] * sum;
+      return __fmaf_rn(-f.p[1], sum, py - f.p[0]);
     }
     case BMF_FIELD_TORUS_Z: {  // ImplicitSampler.cpp:27-34
       const float r1 = f.p[0] / 4.0f, r2 = f.p[0] / 10.0f;

@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
                                                       uint32_t* __restrict__ words, uint32_t* __restrict__ flags) {
   extern __shared__ uint32_t sw[];
   __shared__ int perm2[512];
-  __shared__ uint4 gtab[512];
+  __shared__ float4 gtab[512];
   const int u = blockIdx.x;
   const int c = find_chunk(unit_start, n_chunks, u);
   const ChunkDev ch = chunks[c];
@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
   if (field.kind == BMF_FIELD_TERRAIN_FBM) {  // the noise tables; no other field reads them
     for (int i = threadIdx.x; i < 512; i += blockDim.x) {
       perm2[i] = field.perm[i & 255];
-      gtab[i] = seg_grad_code(field.perm[i & 255]);
+      gtab[i] = grad_coeffs(field.perm[i & 255]);
     }
   }
   for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = 0u;
@@ -160,7 +160,7 @@ __device__ __forceinline__ void oct_line_init(OctLine& s, float px, float py, fl
 
 // Enter z-lattice cell Z: when it is the next cell, the old layer-1 pair is
 // the new layer-0 pair; otherwise both layers are set up.
-__device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const uint4* __restrict__ gtab) {
+__device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const float4* __restrict__ gtab) {
   const int pA = (int)(s.p & 255u), pA1 = (int)((s.p >> 8) & 255u), pB = (int)((s.p >> 16) & 255u),
             pB1 = (int)(s.p >> 24);
   const float x1 = s.xf - 1.0f, y1 = s.yf - 1.0f;
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
                                                              uint32_t* __restrict__ words,
                                                              uint32_t* __restrict__ flags) {
   __shared__ int perm2[512];
-  __shared__ uint4 gtab[512];
+  __shared__ float4 gtab[512];
   __shared__ float4 zt[kZtEntries];
   // density of the CTA's lines for one 16-sample half block, flushed with
   // coalesced 64-byte row stores (rows padded to 17: conflict-free columns)
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
   __shared__ int s_item;
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
     perm2[i] = field.perm[i & 255];
-    gtab[i] = seg_grad_code(field.perm[i & 255]);
+    gtab[i] = grad_coeffs(field.perm[i & 255]);
   }
   const int oct = min((int)field.p[5], kMaxOctaves);
   const float h0 = field.p[0], ampl = field.p[1], freq = field.p[2], lac = field.p[3], gain = field.p[4];
@@ -285,9 +285,9 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
             const float4 t = zo[k];
             const int Z = __float_as_int(t.w);
             if (Z != L.Zp) oct_line_cell(L, Z, gtab);  // same for every lane of the CTA
-            const float l0 = L.a0 + L.b0 * t.x;
-            const float l1 = L.a1 + L.b1 * t.y;
-            sum[k] = sum[k] + amp * (l0 + t.z * (l1 - l0));
+            const float l0 = __fmaf_rn(L.b0, t.x, L.a0);
+            const float l1 = __fmaf_rn(L.b1, t.y, L.a1);
+            sum[k] = __fmaf_rn(amp, __fmaf_rn(t.z, l1 - l0, l0), sum[k]);
           }
           if (cache) {
             s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         }
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) {
-          const float d = (py - h0) - ampl * sum[k];
+          const float d = __fmaf_rn(-ampl, sum[k], py - h0);
           row[k] = d;
           if (d < 0.0f) bits |= 1u << k;
         }
@@ -324,9 +324,9 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
             const float4 t = zt[o * zt_o + zt_k + k];
             const int Z = __float_as_int(t.w);
             if (Z != L.Zp) oct_line_cell(L, Z, gtab);
-            const float l0 = L.a0 + L.b0 * t.x;
-            const float l1 = L.a1 + L.b1 * t.y;
-            sum = sum + amp * (l0 + t.z * (l1 - l0));
+            const float l0 = __fmaf_rn(L.b0, t.x, L.a0);
+            const float l1 = __fmaf_rn(L.b1, t.y, L.a1);
+            sum = __fmaf_rn(amp, __fmaf_rn(t.z, l1 - l0, l0), sum);
             if (cache && k + 1 < n) {
               s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
               s_zp[si] = L.Zp;
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
             fr = fr * lac;
             amp = amp * gain;
           }
-          const float d = (py - h0) - ampl * sum;
+          const float d = __fmaf_rn(-ampl, sum, py - h0);
           row[k] = d;
           if (d < 0.0f) bits |= 1u << k;
         }

@@ -117,21 +117,41 @@ float bmfo_perlin_textbook(const uint8_t perm[256], float x, float y, float z) {
   return lerpf(w, l0, l1);
 }
 
-/* Gradient of hash h split into its x/y part s and its z coefficient c:
- * grad(h, x, y, z) = s + c * z exactly, with s = (+/-u) + (+/-v) and c = +0
- * when v is x or y, and s = +/-u and c = +/-1 when v is z (u is never z). */
-static void grad_split(int h, float x, float y, float* s, float* c) {
+/* The line-separable noise evaluates with fused multiply-adds (fmaf, one
+ * rounding each) at fixed places: fade's two inner steps, every lerp
+ * a + t (b - a) = fmaf(t, b - a, a), a corner's s = fmaf(gy, y, gx * x), and
+ * l = fmaf(beta, zk, alpha).  The GPU kernels use __fmaf_rn at exactly these
+ * places, so the two agree bit for bit. */
+static float fade_fma(float t) {
+  float a = fmaf(t, 6.0f, -15.0f);
+  a = fmaf(t, a, 10.0f);
+  float t3 = t * t;
+  t3 = t3 * t;
+  return t3 * a;
+}
+static float lerp_fma(float t, float a, float b) { return fmaf(t, b - a, a); }
+
+/* Gradient of hash h split into an x/y part and a z coefficient:
+ * grad(h, x, y, z) = gx * x + gy * y + c * z with gx, gy, c in {0, +1, -1};
+ * u (x for h < 8, else y) and v (y for h < 4, x for h = 12 or 14, else z) are
+ * never the same axis, so s = gx * x + gy * y is the textbook (+/-u) + (+/-v)
+ * (or +/-u when v is z) with one rounding, up to the sign of an exact zero. */
+static void grad_split(int h, float* gx, float* gy, float* c) {
   h &= 15;
-  float u = h < 8 ? x : y;
-  u = (h & 1) ? -u : u;
-  if (h < 4 || h == 12 || h == 14) {
-    float v = h < 4 ? y : x;
-    *s = u + ((h & 2) ? -v : v);
-    *c = 0.0f;
-  } else {
-    *s = u;
-    *c = (h & 2) ? -1.0f : 1.0f;
-  }
+  const float su = (h & 1) ? -1.0f : 1.0f, sv = (h & 2) ? -1.0f : 1.0f;
+  *gx = 0.0f;
+  *gy = 0.0f;
+  *c = 0.0f;
+  if (h < 8) *gx = su; else *gy = su;
+  if (h < 4) *gy = sv;
+  else if (h == 12 || h == 14) *gx = sv;
+  else *c = sv;
+}
+
+static void corner_sc(int h, float x, float y, float* s, float* c) {
+  float gx, gy;
+  grad_split(h, &gx, &gy, c);
+  *s = fmaf(gy, y, gx * x);
 }
 
 /* One z-layer of the cell: the x/y lerps of the four corners' s and c parts.
@@ -140,13 +160,13 @@ static void layer_coeffs(const uint8_t perm[256], int AAk, int ABk, int BAk, int
                          float y1, float u, float v, float* alpha, float* beta) {
 #define P(i) ((int)perm[(i) & 255])
   float s00, c00, s10, c10, s01, c01, s11, c11;
-  grad_split(P(AAk), x, y, &s00, &c00);
-  grad_split(P(BAk), x1, y, &s10, &c10);
-  grad_split(P(ABk), x, y1, &s01, &c01);
-  grad_split(P(BBk), x1, y1, &s11, &c11);
+  corner_sc(P(AAk), x, y, &s00, &c00);
+  corner_sc(P(BAk), x1, y, &s10, &c10);
+  corner_sc(P(ABk), x, y1, &s01, &c01);
+  corner_sc(P(BBk), x1, y1, &s11, &c11);
 #undef P
-  *alpha = lerpf(v, lerpf(u, s00, s10), lerpf(u, s01, s11));
-  *beta = lerpf(v, lerpf(u, c00, c10), lerpf(u, c01, c11));
+  *alpha = lerp_fma(v, lerp_fma(u, s00, s10), lerp_fma(u, s01, s11));
+  *beta = lerp_fma(v, lerp_fma(u, c00, c10), lerp_fma(u, c01, c11));
 }
 
 /* Improved gradient noise in line-separable form.  Each corner gradient is
@@ -156,16 +176,16 @@ static void layer_coeffs(const uint8_t perm[256], int AAk, int ABk, int BAk, int
  * In exact arithmetic this is the textbook value; in float it differs from it
  * by rounding only.  alpha and beta depend on x, y and the lattice cell Z, not
  * on the sample's own z, so a kernel walking a z-line sets them up once per
- * lattice cell and spends nine operations per sample and octave.  The layer-1
- * coefficients of cell Z are the layer-0 coefficients of cell Z + 1 (same
- * hashes, same operations). */
+ * lattice cell and spends five operations per sample and octave (four fused).
+ * The layer-1 coefficients of cell Z are the layer-0 coefficients of cell
+ * Z + 1 (same hashes, same operations). */
 float bmfo_perlin(const uint8_t perm[256], float x, float y, float z) {
   float fx = floorf(x), fy = floorf(y), fz = floorf(z);
   int X = ((int)fx) & 255, Y = ((int)fy) & 255, Z = ((int)fz) & 255;
   x = x - fx;
   y = y - fy;
   z = z - fz;
-  float u = fade(x), v = fade(y), w = fade(z);
+  float u = fade_fma(x), v = fade_fma(y), w = fade_fma(z);
 #define P(i) ((int)perm[(i) & 255])
   int A = P(X) + Y, AA = P(A) + Z, AB = P(A + 1) + Z;
   int B = P(X + 1) + Y, BA = P(B) + Z, BB = P(B + 1) + Z;
@@ -174,9 +194,9 @@ float bmfo_perlin(const uint8_t perm[256], float x, float y, float z) {
   float a0, b0, a1, b1;
   layer_coeffs(perm, AA, AB, BA, BB, x, y, x1, y1, u, v, &a0, &b0);
   layer_coeffs(perm, AA + 1, AB + 1, BA + 1, BB + 1, x, y, x1, y1, u, v, &a1, &b1);
-  float l0 = a0 + b0 * z;
-  float l1 = a1 + b1 * z1;
-  return l0 + w * (l1 - l0);
+  float l0 = fmaf(b0, z, a0);
+  float l1 = fmaf(b1, z1, a1);
+  return fmaf(w, l1 - l0, l0);
 }
 
 float bmfo_fbm(const uint8_t perm[256], float x, float y, float z, int octaves, float freq, float lacunarity,
@@ -184,7 +204,7 @@ float bmfo_fbm(const uint8_t perm[256], float x, float y, float z, int octaves, 
   float sum = 0.0f, amp = 1.0f, f = freq;
   for (int o = 0; o < octaves; ++o) {
     float n = bmfo_perlin(perm, x * f, y * f, z * f);
-    sum = sum + amp * n;
+    sum = fmaf(amp, n, sum);
     f = f * lacunarity;
     amp = amp * gain;
   }
@@ -242,7 +262,7 @@ void bmfo_fill_field(int kind, const float* params, int dim, const float origin[
           v = (l - params[3]) + params[4] * s;
         } else if (kind == BMF_FIELD_TERRAIN_FBM) {
           float n = bmfo_fbm(perm, px, py, pz, (int)params[5], params[2], params[3], params[4]);
-          v = (py - params[0]) - params[1] * n;
+          v = fmaf(-params[1], n, py - params[0]);
         } else {
           v = ref_field(kind, params[0], px, py, pz);
         }

@@ -41,10 +41,10 @@ def test_struct_layouts_match_header():
 
 
 def test_fill_fp32_op_count():
-    """The bench's algorithmic FP32 count of the line-separable FBM: per sample
-    9 per octave + 2, plus per-line and per-layer set-up terms; on the
-    mixed-LOD update about 68 per sample, and a single 1-octave chunk inside one
-    z-lattice cell matches the closed form exactly."""
+    """The bench's algorithmic FP32 instruction count of the line-separable
+    FBM: per sample 5 per octave + 1, plus per-line and per-layer set-up terms;
+    on the mixed-LOD update about 45 per sample, and a single 1-octave chunk
+    inside one z-lattice cell matches the closed form exactly."""
     import os
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), ".."))
@@ -52,7 +52,7 @@ def test_fill_fp32_op_count():
     _, rows = workloads.lod_update()
     ops = bench.fill_fp32_ops(rows, workloads.TERRAIN_PARAMS)
     per_sample = ops / (rows[:, 4] ** 3).sum()
-    assert 60.0 < per_sample < 75.0, per_sample
+    assert 40.0 < per_sample < 50.0, per_sample
     # one 33^3 chunk, one octave at a frequency that keeps every line in one cell
     params = (64.0, 40.0, 1e-4, 2.0, 0.5, 1, 1337)
     one = np.array([[0.0, 0.0, 0.0, 1.0, 33, 0]])
