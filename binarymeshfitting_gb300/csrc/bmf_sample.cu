@@ -136,10 +136,10 @@ constexpr int kZtEntries = 1024;
 static_assert(kZtEntries >= kMaxOctaves * kMaxFillRun, "per-run z terms fit");
 
 // Per (line, octave) state of the line walk: the x/y terms, the four hash
-// bases (bytes of p), and the alpha / beta pairs of the current z-lattice cell Zp.
+// bases, and the alpha / beta pairs of the current z-lattice cell Zp.
 struct OctLine {
   float xf, yf, u, v, a0, b0, a1, b1;
-  uint32_t p;
+  int pA, pA1, pB, pB1;
   int Zp;
 };
 
@@ -153,16 +153,17 @@ __device__ __forceinline__ void oct_line_init(OctLine& s, float px, float py, fl
   s.u = fade(s.xf);
   s.v = fade(s.yf);
   const int A = perm2[X] + Y, B = perm2[X + 1] + Y;
-  s.p = (uint32_t)perm2[A] | ((uint32_t)perm2[A + 1] << 8) | ((uint32_t)perm2[B] << 16) |
-        ((uint32_t)perm2[B + 1] << 24);
+  s.pA = perm2[A];
+  s.pA1 = perm2[A + 1];
+  s.pB = perm2[B];
+  s.pB1 = perm2[B + 1];
   s.Zp = -1;
 }
 
 // Enter z-lattice cell Z: when it is the next cell, the old layer-1 pair is
 // the new layer-0 pair; otherwise both layers are set up.
 __device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const float4* __restrict__ gtab) {
-  const int pA = (int)(s.p & 255u), pA1 = (int)((s.p >> 8) & 255u), pB = (int)((s.p >> 16) & 255u),
-            pB1 = (int)(s.p >> 24);
+  const int pA = s.pA, pA1 = s.pA1, pB = s.pB, pB1 = s.pB1;
   const float x1 = s.xf - 1.0f, y1 = s.yf - 1.0f;
   if (s.Zp >= 0 && Z == ((s.Zp + 1) & 255)) {
     s.a0 = s.a1;
@@ -351,12 +352,16 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         // 16-sample row segments per instruction
         __syncthreads();
         const int zh0 = z0 & ~15, nz = min(16, dim - zh0);
-        const int lane = threadIdx.x & 31, w0 = threadIdx.x & ~31, col = lane & 15;
-#pragma unroll 1
-        for (int j = 0; j < 32; j += 2) {
-          const int l = w0 + j + (lane >> 4);
-          if (item.y + l < dim * dim && col < nz)
-            dens_out[ch.dens + (int64_t)(item.y + l) * dim + zh0 + col] = s_stage[l * kStageRow + col];
+        const int lane = threadIdx.x & 31, col = lane & 15;
+        const int l0 = (int)(threadIdx.x & ~31) + (lane >> 4);  // this lane's first row
+        // rows left for this lane (every second row from l0), 0 past the chunk's lines or columns
+        const int nrow = col < nz ? min(16, (dim * dim - item.y - l0 + 1) >> 1) : 0;
+        float* gp = dens_out + ch.dens + (int64_t)(item.y + l0) * dim + zh0 + col;
+        const float* sp = s_stage + l0 * kStageRow + col;
+#pragma unroll 4
+        for (int j = 0; j < 16; ++j) {
+          if (j < nrow) *gp = sp[2 * kStageRow * j];
+          gp += 2 * dim;
         }
         __syncthreads();  // the next half block's rows overwrite the stage
       }
