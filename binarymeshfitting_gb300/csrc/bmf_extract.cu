@@ -838,7 +838,7 @@ void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const ui
 // the results are identical.
 // ---------------------------------------------------------------------------
 template <int MODE, int N>
-__global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
+__global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_ctas<MODE>()) k_sweep_chunks(
     const ChunkDev* __restrict__ chunks, const uint32_t* __restrict__ tot, const int* __restrict__ order,
     int n_chunks, int* __restrict__ queue, const uint32_t* __restrict__ words, WordScratch ws,
     const uint32_t* __restrict__ vkey, int64_t nv, int64_t n_prims, int64_t adj_cap,
@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
     uint32_t* __restrict__ adj, const uint8_t* __restrict__ boundary, const uint32_t* __restrict__ idx,
     float* __restrict__ pos, float* __restrict__ nrm, float* __restrict__ dual_p, float* __restrict__ dual_n,
     int iters, int process_boundary, int sn) {
-  constexpr int kWarps = kChunkSweepThreads / 32;
+  constexpr int kThreads = chunk_sweep_threads<MODE>(), kWarps = kThreads / 32;
   __shared__ SmemTabs T;
   __shared__ uint32_t s_warp[kWarps];
   __shared__ uint32_t s_total;
@@ -870,7 +870,7 @@ __global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
     // CSR offsets (MeshProcessor.cpp:32-40), blockDim vertices per pass;
     // vertex v is always handled by the same thread below
     uint32_t carry = (uint32_t)ch.iout;
-    for (int64_t b = v0; b < v1; b += kChunkSweepThreads) {
+    for (int64_t b = v0; b < v1; b += kThreads) {
       const int64_t v = b + threadIdx.x;
       const uint32_t x = v < v1 ? (uint32_t)__ldg(valence + v) : 0u;
       uint32_t incl = x;
@@ -898,7 +898,7 @@ __global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
       __syncthreads();
     }
     // adjacency, in each vertex's own CSR range and inside adj
-    for (int64_t v = v0 + threadIdx.x; v < v1; v += kChunkSweepThreads) {
+    for (int64_t v = v0 + threadIdx.x; v < v1; v += kThreads) {
       const uint32_t o = off[v];
       const int room = (int)max((int64_t)0, min((int64_t)__ldg(valence + v), adj_cap - (int64_t)o));
       adj_vertex<MODE>(T, ch, words, ws, __ldg(vkey + v), adj + o, room);
@@ -907,10 +907,10 @@ __global__ void __launch_bounds__(kChunkSweepThreads) k_sweep_chunks(
     for (int m = 0; m < iters; ++m) {
       const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
       const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
-      for (int64_t t = p0 + threadIdx.x; t < p1; t += kChunkSweepThreads)
+      for (int64_t t = p0 + threadIdx.x; t < p1; t += kThreads)
         dual_prim<N, true>(t, nvb, idx, pos, nrm, dual_p, dual_n, normal_mode);
       __syncthreads();
-      for (int64_t v = v0 + threadIdx.x; v < v1; v += kChunkSweepThreads)
+      for (int64_t v = v0 + threadIdx.x; v < v1; v += kThreads)
         primal_vertex<true>(v, n_prims, adj_cap, off, nullptr, valence, adj, boundary, dual_p, dual_n, pos, nrm,
                             process_boundary, sn, set_colors);
       __syncthreads();
@@ -927,7 +927,7 @@ static int sweep_chunks_grid() {
   if (grid[gi] == 0) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<MODE, N>, kChunkSweepThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<MODE, N>, chunk_sweep_threads<MODE>(), 0);
     grid[gi] = sms * (per_sm > 0 ? per_sm : 1);
   }
   return grid[gi];
@@ -940,7 +940,7 @@ void launch_sweep_chunks(const StructuredAdj& sa, int N, int64_t nv, int64_t n_p
   cudaMemsetAsync(sa.queue, 0, sizeof(int), st);
   const int64_t adj_cap = n_prims * N;
 #define BMF_SWEEP_CHUNKS(M, NN)                                                                                 \
-  k_sweep_chunks<M, NN><<<sweep_chunks_grid<M, NN>(), kChunkSweepThreads, 0, st>>>(                              \
+  k_sweep_chunks<M, NN><<<sweep_chunks_grid<M, NN>(), chunk_sweep_threads<M>(), 0, st>>>(                     \
       sa.chunks, sa.tot, sa.order, sa.n_chunks, sa.queue, sa.words, sa.ws, sa.vkey, nv, n_prims, adj_cap,        \
       d_counts, s.off, valence, s.adj, boundary, idx, pos, nrm, s.dual_p, s.dual_n, iters, process_boundary,      \
       smooth_normals)

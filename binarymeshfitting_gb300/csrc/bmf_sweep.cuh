@@ -7,8 +7,13 @@
 
 namespace bmf {
 
-// threads of the chunk-by-chunk sweep kernel's CTA
-constexpr int kChunkSweepThreads = 512;
+// Threads of the chunk-by-chunk sweep kernel's CTA and CTAs per SM: Mode R
+// at full occupancy (1024 x 2, 32 registers); Mode Q, whose adjacency keeps a
+// 12-entry list per vertex, at 512 threads without a register cap.
+template <int MODE>
+__host__ __device__ constexpr int chunk_sweep_threads() { return MODE == 0 ? 1024 : 512; }
+template <int MODE>
+__host__ __device__ constexpr int chunk_sweep_min_ctas() { return MODE == 0 ? 2 : 1; }
 
 // COH selects the load for data that the same kernel also writes (positions,
 // normals and dual values in the chunk-by-chunk kernel, which runs every
