@@ -281,9 +281,12 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
             L.Zp = s_zp[si];
           }
           const float4* zo = zt + o * zt_o + zt_k;
+          float4 tn = zo[0];
 #pragma unroll
           for (int k = 0; k < kFillRun; ++k) {
-            const float4 t = zo[k];
+            // the next sample's z terms load before this sample's cell set-up
+            const float4 t = tn;
+            if (k + 1 < kFillRun) tn = zo[k + 1];
             const int Z = __float_as_int(t.w);
             if (Z != L.Zp) oct_line_cell(L, Z, gtab);  // same for every lane of the CTA
             const float l0 = __fmaf_rn(L.b0, t.x, L.a0);

@@ -207,3 +207,47 @@ def test_fit_create_rejects_two_wide_adjoints(ctx):
     st = ctx.lib.bmf_fit_create(ctx.h, 1, DIM, L.PLACE_QEF, ITERS, 100000, 400000,
                                 L.FIT_ADJOINT_F64 | L.FIT_ADJOINT_DF, ctypes.byref(h))
     assert st == L.ERR_INVALID_ARGUMENT and not h.value
+
+
+def test_chunk_sweep_fit_matches_whole_mesh_fit(ctx):
+    """A fit plan of 2048 chunks or more runs its sweeps chunk by chunk, with
+    the CSR offsets and adjacency built inside that kernel; the backward reads
+    them.  The same chunks in two smaller plans (whole-mesh sweeps) give
+    bit-identical positions and indices, and the same density gradient up to
+    float32 reordering of the atomics (1e-5 of max|g|)."""
+    n, dim = 2100, 13
+    g = np.arange(dim, dtype=np.float64)
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    rng = np.random.default_rng(31)
+    radii = rng.uniform(3.0, 5.5, n)
+    base = np.sqrt((X - 6) ** 2 + (Y - 6) ** 2 + (Z - 6) ** 2).reshape(1, -1)
+    dens = (base - radii[:, None] + rng.normal(0, 0.1, (n, dim ** 3))).astype(np.float32)
+    dd = torch.from_numpy(dens.reshape(-1)).cuda()
+
+    def run(lo, hi):
+        plan = FitPlan(ctx, hi - lo, dim, L.PLACE_QEF, ITERS)
+        pos, idx, info = plan.forward(dd[lo * dim ** 3: hi * dim ** 3].contiguous())
+        pos, idx, info = pos.clone(), idx.clone(), info.clone()
+        w = torch.sin(torch.arange(pos.numel(), device=pos.device, dtype=torch.float32) * 0.37).view(-1, 3)
+        grad = plan.backward(w).clone()
+        plan.close()
+        return pos, idx, info, grad
+
+    pos, idx, info, grad = run(0, n)
+    parts = [run(0, 1000), run(1000, n)]
+    assert info[:, 1].sum().item() == pos.shape[0] and (info[:, 4] > 0).sum().item() > n // 2
+    assert torch.equal(pos.view(torch.int32), torch.cat([p[0] for p in parts]).view(torch.int32))
+    # indices are chunk-local: the two plans' concatenation is the big plan's
+    assert torch.equal(idx, torch.cat([p[1] for p in parts]))
+    # the weights restart at vertex 0 in each part: compare each part's chunks
+    # with a big-plan backward whose weights restart the same way
+    nv0 = parts[0][0].shape[0]
+    plan = FitPlan(ctx, n, dim, L.PLACE_QEF, ITERS)
+    plan.forward(dd)
+    w = torch.cat([torch.sin(torch.arange(p[0].numel(), device=dd.device, dtype=torch.float32) * 0.37).view(-1, 3)
+                   for p in parts])
+    gb = plan.backward(w).double().cpu().numpy()
+    plan.close()
+    gs = torch.cat([p[3] for p in parts]).double().cpu().numpy()
+    assert nv0 > 0 and np.abs(gs).max() > 0
+    assert np.abs(gb - gs).max() <= 1e-5 * np.abs(gs).max()
