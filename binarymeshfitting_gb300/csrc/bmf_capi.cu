@@ -639,7 +639,8 @@ bmf_status batch_proc_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   BMF_CUDA(ctx, cudaMalloc(&b->ps.off, sizeof(uint32_t) * (vcap + 1)));
   BMF_CUDA(ctx, cudaMalloc(&b->ps.cursor, sizeof(uint32_t) * (vcap + 1)));
   BMF_CUDA(ctx, cudaMalloc(&b->ps.adj, sizeof(uint32_t) * (np * N + 1)));
-  BMF_CUDA(ctx, cudaMalloc(&b->ps.dual_p, sizeof(float) * (3 * np + 3)));
+  // 4 floats per primitive: the chunk-by-chunk sweeps keep (p, n.x) as one float4
+  BMF_CUDA(ctx, cudaMalloc(&b->ps.dual_p, sizeof(float) * (4 * np + 4)));
   BMF_CUDA(ctx, cudaMalloc(&b->ps.dual_n, sizeof(float) * (3 * np + 3)));
   BMF_CUDA(ctx, cudaMalloc(&b->ps.tmp, sizeof(uint32_t) * (vcap / 4096 + 2)));
   BMF_CUDA(ctx, cudaMalloc(&b->d_idxg, sizeof(uint32_t) * (icap + 1)));
@@ -1050,7 +1051,7 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
             cudaMalloc(&f->ws.gpl, sizeof(uint32_t) * 3 * words) == cudaSuccess &&
             cudaMalloc(&f->ps.off, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&
             cudaMalloc(&f->ps.adj, sizeof(uint32_t) * (np * 4 + 1)) == cudaSuccess &&
-            cudaMalloc(&f->ps.dual_p, sizeof(float) * (3 * np + 3)) == cudaSuccess &&
+            cudaMalloc(&f->ps.dual_p, sizeof(float) * (4 * np + 4)) == cudaSuccess &&
             cudaMalloc(&f->ps.tmp, sizeof(uint32_t) * (vcap / 4096 + 2)) == cudaSuccess &&
             cudaMalloc(&f->d_idxg, sizeof(uint32_t) * (icap + 1)) == cudaSuccess &&
             cudaMalloc(&f->d_vkey, sizeof(uint32_t) * (vcap + 1)) == cudaSuccess &&

@@ -908,10 +908,10 @@ __global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_c
       const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
       const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
       for (int64_t t = p0 + threadIdx.x; t < p1; t += kThreads)
-        dual_prim<N, true>(t, nvb, idx, pos, nrm, dual_p, dual_n, normal_mode);
+        dual_prim<N, true, true>(t, nvb, idx, pos, nrm, dual_p, dual_n, normal_mode);
       __syncthreads();
       for (int64_t v = v0 + threadIdx.x; v < v1; v += kThreads)
-        primal_vertex<true>(v, n_prims, adj_cap, off, nullptr, valence, adj, boundary, dual_p, dual_n, pos, nrm,
+        primal_vertex<true, true>(v, n_prims, adj_cap, off, nullptr, valence, adj, boundary, dual_p, dual_n, pos, nrm,
                             process_boundary, sn, set_colors);
       __syncthreads();
     }

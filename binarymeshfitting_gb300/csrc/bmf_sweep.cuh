@@ -39,8 +39,11 @@ __device__ __forceinline__ void cross3(const float a[3], const float b[3], float
 }
 
 // optimize_dual_grid body (MeshProcessor.cpp:142-227).  normal_mode: 0 none,
-// 1 face normal, 2 sum of vertex normals.
-template <int N, bool COH = false>
+// 1 face normal, 2 sum of vertex normals.  PACKED: primitive t's dual point
+// and normal go to ((float4*)dual_p)[t] = (p, n.x) and ((float2*)dual_n)[t] =
+// (n.y, n.z) -- one 16-byte and one 8-byte gather per primitive in the primal
+// step instead of six 4-byte ones; the values are the same.
+template <int N, bool COH = false, bool PACKED = false>
 __device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t* __restrict__ idx,
                                           const float* __restrict__ pos, const float* __restrict__ nrm,
                                           float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
@@ -57,8 +60,16 @@ __device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t
     for (int c = 0; c < 3; ++c) p[c] = p[c] + sweep_ld<COH>(pos + 3 * v[k] + c);
   }
 #pragma unroll
-  for (int c = 0; c < 3; ++c) dual_p[3 * t + c] = p[c] / (float)N;
-  if (normal_mode == 0) return;
+  for (int c = 0; c < 3; ++c) p[c] = p[c] / (float)N;
+  if (normal_mode == 0) {
+    if (PACKED) {
+      reinterpret_cast<float4*>(dual_p)[t] = make_float4(p[0], p[1], p[2], 0.0f);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) dual_p[3 * t + c] = p[c];
+    }
+    return;
+  }
   float o[3];
   if (normal_mode == 1) {
     if (N == 3) {
@@ -112,11 +123,18 @@ __device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t
       for (int c = 0; c < 3; ++c) o[c] = o[c] + sweep_ld<COH>(nrm + 3 * v[k] + c);
     }
   }
+  if (PACKED) {
+    reinterpret_cast<float4*>(dual_p)[t] = make_float4(p[0], p[1], p[2], o[0]);
+    reinterpret_cast<float2*>(dual_n)[t] = make_float2(o[1], o[2]);
+  } else {
 #pragma unroll
-  for (int c = 0; c < 3; ++c) dual_n[3 * t + c] = o[c];
+    for (int c = 0; c < 3; ++c) dual_p[3 * t + c] = p[c];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) dual_n[3 * t + c] = o[c];
+  }
 }
 
-template <bool COH = false>
+template <bool COH = false, bool PACKED = false>
 __device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t adj_cap,
                                               const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
                                               const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
@@ -135,11 +153,24 @@ __device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t
   for (uint32_t k = 0; k < n; ++k) {
     const uint32_t t = sweep_ld<COH>(a + k);
     if ((int64_t)t >= np_lim) continue;  // never read past the dual points
+    if (PACKED) {
+      const float4 q = sweep_ld<COH>(reinterpret_cast<const float4*>(dual_p) + t);
+      p[0] = p[0] + q.x;
+      p[1] = p[1] + q.y;
+      p[2] = p[2] + q.z;
+      if (smooth_normals) {
+        const float2 r = sweep_ld<COH>(reinterpret_cast<const float2*>(dual_n) + t);
+        nn[0] = nn[0] + q.w;
+        nn[1] = nn[1] + r.x;
+        nn[2] = nn[2] + r.y;
+      }
+    } else {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) p[c] = p[c] + sweep_ld<COH>(dual_p + 3 * t + c);
-    if (smooth_normals) {
+      for (int c = 0; c < 3; ++c) p[c] = p[c] + sweep_ld<COH>(dual_p + 3 * t + c);
+      if (smooth_normals) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) nn[c] = nn[c] + sweep_ld<COH>(dual_n + 3 * t + c);
+        for (int c = 0; c < 3; ++c) nn[c] = nn[c] + sweep_ld<COH>(dual_n + 3 * t + c);
+      }
     }
   }
   const float cnt = (float)n;
