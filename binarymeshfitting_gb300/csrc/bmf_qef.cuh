@@ -422,6 +422,16 @@ __device__ void eig3_refine(const R A[3][3], const float V0[3][3], R w[3], R V[3
 
 // LIST = 0: every vertex; 1: every vertex, but QEF-placed ones are only
 // appended to qlist (for a dense second pass); 2: the vertices of qlist.
+// The edges of cell-mask group g as a 12-bit set.  The adjoint loops walk
+// it in ascending edge order (the order of the forward's accumulation): each
+// lane runs only its own vertex's edges, not the union of the warp's.
+__device__ __forceinline__ uint32_t group_edges(int mask, int g) {
+  uint32_t m = 0u;
+#pragma unroll
+  for (int e = 0; e < 12; ++e) m |= (group_of(mask, e) == g ? 1u : 0u) << e;
+  return m;
+}
+
 template <int PLACE, typename T, int LIST>
 __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ chunks, int n_chunks,
                                                    const uint32_t* __restrict__ words, const float* __restrict__ dens,
@@ -446,6 +456,7 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
   int x, y, z, g;
   vertex_key_decode(vkey[v], x, y, z, g);
   const int mask = cell_mask_at(W, dim, zc, x, y, z);
+  const uint32_t edges = group_edges(mask, g);
   const T gx[3] = {(T)grad_pos[3 * v], (T)grad_pos[3 * v + 1], (T)grad_pos[3 * v + 2]};
   int cnt = 0;
   bool use_qef = false;
@@ -456,7 +467,7 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
     // a listed vertex is QEF-placed (the first pass's exact FP32 replay
     // decided it) and its FP32 eigenvectors, which seed the wide re-solve, were
     // kept by that pass
-    for (int e = 0; e < 12; ++e) cnt += group_of(mask, e) == g;
+    cnt = __popc(edges);
     if (cnt == 0) return;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
@@ -467,8 +478,8 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
   } else {
     // the forward's branch: replay of q_place in FP32
     if (PLACE == 2) q.init();
-    for (int e = 0; e < 12; ++e) {
-      if (group_of(mask, e) != g) continue;
+    for (uint32_t em = edges; em; em &= em - 1u) {
+      const int e = __ffs(em) - 1;
       float p[3], n[3];
       hermite(D, dim, x, y, z, e, PLACE == 2, p, n);
       ++cnt;
@@ -512,8 +523,8 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
         // point, converged eigen pairs
         T A[3][3] = {{T(0.0f), T(0.0f), T(0.0f)}, {T(0.0f), T(0.0f), T(0.0f)}, {T(0.0f), T(0.0f), T(0.0f)}};
         T b[3] = {T(0.0f), T(0.0f), T(0.0f)}, m[3] = {T(0.0f), T(0.0f), T(0.0f)};
-        for (int e = 0; e < 12; ++e) {
-          if (group_of(mask, e) != g) continue;
+        for (uint32_t em = edges; em; em &= em - 1u) {
+          const int e = __ffs(em) - 1;
           HermiteT<T> h;
           hermite_t<T>(D, dim, x, y, z, e, true, h);
           const T d = h.n[0] * h.p[0] + h.n[1] * h.p[1] + h.n[2] * h.p[2];
@@ -624,8 +635,8 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
   }
   const float inv_cnt = 1.0f / (float)cnt;
   // per hermite pair: g_p, g_n, then into the density
-  for (int e = 0; e < 12; ++e) {
-    if (group_of(mask, e) != g) continue;
+  for (uint32_t em = edges; em; em &= em - 1u) {
+    const int e = __ffs(em) - 1;
     HermiteT<float> h;
     hermite_t<float>(D, dim, x, y, z, e, PLACE == 2, h);
     const int ax = e >> 2;
