@@ -420,8 +420,6 @@ __device__ void eig3_refine(const R A[3][3], const float V0[3][3], R w[3], R V[3
   for (int i = 0; i < 3; ++i) w[i] = B[i][i];
 }
 
-// LIST = 0: every vertex; 1: every vertex, but QEF-placed ones are only
-// appended to qlist (for a dense second pass); 2: the vertices of qlist.
 // The edges of cell-mask group g as a 12-bit set.  The adjoint loops walk
 // it in ascending edge order (the order of the forward's accumulation): each
 // lane runs only its own vertex's edges, not the union of the warp's.
@@ -432,6 +430,8 @@ __device__ __forceinline__ uint32_t group_edges(int mask, int g) {
   return m;
 }
 
+// LIST = 0: every vertex; 1: every vertex, but QEF-placed ones are only
+// appended to qlist (for a dense second pass); 2: the vertices of qlist.
 template <int PLACE, typename T, int LIST>
 __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ chunks, int n_chunks,
                                                    const uint32_t* __restrict__ words, const float* __restrict__ dens,
