@@ -24,6 +24,9 @@ constexpr int kMaxDim = 512;
 // chunk needs several chunks per resident CTA (~450 on a GB300) to balance
 // (measured: 4096 mixed chunks gain 3 %, 512 equal chunks lose 3 %)
 constexpr int kChunkSweepMinChunks = 2048;
+// fit plans: the adjoint sweeps run chunk by chunk from this many chunks (one
+// 512-thread CTA per chunk, four per SM)
+constexpr int kChunkSweepBwdMinChunks = 256;
 
 struct DevBuf {
   void* p = nullptr;
@@ -1133,8 +1136,15 @@ bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_
   BMF_CUDA(ctx, cudaMemsetAsync(f->d_g, 0, sizeof(float) * 3 * f->vcap, st));
   if (ng > 0)
     BMF_CUDA(ctx, cudaMemcpyAsync(f->d_g, d_grad_pos, sizeof(float) * 3 * ng, cudaMemcpyDeviceToDevice, st));
+  // with enough chunks to fill the GPU the adjoint sweeps run chunk by chunk
+  StructuredAdj sa{BMF_MODE_Q, f->d_chunks, f->n, f->d_words, f->ws, f->d_vkey};
+  if (f->n >= kChunkSweepBwdMinChunks) {
+    sa.tot = f->d_tot;
+    sa.order = f->d_order;
+    sa.queue = f->d_pqueue;
+  }
   int k = launch_process_bwd(4, f->vcap, f->icap / 4, f->d_totals, f->d_boundary, f->d_valence, f->d_idxg, f->iters,
-                             0, f->ps, f->d_g, st);
+                             0, f->ps, f->d_g, &sa, st);
   BMF_CUDA(ctx, cudaMemsetAsync(d_grad_density, 0, sizeof(float) * (size_t)f->n * f->dim * f->dim * f->dim, st));
   const int wide = (f->flags & BMF_FIT_ADJOINT_F64) ? 1 : ((f->flags & BMF_FIT_ADJOINT_DF) ? 2 : 0);
   launch_place_bwd(f->placement, wide, f->d_chunks, f->n, f->d_words, f->last_density, f->d_vkey, f->d_totals,

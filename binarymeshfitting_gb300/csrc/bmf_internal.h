@@ -139,7 +139,7 @@ int launch_format(const ChunkDev* d_chunks, int n_chunks, int64_t nv, int64_t ni
 // dL/d(initial positions) on return.  Returns the number of kernels launched.
 int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, const uint8_t* boundary,
                        const uint8_t* valence, const uint32_t* idx, int iters, int process_boundary,
-                       const ProcessScratch& s, float* g, cudaStream_t st);
+                       const ProcessScratch& s, float* g, const StructuredAdj* sa, cudaStream_t st);
 // Adjoint of Mode Q placement (placement 1 mass point, 2 QEF; f64: the QEF
 // derivative from an FP64 re-solve); accumulates into grad_dens (the caller
 // clears it).

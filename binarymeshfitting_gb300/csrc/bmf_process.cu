@@ -327,10 +327,100 @@ __global__ void k_dual_bwd(int N, int64_t nv, int64_t n_prims, int64_t adj_cap, 
   for (int c = 0; c < 3; ++c) g[3 * v + c] = s[c];
 }
 
+// Both transposes chunk by chunk: one CTA per chunk (from the queue) runs
+// every backward step of its chunk with block barriers in between -- a
+// chunk's primitives only read its own vertices and the reverse.  Per item the
+// operations are those of k_primal_bwd / k_dual_bwd, so the results are the
+// same; g and g_dual, which the kernel itself writes, are read with coherent
+// L1 loads.
+constexpr int kBwdChunkThreads = 512;
+
+template <int N>
+__global__ void __launch_bounds__(kBwdChunkThreads, 4) k_sweep_bwd_chunks(
+    const ChunkDev* __restrict__ chunks, const uint32_t* __restrict__ tot, const int* __restrict__ order,
+    int n_chunks, int* __restrict__ queue, int64_t nv, int64_t n_prims, int64_t adj_cap,
+    const int64_t* __restrict__ d_counts, const uint32_t* __restrict__ off, const uint8_t* __restrict__ valence,
+    const uint32_t* __restrict__ adj, const uint8_t* __restrict__ boundary, int process_boundary,
+    const uint32_t* __restrict__ idx, float* __restrict__ g, float* __restrict__ g_dual, int iters) {
+  __shared__ int s_item;
+  const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
+  const int64_t npb = d_counts ? min(n_prims, d_counts[1] / N) : n_prims;
+  const float invN = 1.0f / (float)N;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(queue, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();  // everyone has read s_item before thread 0 takes the next
+    if (it >= n_chunks) break;
+    const int c = order[it];
+    const int64_t v0 = chunks[c].vout, v1 = min(v0 + (int64_t)tot[2 * c], nvb);
+    const int64_t p0 = chunks[c].iout / N, p1 = min((chunks[c].iout + (int64_t)tot[2 * c + 1]) / N, npb);
+    for (int m = iters - 1; m >= 0; --m) {
+      for (int64_t t = p0 + threadIdx.x; t < p1; t += kBwdChunkThreads) {
+        float sd[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+          const uint32_t v = __ldg(idx + N * t + k);
+          if ((int64_t)v >= nvb || !primal_updates(valence, boundary, v, process_boundary)) continue;
+          const float inv = 1.0f / (float)valence[v];
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) sd[cc] += __ldca(g + 3 * v + cc) * inv;
+        }
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) g_dual[3 * t + cc] = sd[cc];
+      }
+      __syncthreads();
+      for (int64_t v = v0 + threadIdx.x; v < v1; v += kBwdChunkThreads) {
+        const int64_t room = adj_cap - (int64_t)off[v];
+        const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)valence[v], room));
+        float sv[3] = {0.0f, 0.0f, 0.0f};
+        if (!primal_updates(valence, boundary, v, process_boundary)) {
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) sv[cc] = g[3 * v + cc];
+        }
+        for (uint32_t k = 0; k < n; ++k) {
+          const uint32_t t = __ldg(adj + off[v] + k);
+          if ((int64_t)t >= n_prims) continue;
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc) sv[cc] += __ldca(g_dual + 3 * t + cc) * invN;
+        }
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) g[3 * v + cc] = sv[cc];
+      }
+      __syncthreads();
+    }
+  }
+}
+
 int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_counts, const uint8_t* boundary,
                        const uint8_t* valence, const uint32_t* idx, int iters, int process_boundary,
-                       const ProcessScratch& s, float* g, cudaStream_t st) {
+                       const ProcessScratch& s, float* g, const StructuredAdj* sa, cudaStream_t st) {
   if (nv == 0 || n_prims == 0 || iters <= 0) return 0;
+  if (sa && sa->tot && sa->order && sa->queue) {
+    static int grid[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int gi = dev >= 0 && dev < 64 ? dev : 0;
+    if (grid[gi] == 0) {
+      int sms = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (N == 3)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_bwd_chunks<3>, kBwdChunkThreads, 0);
+      else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_bwd_chunks<4>, kBwdChunkThreads, 0);
+      grid[gi] = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    cudaMemsetAsync(sa->queue, 0, sizeof(int), st);
+    if (N == 3)
+      k_sweep_bwd_chunks<3><<<grid[gi], kBwdChunkThreads, 0, st>>>(
+          sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_prims * N, d_counts, s.off,
+          valence, s.adj, boundary, process_boundary, idx, g, s.dual_p, iters);
+    else
+      k_sweep_bwd_chunks<4><<<grid[gi], kBwdChunkThreads, 0, st>>>(
+          sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_prims * N, d_counts, s.off,
+          valence, s.adj, boundary, process_boundary, idx, g, s.dual_p, iters);
+    return 1;
+  }
   const int vb = (int)((nv + 255) / 256), pb = (int)((n_prims + 255) / 256);
   for (int m = iters - 1; m >= 0; --m) {
     if (N == 3)

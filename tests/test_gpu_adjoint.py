@@ -210,11 +210,13 @@ def test_fit_create_rejects_two_wide_adjoints(ctx):
 
 
 def test_chunk_sweep_fit_matches_whole_mesh_fit(ctx):
-    """A fit plan of 2048 chunks or more runs its sweeps chunk by chunk, with
-    the CSR offsets and adjacency built inside that kernel; the backward reads
-    them.  The same chunks in two smaller plans (whole-mesh sweeps) give
-    bit-identical positions and indices, and the same density gradient up to
-    float32 reordering of the atomics (1e-5 of max|g|)."""
+    """A fit plan of 2048 chunks or more runs its forward sweeps chunk by
+    chunk, with the CSR offsets and adjacency built inside that kernel, and
+    from 256 chunks its adjoint sweeps too.  The same chunks in a 100-chunk
+    plan (whole-mesh forward and adjoint sweeps) and a 2000-chunk plan
+    (whole-mesh forward, chunk-by-chunk adjoint) give bit-identical positions
+    and indices, and the same density gradient up to float32 reordering of the
+    QEF adjoint's atomics (1e-5 of max|g|)."""
     n, dim = 2100, 13
     g = np.arange(dim, dtype=np.float64)
     X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
@@ -234,7 +236,7 @@ def test_chunk_sweep_fit_matches_whole_mesh_fit(ctx):
         return pos, idx, info, grad
 
     pos, idx, info, grad = run(0, n)
-    parts = [run(0, 1000), run(1000, n)]
+    parts = [run(0, 100), run(100, n)]
     assert info[:, 1].sum().item() == pos.shape[0] and (info[:, 4] > 0).sum().item() > n // 2
     assert torch.equal(pos.view(torch.int32), torch.cat([p[0] for p in parts]).view(torch.int32))
     # indices are chunk-local: the two plans' concatenation is the big plan's
