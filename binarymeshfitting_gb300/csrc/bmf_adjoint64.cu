@@ -16,10 +16,10 @@ void launch_place_bwd_wide_list(int wide, const ChunkDev* d_chunks, int n_chunks
   if (blocks == 0) return;
   if (wide == 2)
     k_place_bwd<2, DF, 2><<<blocks, 128, 0, st>>>(d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos,
-                                                  grad_dens, qlist, qcount, qseed);
+                                                  grad_dens, qlist, qcount, qseed, nullptr);
   else
     k_place_bwd<2, double, 2><<<blocks, 128, 0, st>>>(d_chunks, n_chunks, words, dens, vkey, d_counts, vcap,
-                                                      grad_pos, grad_dens, qlist, qcount, qseed);
+                                                      grad_pos, grad_dens, qlist, qcount, qseed, nullptr);
 }
 
 }  // namespace bmf

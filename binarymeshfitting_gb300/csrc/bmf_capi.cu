@@ -987,8 +987,9 @@ struct bmf_fit {
   float* d_g = nullptr;           // position-gradient work buffer
   int* d_order = nullptr;         // chunk order of the chunk-by-chunk sweeps (identity) and its queue
   int* d_pqueue = nullptr;
-  uint32_t* d_qlist = nullptr;    // QEF-placed vertices of the wide backward (+ counter at [vcap])
-  float* d_qseed = nullptr;       // their FP32 eigenvectors from the first backward pass (9 per entry)
+  uint32_t* d_qlist = nullptr;    // QEF-placed vertices of the forward, for the wide backward (+ counter at [vcap])
+  float* d_qseed = nullptr;       // their FP32 eigenvectors (9 per entry), recorded by the forward
+  uint8_t* d_qflag = nullptr;     // per vertex: took the QEF branch in the forward
   uint2* d_clist = nullptr;       // work list of active cells (+ counter after it)
   const float* last_density = nullptr;
   int64_t* h_pinned = nullptr;
@@ -1001,7 +1002,7 @@ bmf_status bmf_fit_destroy(bmf_fit* f) {
   void* ptrs[] = {f->d_chunks, f->d_units, f->d_flags, f->d_tot, f->d_words, f->d_totals, f->ws.vcnt, f->ws.icnt,
                   f->ws.gpl, f->ps.off, f->ps.cursor, f->ps.adj, f->ps.dual_p, f->ps.dual_n, f->ps.tmp, f->d_idxg,
                   f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist, f->d_qseed, f->d_clist, f->d_order,
-                  f->d_pqueue};
+                  f->d_pqueue, f->d_qflag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (f->h_pinned) cudaFreeHost(f->h_pinned);
@@ -1064,7 +1065,8 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
             cudaMalloc(&f->d_order, sizeof(int) * n_chunks) == cudaSuccess &&
             cudaMalloc(&f->d_pqueue, sizeof(int)) == cudaSuccess &&
             (!(flags & (BMF_FIT_ADJOINT_F64 | BMF_FIT_ADJOINT_DF)) ||
-             cudaMalloc(&f->d_qseed, sizeof(float) * 9 * (vcap + 1)) == cudaSuccess) &&
+             (cudaMalloc(&f->d_qseed, sizeof(float) * 9 * (vcap + 1)) == cudaSuccess &&
+              cudaMalloc(&f->d_qflag, vcap + 1) == cudaSuccess)) &&
             cudaMalloc(&f->d_clist, sizeof(uint2) * (vcap + icap / 4 + 2)) == cudaSuccess &&
             cudaMallocHost(&f->h_pinned, sizeof(int64_t) * 4) == cudaSuccess &&
             cudaMemcpy(f->d_chunks, hc.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -1100,6 +1102,12 @@ bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uin
   launch_scan_chunks(f->d_chunks, f->n, f->ws, f->d_tot, st);
   launch_chunk_offsets(f->d_chunks, f->n, f->d_tot, f->d_flags, f->vcap, f->icap, d_chunk_info, f->d_totals, st);
   MeshOut mo{d_pos, nullptr, f->d_boundary, f->d_valence, d_idx, f->d_idxg, f->vcap, f->icap, f->d_vkey};
+  if (f->d_qflag && f->placement == BMF_PLACE_QEF) {  // the wide adjoint reads the forward's QEF branches
+    mo.qflag = f->d_qflag;
+    mo.qlist = f->d_qlist;
+    mo.qcount = f->d_qlist + f->vcap;
+    mo.qseed = f->d_qseed;
+  }
   int k = 4 + launch_emit(BMF_MODE_Q, f->placement, f->d_chunks, f->n, f->d_units, f->n * f->dim, f->d_words,
                           d_density, f->d_flags, f->ws, mo, f->d_totals, st);
   if (f->iters > 0) {
@@ -1148,7 +1156,7 @@ bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_
   BMF_CUDA(ctx, cudaMemsetAsync(d_grad_density, 0, sizeof(float) * (size_t)f->n * f->dim * f->dim * f->dim, st));
   const int wide = (f->flags & BMF_FIT_ADJOINT_F64) ? 1 : ((f->flags & BMF_FIT_ADJOINT_DF) ? 2 : 0);
   launch_place_bwd(f->placement, wide, f->d_chunks, f->n, f->d_words, f->last_density, f->d_vkey, f->d_totals,
-                   f->vcap, f->d_g, d_grad_density, f->d_qlist, f->d_qlist + f->vcap, f->d_qseed, st);
+                   f->vcap, f->d_g, d_grad_density, f->d_qlist, f->d_qlist + f->vcap, f->d_qseed, f->d_qflag, st);
   BMF_LAUNCHED(ctx, k + (wide && f->placement == BMF_PLACE_QEF ? 2 : 1));
   return BMF_OK;
 }

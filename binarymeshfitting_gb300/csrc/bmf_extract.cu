@@ -665,13 +665,19 @@ __global__ void __launch_bounds__(256) k_emit(const ChunkDev* __restrict__ chunk
 void launch_place_bwd(int placement, int wide, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
                       const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount, float* qseed,
-                      cudaStream_t st) {
+                      const uint8_t* qflag, cudaStream_t st) {
   const int blocks = (int)((vcap + 127) / 128);
   if (blocks == 0) return;
 #define BMF_PLACE_BWD(P, T, L)                                                                                     \
   k_place_bwd<P, T, L><<<blocks, 128, 0, st>>>(d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos, \
-                                               grad_dens, qlist, qcount, qseed)
-  if (placement == 2 && wide && qlist && qcount && qseed) {
+                                               grad_dens, qlist, qcount, qseed, qflag)
+  if (placement == 2 && wide && qlist && qcount && qseed && qflag) {
+    // the forward recorded the branch and built the list: float pass over the
+    // mass-point vertices, then the wide QEF adjoint over the list
+    BMF_PLACE_BWD(2, float, 3);
+    launch_place_bwd_wide_list(wide, d_chunks, n_chunks, words, dens, vkey, d_counts, vcap, grad_pos, grad_dens,
+                               qlist, qcount, qseed, st);
+  } else if (placement == 2 && wide && qlist && qcount && qseed) {
     // float pass for the mass-point vertices, then the wide QEF adjoint over
     // the compacted list of QEF-placed ones (no idle lanes in the wide code;
     // its own translation unit, compiled with FMA contraction)
@@ -1321,7 +1327,9 @@ __global__ void __launch_bounds__(128) k_place_qef(const ChunkDev* __restrict__ 
                                                    const uint32_t* __restrict__ words, const float* __restrict__ dens,
                                                    const uint32_t* __restrict__ vkey,
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
-                                                   float* __restrict__ pos) {
+                                                   float* __restrict__ pos, uint8_t* __restrict__ qflag,
+                                                   uint32_t* __restrict__ qlist, uint32_t* __restrict__ qcount,
+                                                   float* __restrict__ qseed) {
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= min(vcap, d_counts[0])) return;
   const int c = find_chunk_by_vertex(chunks, n_chunks, v);
@@ -1331,7 +1339,25 @@ __global__ void __launch_bounds__(128) k_place_qef(const ChunkDev* __restrict__ 
   vertex_key_decode(vkey[v], x, y, z, g);
   const int mask = cell_mask_at(words + ch.words, dim, ch.zc, x, y, z);
   float P[3];
-  q_place<2>(dens + ch.dens, dim, x, y, z, mask, g, P);
+  if (qflag) {
+    // record the branch, and for a QEF-placed vertex its FP32 eigenvectors
+    // (the seeds of the wide adjoint), in the list of QEF-placed vertices
+    QefSolveInfo info;
+    bool used = false;
+    q_place<2>(dens + ch.dens, dim, x, y, z, mask, g, P, &info, &used);
+    qflag[v] = used ? 1 : 0;
+    if (used) {
+      const uint32_t k = atomicAdd(qcount, 1u);
+      qlist[k] = (uint32_t)v;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+#pragma unroll
+        for (int c3 = 0; c3 < 3; ++c3) qseed[9 * (int64_t)k + 3 * r + c3] = info.V[r][c3];
+      }
+    }
+  } else {
+    q_place<2>(dens + ch.dens, dim, x, y, z, mask, g, P);
+  }
   pos[3 * v] = P[0];
   pos[3 * v + 1] = P[1];
   pos[3 * v + 2] = P[2];
@@ -1368,8 +1394,10 @@ int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks,
     else if (placement == 1) k_emit_cells_q<1><<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
     else k_emit_cells_q<2><<<sms * 8, 256, 0, st>>>(d_chunks, words, dens, ws, out);
     if (placement == 2 && out.vkey && out.vcap > 0) {
+      if (out.qflag) cudaMemsetAsync(out.qcount, 0, sizeof(uint32_t), st);
       k_place_qef<<<(int)((out.vcap + 127) / 128), 128, 0, st>>>(d_chunks, n_chunks, words, dens, out.vkey, d_counts,
-                                                                out.vcap, out.pos);
+                                                                out.vcap, out.pos, out.qflag, out.qlist, out.qcount,
+                                                                out.qseed);
       return 2;
     }
   } else if (placement == 0) {
@@ -1380,8 +1408,10 @@ int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks,
     if (!out.vkey || !d_counts) out.vkey = nullptr;  // no keys: the emit places in place
     k_emit<1, 2><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
     if (out.vkey && out.vcap > 0) {
+      if (out.qflag) cudaMemsetAsync(out.qcount, 0, sizeof(uint32_t), st);
       k_place_qef<<<(int)((out.vcap + 127) / 128), 128, 0, st>>>(d_chunks, n_chunks, words, dens, out.vkey, d_counts,
-                                                                out.vcap, out.pos);
+                                                                out.vcap, out.pos, out.qflag, out.qlist, out.qcount,
+                                                                out.qseed);
       return 2;
     }
   }

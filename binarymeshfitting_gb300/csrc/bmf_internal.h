@@ -23,6 +23,13 @@ struct MeshOut {
   // k = crossing axis (Mode R) or vertex group (Mode Q); the key the analytic
   // adjacency build starts from.
   uint32_t* vkey = nullptr;
+  // optional (QEF placement with keys): the record the QEF adjoint reads --
+  // per vertex whether it took the QEF branch, the list of those vertices
+  // (count in *qcount) and their FP32 eigenvectors (9 floats per entry)
+  uint8_t* qflag = nullptr;
+  uint32_t* qlist = nullptr;
+  uint32_t* qcount = nullptr;
+  float* qseed = nullptr;
 };
 
 // Per-word scratch of the extraction kernels, indexed like the occupancy
@@ -156,7 +163,7 @@ void launch_place_bwd_wide_list(int wide, const ChunkDev* d_chunks, int n_chunks
 void launch_place_bwd(int placement, int wide, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words,
                       const float* dens, const uint32_t* vkey, const int64_t* d_counts, int64_t vcap,
                       const float* grad_pos, float* grad_dens, uint32_t* qlist, uint32_t* qcount, float* qseed,
-                      cudaStream_t st);
+                      const uint8_t* qflag, cudaStream_t st);
 void launch_exclusive_scan_u8_to_u32(const uint8_t* in, uint32_t* out, int64_t n, const int64_t* d_n,
                                      uint32_t* block_tmp, cudaStream_t st);
 

@@ -217,8 +217,12 @@ __device__ __forceinline__ void hermite(const float* D, int dim, int x, int y, i
   }
 }
 
+// info / qef_used (optional, QEF placement): the solve's eigen data and
+// whether the vertex took the QEF branch (a successful solve inside the cell)
+// -- what the QEF adjoint needs from the forward.
 template <int PLACE>
-__device__ __forceinline__ void q_place(const float* D, int dim, int x, int y, int z, int mask, int g, float out[3]) {
+__device__ __forceinline__ void q_place(const float* D, int dim, int x, int y, int z, int mask, int g, float out[3],
+                                        QefSolveInfo* info = nullptr, bool* qef_used = nullptr) {
   if (PLACE == 0) {
     out[0] = (float)x + 0.5f;
     out[1] = (float)y + 0.5f;
@@ -242,9 +246,10 @@ __device__ __forceinline__ void q_place(const float* D, int dim, int x, int y, i
   for (int k = 0; k < 3; ++k) mp[k] = mp[k] / (float)cnt;
   if (PLACE == 2) {
     float s[3];
-    q.solve(s);
+    const bool solved = q.solve(s, info);
     const bool ok = s[0] >= (float)x && s[0] <= (float)(x + 1) && s[1] >= (float)y && s[1] <= (float)(y + 1) &&
                     s[2] >= (float)z && s[2] <= (float)(z + 1);
+    if (qef_used) *qef_used = solved && ok;
     if (ok) {
       out[0] = s[0]; out[1] = s[1]; out[2] = s[2];
       return;
@@ -431,7 +436,9 @@ __device__ __forceinline__ uint32_t group_edges(int mask, int g) {
 }
 
 // LIST = 0: every vertex; 1: every vertex, but QEF-placed ones are only
-// appended to qlist (for a dense second pass); 2: the vertices of qlist.
+// appended to qlist (for a dense second pass); 2: the vertices of qlist;
+// 3: the vertices the forward did not flag in qflag (mass-point placed; the
+// forward built qlist / qseed).
 template <int PLACE, typename T, int LIST>
 __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ chunks, int n_chunks,
                                                    const uint32_t* __restrict__ words, const float* __restrict__ dens,
@@ -439,7 +446,7 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
                                                    const float* __restrict__ grad_pos, float* __restrict__ grad_dens,
                                                    uint32_t* __restrict__ qlist, uint32_t* __restrict__ qcount,
-                                                   float* __restrict__ qseed) {
+                                                   float* __restrict__ qseed, const uint8_t* __restrict__ qflag) {
   int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t slot = v;  // LIST == 2: the list entry
   if (LIST == 2) {
@@ -447,6 +454,7 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
     v = qlist[v];
   }
   if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
+  if (LIST == 3 && qflag[v]) return;  // QEF-placed: the list pass
   const int c = find_chunk_by_vertex(chunks, n_chunks, v);
   const ChunkDev ch = chunks[c];
   const int dim = ch.dim, zc = ch.zc;
@@ -475,6 +483,10 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
       for (int k = 0; k < 3; ++k) info.V[r][k] = qseed[9 * slot + 3 * r + k];
     }
     use_qef = true;
+  } else if constexpr (LIST == 3) {
+    // the forward recorded the branch: a vertex left to this pass took the mass point
+    cnt = __popc(edges);
+    if (cnt == 0) return;
   } else {
     // the forward's branch: replay of q_place in FP32
     if (PLACE == 2) q.init();
@@ -638,7 +650,7 @@ __global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ 
   for (uint32_t em = edges; em; em &= em - 1u) {
     const int e = __ffs(em) - 1;
     HermiteT<float> h;
-    hermite_t<float>(D, dim, x, y, z, e, PLACE == 2, h);
+    hermite_t<float>(D, dim, x, y, z, e, PLACE == 2 && use_qef, h);  // the mass point needs no normals
     const int ax = e >> 2;
     float gp[3], gn[3] = {0.0f, 0.0f, 0.0f};
     if (!use_qef) {
