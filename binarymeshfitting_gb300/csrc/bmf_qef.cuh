@@ -2,6 +2,8 @@
 // extraction TU and the FP64 adjoint TU (compiled with FMA contraction).
 #pragma once
 
+#include <type_traits>
+
 #include "bmf_device.cuh"
 #include "bmf_df.cuh"
 #include "bmf_internal.h"
@@ -439,8 +441,15 @@ __device__ __forceinline__ uint32_t group_edges(int mask, int g) {
 // appended to qlist (for a dense second pass); 2: the vertices of qlist;
 // 3: the vertices the forward did not flag in qflag (mass-point placed; the
 // forward built qlist / qseed).
+// CTAs per SM the double-float pass asks for: its code is larger than the
+// instruction cache, and more resident warps hide the fetch misses better
+// than the registers saved by spilling cost (measured: 3.71 ms backward at 4
+// CTAs, 3.46 at 8, the same at 10 and 12).
+template <typename T>
+__host__ __device__ constexpr int place_bwd_min_ctas() { return std::is_same<T, DF>::value ? 8 : 1; }
+
 template <int PLACE, typename T, int LIST>
-__global__ void __launch_bounds__(128) k_place_bwd(const ChunkDev* __restrict__ chunks, int n_chunks,
+__global__ void __launch_bounds__(128, place_bwd_min_ctas<T>()) k_place_bwd(const ChunkDev* __restrict__ chunks, int n_chunks,
                                                    const uint32_t* __restrict__ words, const float* __restrict__ dens,
                                                    const uint32_t* __restrict__ vkey,
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
