@@ -38,10 +38,10 @@ OPS_PER_LINE_OCTAVE = 20    # xs, ys, 2 floor, xf, yf, 2 fade (5 each), x1, y1, 
 OPS_PER_LINE = 1            # py - h
 OPS_PER_LAYER = 20          # 4 corners (mul + fma), alpha and beta (3 lerps of 2 each)
 # DRAM bytes (read + write) per sample of k_fill_terrain from one ncu capture on
-# the 256-chunk update (110,890,368 samples, 80.08 MB read + 479.36 MB written):
+# the 256-chunk update (110,890,368 samples, 80.04 MB read + 484.17 MB written):
 # traffic grows with the samples, so a full launch is scaled from it
 # (profiles/k_fill_terrain_lod_update_256.txt)
-FILL_DRAM_BYTES_PER_SAMPLE = (80.08e6 + 479.36e6) / 110_890_368
+FILL_DRAM_BYTES_PER_SAMPLE = (80.04e6 + 484.17e6) / 110_890_368
 
 
 def fill_fp32_ops(rows, params):
