@@ -674,7 +674,7 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
   batch_fill(b, st);
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
-  launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st);
+  launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
@@ -796,7 +796,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   BMF_CUDA(ctx, cudaEventRecord(ev[1], st));
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[2], st));
-  launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st);
+  launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   BMF_CUDA(ctx, cudaEventRecord(ev[3], st));
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);

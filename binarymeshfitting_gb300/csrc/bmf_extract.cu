@@ -310,9 +310,12 @@ __device__ __forceinline__ void block_excl_scan2(uint32_t& a, uint32_t& b, uint3
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 
+// order (nullable): CTA i scans chunk order[i] -- largest chunks first, so the
+// longest scans do not start last.
 __global__ void __launch_bounds__(kScanThreads) k_scan_chunks(const ChunkDev* __restrict__ chunks, WordScratch ws,
-                                                            uint32_t* __restrict__ tot) {
-  const ChunkDev ch = chunks[blockIdx.x];
+                                                            uint32_t* __restrict__ tot, const int* __restrict__ order) {
+  const int cid = order ? __ldg(order + blockIdx.x) : (int)blockIdx.x;
+  const ChunkDev ch = chunks[cid];
   const int64_t n = (int64_t)ch.dim * ch.dim * ch.zc;
   uint32_t* v = ws.vcnt + ch.words;
   uint32_t* ic = ws.icnt + ch.words;
@@ -344,8 +347,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_chunks(const ChunkDev* __
     carry_i += ti;
   }
   if (threadIdx.x == 0) {
-    tot[2 * blockIdx.x] = carry_v;
-    tot[2 * blockIdx.x + 1] = carry_i;
+    tot[2 * cid] = carry_v;
+    tot[2 * cid + 1] = carry_i;
   }
 }
 
@@ -965,8 +968,9 @@ void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d
   else k_count<1><<<n_units, kCountThreads, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
 }
 
-void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, uint32_t* d_tot, cudaStream_t st) {
-  k_scan_chunks<<<n_chunks, kScanThreads, 0, st>>>(d_chunks, ws, d_tot);
+void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, uint32_t* d_tot, cudaStream_t st,
+                        const int* d_order) {
+  k_scan_chunks<<<n_chunks, kScanThreads, 0, st>>>(d_chunks, ws, d_tot, d_order);
 }
 
 void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_tot, const uint32_t* flags,

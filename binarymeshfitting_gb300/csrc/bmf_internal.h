@@ -73,8 +73,10 @@ void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* w
 // Extraction: count -> per-chunk scan -> (chunk offsets) -> emit.
 void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
                   const uint32_t* words, const uint32_t* flags, WordScratch ws, cudaStream_t st);
-// Scans each chunk's word counts; writes chunk totals (vertices, indices) to d_tot[2c].
-void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, uint32_t* d_tot, cudaStream_t st);
+// Scans each chunk's word counts; writes chunk totals (vertices, indices) to
+// d_tot[2c].  d_order (optional): a permutation of the chunks, largest first.
+void launch_scan_chunks(const ChunkDev* d_chunks, int n_chunks, WordScratch ws, uint32_t* d_tot, cudaStream_t st,
+                        const int* d_order = nullptr);
 // Exclusive scan of the chunk totals into chunk.vout / chunk.iout, and the
 // per-chunk info table {voff, vcount, ioff, icount, contains_mesh, status}.
 void launch_chunk_offsets(ChunkDev* d_chunks, int n_chunks, const uint32_t* d_tot, const uint32_t* flags,
