@@ -155,7 +155,7 @@ constexpr CaseCounts make_case_counts() {
 }
 static __device__ const CaseCounts g_case_counts = make_case_counts();
 
-constexpr int kCountThreads = 128;
+constexpr int kCountThreads = 64;
 
 // Cells z of block zb with z <= hi (bits [0, hi - 32 zb]).
 __device__ __forceinline__ uint32_t zbits_upto(int hi, int zb) {
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
   __shared__ uint32_t s_cnt[64];
   __shared__ int s_c;
   const int u = blockIdx.x;
-  if (threadIdx.x < 64) s_cnt[threadIdx.x] = g_case_counts.w[threadIdx.x];
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) s_cnt[i] = g_case_counts.w[i];
   if (threadIdx.x == 0) s_c = find_chunk_e(unit_start, n_chunks, u);
   __syncthreads();
   const int c = s_c;
@@ -308,7 +308,7 @@ __device__ __forceinline__ void block_excl_scan2(uint32_t& a, uint32_t& b, uint3
 }
 
 constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 4;
+constexpr int kScanItems = 2;
 
 // order (nullable): CTA i scans chunk order[i] -- largest chunks first, so the
 // longest scans do not start last.
