@@ -189,7 +189,7 @@ __host__ __device__ constexpr size_t fill_smem_bytes(int octaves) {
 }
 
 template <int kFillRun>
-__global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __restrict__ chunks,
+__global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* __restrict__ chunks,
                                                              const int2* __restrict__ items, int n_items,
                                                              int* __restrict__ queue, FieldDev field,
                                                              float* __restrict__ dens_out,
@@ -226,9 +226,13 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
     const int x = active ? line / dim : 0, y = active ? line - x * dim : 0;
     const float px = ch.ox + (float)x * ch.scale, py = ch.oy + (float)y * ch.scale;
     uint32_t* wline = words + ch.words + (int64_t)line * zc;
-    const int nruns = (dim + kFillRun - 1) / kFillRun;
     // the z terms depend on the chunk only: all of them once per item when they fit
     const bool whole = oct * dim <= kZtEntries;
+    // dim = RUN k + 1 (33, 65, 129, ...): the line's last sample is evaluated
+    // in its last full run instead of a one-sample run that would set up every
+    // octave's line state again (needs the z terms of every sample resident)
+    const bool fold = whole && dim > kFillRun && (dim - 1) % kFillRun == 0;
+    const int nruns = fold ? (dim - 1) / kFillRun : (dim + kFillRun - 1) / kFillRun;
     if (whole) {
       for (int e = threadIdx.x; e < oct * dim; e += blockDim.x) {
         const int o = e / dim, z = e - o * dim;
@@ -261,9 +265,11 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
       if (active) {
       uint32_t bits = 0u;
       float* row = s_stage + threadIdx.x * kStageRow + (z0 & 15);
+      const bool tail = fold && zr == nruns - 1;  // sample z0 + RUN too
+      uint32_t tail_bit = 0u;
       if (n == kFillRun) {
         // a full run: RUN samples per octave, unrolled, no tail guards
-        float sum[kFillRun];
+        float sum[kFillRun], sum_t = 0.0f;
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) sum[k] = 0.0f;
         float amp = 1.0f, fr = freq;
@@ -293,6 +299,14 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
             const float l1 = __fmaf_rn(L.b1, t.y, L.a1);
             sum[k] = __fmaf_rn(amp, __fmaf_rn(t.z, l1 - l0, l0), sum[k]);
           }
+          if (tail) {  // the same operations as the sample's own run would do
+            const float4 t = zo[kFillRun];
+            const int Z = __float_as_int(t.w);
+            if (Z != L.Zp) oct_line_cell(L, Z, gtab);
+            const float l0 = __fmaf_rn(L.b0, t.x, L.a0);
+            const float l1 = __fmaf_rn(L.b1, t.y, L.a1);
+            sum_t = __fmaf_rn(amp, __fmaf_rn(t.z, l1 - l0, l0), sum_t);
+          }
           if (cache) {
             s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
             s_zp[si] = L.Zp;
@@ -305,6 +319,11 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
           const float d = __fmaf_rn(-ampl, sum[k], py - h0);
           row[k] = d;
           if (d < 0.0f) bits |= 1u << k;
+        }
+        if (tail) {  // outside the staged half block: stored directly
+          const float d = __fmaf_rn(-ampl, sum_t, py - h0);
+          if (dens_out) dens_out[ch.dens + (int64_t)line * dim + z0 + kFillRun] = d;
+          tail_bit = d < 0.0f ? 1u : 0u;
         }
       } else {
         // the line's last, partial run: one sample at a time (same operations
@@ -344,10 +363,16 @@ __global__ void __launch_bounds__(kFillLines) k_fill_terrain(const ChunkDev* __r
         }
       }
       wacc |= bits << (z0 & 31);
+      const int tz = z0 + kFillRun;  // the folded sample, in this word or the next
+      if (tail && (tz & 31) != 0) wacc |= tail_bit << (tz & 31);
       if (((z0 + kFillRun) & 31) == 0 || zr == nruns - 1) {
         wline[z0 >> 5] = wacc;
         fl |= (wacc != 0u && wacc != kFull) ? 1u : (wacc == kFull ? 2u : 4u);
         wacc = 0u;
+      }
+      if (tail && (tz & 31) == 0) {
+        wline[tz >> 5] = tail_bit;
+        fl |= tail_bit ? 1u : 4u;  // a one-sample word: any value but all-ones
       }
       }  // active
       if (dens_out && (((z0 + kFillRun) & 15) == 0 || zr == nruns - 1)) {
