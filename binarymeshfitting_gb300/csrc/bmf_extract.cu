@@ -1015,7 +1015,7 @@ __device__ __forceinline__ int packed_mask(uint32_t nbits, int ox, int oy, int o
 // two endpoint densities of a vertex come from global memory.  Warps work on
 // their own tiles with no block-wide barrier, so one warp's staging loads
 // overlap the others' cell work.
-constexpr int kTileWords = 8;
+constexpr int kTileWords = 16;
 constexpr int kEmitWarps = 8;
 
 struct RTile {
