@@ -218,6 +218,69 @@ def config(args):
             args.gpus == 1 else "weak: one independent update per GPU"}
 
 
+def arena_chunks(bufs, chunk_ids, normals):
+    """Host copies of the given chunks' slices of a batch arena: per chunk
+    (info row, positions, indices, boundary flags, normals or None)."""
+    info = bufs["info"].cpu().numpy()
+    out = []
+    for i in chunk_ids:
+        vo, vc, io, ic = (int(x) for x in info[i, :4])
+        out.append((info[i].copy(), bufs["pos"][vo:vo + vc].cpu().numpy(),
+                    bufs["idx"][io:io + ic].cpu().numpy().view(np.uint32),
+                    bufs["boundary"][vo:vo + vc].cpu().numpy(),
+                    bufs["nrm"][vo:vo + vc].cpu().numpy() if normals else None))
+    return out
+
+
+def time_per_chunk_c(descs, field, mode, args, normals):
+    """The plain per-chunk drop-in timed by the compiled C++ caller
+    (binarymeshfitting_gb300/dropin/bmf_dropin.cpp, `time` mode) over the same
+    chunk descriptors."""
+    import tempfile
+
+    from binarymeshfitting_gb300 import build
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "descs.bin")
+        with open(path, "wb") as f:
+            for dsc in descs:
+                f.write(bytes(dsc))
+        cmd = [build.DROPIN, "time", path, str(field.kind)] + ["%r" % float(field.params[i]) for i in range(8)] + [
+            str(mode), str(args.placement), str(args.iters), str(int(normals)), "16"]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError("bmf_dropin time failed: %s" % r.stderr.strip())
+    out = json.loads(r.stdout)
+    return {"value": out["chunks_per_s"], "unit": "chunks/s", "kind": "c_loop",
+            "launches": "one bmf_extract_chunk per chunk from C++, buffers allocated once (%d kernels)" %
+                        out["launches"], "vertices": out["vertices"], "seconds": out["seconds"]}
+
+
+def check_parity(sub, gpu_chunks, args):
+    """The oracle's CPU path on the sampled chunks of the benchmarked update
+    (the chunks the CPU baseline timed) against the same chunks of the GPU
+    arena: counts and digests of indices, positions, boundary flags and
+    normals, bit for bit."""
+    from binarymeshfitting_gb300 import workloads
+    from oracle import cpu
+    mode = 0 if args.mode == "R" else 1
+    counts, want = cpu.extract_batch_digest(sub[:, :5].astype(np.float32), 2, list(workloads.TERRAIN_PARAMS), mode,
+                                            args.placement, args.iters, False, not args.no_normals)
+    bad, with_mesh, verts = [], 0, 0
+    for k, (info, pos, idx, bnd, nrm) in enumerate(gpu_chunks):
+        got = cpu.chunk_digests(pos, idx, bnd, nrm)
+        ok = (int(info[4]) == counts[k, 0] and int(info[1]) == counts[k, 1] and int(info[3]) == counts[k, 2]
+              and int(info[5]) == 0 and tuple(int(x) for x in want[k]) == got)
+        if not ok:
+            bad.append(k)
+        with_mesh += int(counts[k, 1] > 0)
+        verts += int(counts[k, 1])
+    tiers = {int(d): int((sub[:, 4] == d).sum()) for d in np.unique(sub[:, 4])}
+    return {"chunks_checked": len(gpu_chunks), "chunks_with_mesh": with_mesh, "vertices_checked": verts,
+            "tiers": tiers, "bit_exact": not bad, "mismatched_chunks": bad[:16],
+            "compared": "per chunk: contains_mesh, vertex and index counts, status, and digests of indices, "
+                        "positions, boundary flags and normals (oracle CPU path vs the GPU arena)"}
+
+
 def run_fit(ctx, args, stream):
     """Batched fitting: forward / backward kernel times (bwd/fwd) and an Adam
     loop on fit_chunks learnable 65^3 grids with sphere-union targets."""
@@ -367,6 +430,9 @@ def run_gb300(args):
     ms = float(ms_t.item())
     value = args.chunks * world / (ms / 1000.0)
     nv, ni = b.run(use_graph=True, sync=True)
+    # the GPU meshes of the chunks the CPU leg re-computes (parity, below)
+    parity_idx = cpu_sample_rows(rows, args.cpu_sample, 7)
+    gpu_chunks = arena_chunks(bufs, parity_idx, normals)
 
     # ---- per-stage profile (outside the timed region) ----
     stages = [b.profile() for _ in range(3)]
@@ -413,8 +479,8 @@ def run_gb300(args):
 
     # ---- end to end through the public API with host buffers ----
     # Every step uploads its descriptors from pinned host memory, runs the
-    # update and reads its positions, indices and chunk table back to pinned
-    # host memory.  Two plans (double-buffered output arenas) let the read-back
+    # update and reads everything it produced back to pinned host memory:
+    # positions, indices, the chunk table, normals and boundary flags.  Two plans (double-buffered output arenas) let the read-back
     # of step i run on a copy stream while step i + 1 computes.
     h_desc_list = descs
     vbytes = nv * 12
@@ -426,16 +492,18 @@ def run_gb300(args):
     plans = [(b, bufs), (b2, bufs2)]
     hosts = [(torch.empty((nv, 3), dtype=torch.float32, pin_memory=True),
               torch.empty(ni, dtype=torch.int32, pin_memory=True),
-              torch.empty((args.chunks, 6), dtype=torch.int64, pin_memory=True)) for _ in range(2)]
+              torch.empty((args.chunks, 6), dtype=torch.int64, pin_memory=True),
+              torch.empty((nv, 3), dtype=torch.float32, pin_memory=True) if normals else None,
+              torch.empty(nv, dtype=torch.uint8, pin_memory=True)) for _ in range(2)]
     copy_stream = torch.cuda.Stream()
     done = [torch.cuda.Event() for _ in range(2)]
     copied = [torch.cuda.Event() for _ in range(2)]
     h2d = args.chunks * 56
-    d2h = vbytes + ibytes + args.chunks * 48
+    d2h = vbytes + ibytes + args.chunks * 48 + (vbytes if normals else 0) + nv
 
     def e2e_step(k):
         pb, pbufs = plans[k & 1]
-        hp, hi, hn = hosts[k & 1]
+        hp, hi, hn, hnr, hb = hosts[k & 1]
         stream.wait_event(copied[k & 1])  # this arena's previous read-back is done
         pb.set_descs(h_desc_list, stream=stream)
         pb.run(use_graph=True, sync=False, stream=stream)
@@ -445,6 +513,9 @@ def run_gb300(args):
             hp.copy_(pbufs["pos"][:nv], non_blocking=True)
             hi.copy_(pbufs["idx"][:ni], non_blocking=True)
             hn.copy_(pbufs["info"], non_blocking=True)
+            if hnr is not None:
+                hnr.copy_(pbufs["nrm"][:nv], non_blocking=True)
+            hb.copy_(pbufs["boundary"][:nv], non_blocking=True)
             copied[k & 1].record(copy_stream)
 
     for k in range(4):
@@ -462,13 +533,20 @@ def run_gb300(args):
     e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1000.0) / args.steps
     e2e = {"value": args.chunks * world / (e2e_ms / 1000.0), "unit": "chunks/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+           "read_back": "positions, indices, chunk table" + (", normals" if normals else "") + ", boundary flags",
            "pipeline": "two plans; step i's read-back on a copy stream overlaps step i + 1"}
     b2.close()
     del plans, hosts, bufs2
 
     # ---- the plain per-chunk path (the drop-in), same chunks ----
+    # Timed as a C++ caller makes it (bmf_dropin time: one bmf_extract_chunk
+    # per chunk on device buffers allocated once, one context, one stream), and
+    # through the Python binding for comparison.
     per_chunk = None
     if not args.skip_per_chunk and rank == 0:
+        per_chunk = time_per_chunk_c(descs, field, mode, args, normals)
+        per_chunk["vertices_match_batch"] = per_chunk["vertices"] == nv
+        per_chunk["batch_speedup"] = value / world / per_chunk["value"]
         for dsc in descs[:16]:
             ctx.extract_chunk(dsc, field, mode=mode, placement=args.placement, iters=args.iters,
                               smooth_normals=normals)
@@ -481,9 +559,9 @@ def run_gb300(args):
             pv += m.n_verts
         torch.cuda.synchronize()
         pc_s = time.perf_counter() - t0
-        per_chunk = {"value": args.chunks / pc_s, "unit": "chunks/s", "launches": "one bmf_extract_chunk per chunk",
-                     "vertices_match_batch": pv == nv, "batch_speedup": (args.chunks / (ms / 1000.0)) /
-                     (args.chunks / pc_s)}
+        per_chunk["python_binding"] = {"value": args.chunks / pc_s, "unit": "chunks/s",
+                                       "kind": "python ctypes, torch buffers allocated per call",
+                                       "vertices_match_batch": pv == nv}
 
     # ---- batched fitting: backward vs forward ----
     bwd_fwd = None
@@ -496,6 +574,7 @@ def run_gb300(args):
 
     # ---- CPU baseline (rank 0): bounded sample of the same update, all host threads ----
     cpu_baseline = None
+    parity = None
     if not args.skip_cpu and rank == 0:
         from oracle import cpu
         cpu.build()
@@ -506,6 +585,7 @@ def run_gb300(args):
         cpu_baseline = {"value": len(sub) / t, "unit": "chunks/s", "cores": threads, "kind": "port",
                         "sample": "%d tier-stratified chunks of the %d-chunk update, OpenMP over chunks" %
                                   (len(sub), args.chunks)}
+        parity = check_parity(sub, gpu_chunks, args)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "chunks/s", "n_gpus": world, "steps": args.steps,
@@ -513,7 +593,8 @@ def run_gb300(args):
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config(args),
                 "samples_per_s": samples * world / (ms / 1000.0),
                 "vertices_per_s": nv * world / (ms / 1000.0), "vertices_per_step": nv, "indices_per_step": ni,
-                "roofline": roofline, "cpu_baseline": cpu_baseline, "e2e": e2e, "per_chunk": per_chunk,
+                "roofline": roofline, "cpu_baseline": cpu_baseline, "parity": parity, "e2e": e2e,
+                "per_chunk": per_chunk,
                 "gpu_launches": launches, "clocks": clk, "bwd_fwd": bwd_fwd,
                 "tuning": {"chosen": tuned, "candidates_ms": tune_ms,
                            "candidates": "fill (mode, run): (0,8) (1,4) (1,8) (1,16) (2,4) (2,8) (2,16); "

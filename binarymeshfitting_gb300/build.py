@@ -15,6 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libbmf_gb300.so")
+# A compiled C++ caller of the library (include/bmf.h + include/bmf_adapter.hpp).
+DROPIN_SRC = os.path.join(HERE, "dropin", "bmf_dropin.cpp")
+DROPIN = os.path.join(BUILD, "bmf_dropin")
 SOURCES = ["bmf_sample.cu", "bmf_extract.cu", "bmf_process.cu", "bmf_capi.cu", "bmf_noalloc.cu", "bmf_lod.cu",
            "bmf_adjoint64.cu"]
 # Sources whose arithmetic does not mirror the reference's float rounding may
@@ -36,13 +39,16 @@ def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))]
     files.append(os.path.join(HERE, "..", "include", "bmf.h"))
     files.append(os.path.join(HERE, "..", "include", "bmf_fields.h"))
+    files.append(os.path.join(HERE, "..", "include", "bmf_adapter.hpp"))
+    files.append(DROPIN_SRC)
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
 
 
 def build(force=False, verbose=False, extra_flags=()):
     """Compiles (if stale) and returns the library path."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps():
+    if (not force and os.path.exists(LIB) and os.path.exists(DROPIN)
+            and min(os.path.getmtime(LIB), os.path.getmtime(DROPIN)) >= _deps()):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
@@ -69,7 +75,20 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_dropin(cc)
     return LIB
+
+
+def build_dropin(cc):
+    """The drop-in caller: host C++ only, linked against the library (rpath
+    $ORIGIN, both live in _build/)."""
+    tmp = DROPIN + ".tmp"
+    cmd = [cc, "-std=c++17", "-O2", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(HERE, ".."), DROPIN_SRC,
+           "-o", tmp, "-L" + BUILD, "-lbmf_gb300", "-lcudart", "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("drop-in caller build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, DROPIN)
 
 
 if __name__ == "__main__":

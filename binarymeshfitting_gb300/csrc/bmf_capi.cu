@@ -1,9 +1,12 @@
 // C ABI (include/bmf.h): context, scratch arena, per-chunk entry points and
 // the batched, CUDA-graph-captured update.
 #include <algorithm>
+#include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/bmf.h"
@@ -71,6 +74,9 @@ struct bmf_batch {
   int64_t* h_pinned = nullptr;
   ChunkDev* h_stage = nullptr;       // pinned staging for bmf_batch_set_descs
   cudaEvent_t stage_done = nullptr;  // the last staging copy has been consumed
+  cudaEvent_t run_done = nullptr;    // recorded after every bmf_batch_run (bmf_batch_wait polls it)
+  cudaStream_t aux = nullptr;        // private stream for bmf_batch_wait's read of the totals
+  bool ran = false;
   // terrain fill: line items {chunk, first line}, largest chunks first, and
   // the work queue of the persistent form; fill_mode 0 = x-plane kernel,
   // 1 = one CTA per item, 2 = persistent CTAs on the queue
@@ -156,11 +162,21 @@ FieldDev make_field(const bmf_field* f) {
 }
 
 bool field_ok(const bmf_field* f) {
-  return f && f->kind >= BMF_FIELD_GRID && f->kind <= BMF_FIELD_PLANE_Y &&
-         (f->kind != BMF_FIELD_TERRAIN_FBM || (f->params[5] >= 0 && f->params[5] <= 32));
+  if (!f || f->kind < BMF_FIELD_GRID || f->kind > BMF_FIELD_PLANE_Y) return false;
+  for (int i = 0; i < BMF_FIELD_MAX_PARAMS; ++i)
+    if (!std::isfinite(f->params[i])) return false;
+  return f->kind != BMF_FIELD_TERRAIN_FBM || (f->params[5] >= 0 && f->params[5] <= 32);
 }
 
 bool dim_ok(int dim) { return dim >= 2 && dim <= kMaxDim; }
+
+// A chunk descriptor the kernels can sample: dim in range, a finite origin
+// and a finite positive sample spacing (a NaN or infinite frame would give
+// NaN densities whose signs mean nothing).
+bool desc_ok(const bmf_chunk_desc* d) {
+  return d && dim_ok(d->dim) && std::isfinite(d->origin[0]) && std::isfinite(d->origin[1]) &&
+         std::isfinite(d->origin[2]) && std::isfinite(d->scale) && d->scale > 0.0f;
+}
 
 ChunkDev chunk_of(const bmf_chunk_desc* d) {
   ChunkDev c{};
@@ -298,7 +314,7 @@ int64_t bmf_launch_count(const bmf_ctx* ctx) { return ctx ? ctx->launches : 0; }
 bmf_status bmf_sample_label(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
                             uint32_t* d_words, int32_t* h_contains_mesh, void* stream) {
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
-  if (!desc || !dim_ok(desc->dim) || !field_ok(field) || !d_words)
+  if (!desc_ok(desc) || !field_ok(field) || !d_words)
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_sample_label: bad descriptor, field or words pointer");
   if (field->kind == BMF_FIELD_GRID && !d_density)
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "BMF_FIELD_GRID reads d_density, which must be given");
@@ -327,7 +343,7 @@ bmf_status bmf_sample_label(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_
 bmf_status bmf_sample_block(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
                             void* stream) {
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
-  if (!desc || !dim_ok(desc->dim) || !field_ok(field) || field->kind == BMF_FIELD_GRID || !d_density)
+  if (!desc_ok(desc) || !field_ok(field) || field->kind == BMF_FIELD_GRID || !d_density)
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_sample_block: bad descriptor, field or density pointer");
   const int dim = desc->dim, zc = (dim + 31) / 32;
   uint32_t* words;
@@ -451,7 +467,7 @@ bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   bmf_status s;
   if ((s = mesh_valid(ctx, out)) != BMF_OK) return s;
-  if (!desc || !dim_ok(desc->dim) || !field_ok(field) || field->kind == BMF_FIELD_GRID || !opts ||
+  if (!desc_ok(desc) || !field_ok(field) || field->kind == BMF_FIELD_GRID || !opts ||
       (opts->mode != BMF_MODE_R && opts->mode != BMF_MODE_Q) || opts->placement < 0 || opts->placement > 2 ||
       opts->iters < 0)
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_extract_chunk: bad descriptor, field or options");
@@ -525,9 +541,11 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
   int64_t dens = 0, words = 0;
   int n_units = 0;
   for (int i = 0; i < n_chunks; ++i) {
-    if (!dim_ok(h_descs[i].dim)) {
+    if (!desc_ok(h_descs + i)) {
       delete b;
-      return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_create: chunk dim out of range");
+      return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
+                  "bmf_batch_create: chunk " + std::to_string(i) +
+                      ": dim out of range, or a non-finite origin or a non-positive / non-finite scale");
     }
     ChunkDev c = chunk_of(h_descs + i);
     c.dens = dens;
@@ -740,6 +758,9 @@ bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, in
     if ((s = batch_record(b, out, st, &k)) != BMF_OK) return s;
     ctx->launches += k;
   }
+  if (!b->run_done) BMF_CUDA(ctx, cudaEventCreateWithFlags(&b->run_done, cudaEventDisableTiming));
+  BMF_CUDA(ctx, cudaEventRecord(b->run_done, st));
+  b->ran = true;
   if (sync) {
     BMF_CUDA(ctx, cudaMemcpyAsync(b->h_pinned, b->d_totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     BMF_CUDA(ctx, cudaStreamSynchronize(st));
@@ -751,13 +772,43 @@ bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, in
   return BMF_OK;
 }
 
+bmf_status bmf_batch_wait(bmf_batch* b, bmf_batch_out* out, int32_t timeout_ms) {
+  if (!b) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  if (!out || timeout_ms < 0) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_wait: no output or timeout < 0");
+  if (!b->ran) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_wait: the plan has not run");
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+  for (;;) {
+    const cudaError_t e = cudaEventQuery(b->run_done);
+    if (e == cudaSuccess) break;
+    if (e != cudaErrorNotReady) return cuda_check(ctx, e, "bmf_batch_wait");
+    if (std::chrono::steady_clock::now() >= deadline)
+      return fail(ctx, BMF_ERR_TIMEOUT,
+                  "bmf_batch_wait: the update is still running after " + std::to_string(timeout_ms) +
+                      " ms (nothing was cancelled; wait again)");
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+  if (!b->aux) BMF_CUDA(ctx, cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking));
+  BMF_CUDA(ctx, cudaMemcpyAsync(b->h_pinned, b->d_totals, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, b->aux));
+  BMF_CUDA(ctx, cudaStreamSynchronize(b->aux));
+  out->n_verts = b->h_pinned[0];
+  out->n_idx = b->h_pinned[1];
+  if (out->n_verts > out->vcap || out->n_idx > out->icap)
+    return fail(ctx, BMF_ERR_CAPACITY, "bmf_batch_wait: output capacity exceeded (needed totals reported)");
+  return BMF_OK;
+}
+
 bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_descs, int32_t n_chunks, void* stream) {
   if (!b) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = b->ctx;
   if (!h_descs || n_chunks != b->n) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_set_descs: count differs");
-  for (int i = 0; i < n_chunks; ++i)
+  for (int i = 0; i < n_chunks; ++i) {
     if (h_descs[i].dim != b->h_chunks[i].dim)
       return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_set_descs: a chunk's dim differs from the plan");
+    if (!desc_ok(h_descs + i))
+      return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
+                  "bmf_batch_set_descs: chunk " + std::to_string(i) + ": non-finite origin or bad scale");
+  }
   cudaStream_t st = (cudaStream_t)stream;
   if (!b->h_stage) {
     BMF_CUDA(ctx, cudaMallocHost(&b->h_stage, sizeof(ChunkDev) * b->n));
@@ -1173,6 +1224,8 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
   if (b->h_stage) cudaFreeHost(b->h_stage);
   if (b->stage_done) cudaEventDestroy(b->stage_done);
+  if (b->run_done) cudaEventDestroy(b->run_done);
+  if (b->aux) cudaStreamDestroy(b->aux);
   delete b;
   return BMF_OK;
 }

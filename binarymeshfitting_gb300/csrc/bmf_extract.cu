@@ -929,17 +929,13 @@ __global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_c
 
 template <int MODE, int N>
 static int sweep_chunks_grid() {
-  static int grid[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  const int gi = dev >= 0 && dev < 64 ? dev : 0;
-  if (grid[gi] == 0) {
+  static std::atomic<int> grid[64] = {};
+  return per_device_once(grid, [](int dev) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_chunks<MODE, N>, chunk_sweep_threads<MODE>(), 0);
-    grid[gi] = sms * (per_sm > 0 ? per_sm : 1);
-  }
-  return grid[gi];
+    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  });
 }
 
 void launch_sweep_chunks(const StructuredAdj& sa, int N, int64_t nv, int64_t n_prims, const int64_t* d_counts,
@@ -1372,21 +1368,14 @@ int launch_emit(int mode, int placement, const ChunkDev* d_chunks, int n_chunks,
                 MeshOut out, const int64_t* d_counts, cudaStream_t st) {
   if (mode == 0 && ws.clist) {
     // persistent: one wave of resident CTAs
-    static int grid[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64 || grid[dev] == 0) {
+    static std::atomic<int> grid[64] = {};
+    const int g = per_device_once(grid, [](int dev) {
       int sms = 0, per_sm = 0;
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_emit_words_r, 32 * kEmitWarps, 0);
-      const int g = sms * (per_sm > 0 ? per_sm : 1);
-      if (dev < 0 || dev >= 64) {
-        k_emit_words_r<<<g, 32 * kEmitWarps, 0, st>>>(d_chunks, words, dens, ws, out);
-        return 1;
-      }
-      grid[dev] = g;
-    }
-    k_emit_words_r<<<grid[dev], 32 * kEmitWarps, 0, st>>>(d_chunks, words, dens, ws, out);
+      return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    });
+    k_emit_words_r<<<g, 32 * kEmitWarps, 0, st>>>(d_chunks, words, dens, ws, out);
   } else if (mode == 0) {
     k_emit<0, 0><<<n_units, 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, dens, flags, ws, out);
   } else if (ws.clist) {

@@ -2,10 +2,28 @@
 #pragma once
 
 #include "../../include/bmf.h"
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace bmf {
+
+// A launch constant worked out once per device (an occupancy-sized grid, a
+// shared-memory opt-in done).  Host threads may race on the first call: each
+// computes the same value, and the atomic slot makes the publication well
+// defined.  compute(dev) must return a non-zero value.
+template <class F>
+inline int per_device_once(std::atomic<int> (&slot)[64], F compute) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return compute(dev);
+  int v = slot[dev].load(std::memory_order_acquire);
+  if (v == 0) {
+    v = compute(dev);
+    slot[dev].store(v, std::memory_order_release);
+  }
+  return v;
+}
 
 struct ChunkDev;
 struct FieldDev;

@@ -171,13 +171,11 @@ int lod_generate(const bmf_lod_params& p, bmf_chunk_desc* d_descs, int cap, int3
     k_lod_level<<<blocks, 256, 0, st>>>(p, l, odd ? f1 : f0, odd ? f0 : f1, leaves, cap, s);
   }
   const size_t smem = (size_t)n_pow2 * (sizeof(unsigned long long) + sizeof(int));
-  static bool attr_set[64] = {};  // the shared-memory opt-in, once per device
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || !attr_set[dev]) {
+  static std::atomic<int> attr_set[64] = {};  // the shared-memory opt-in, once per device
+  per_device_once(attr_set, [](int) {
     cudaFuncSetAttribute(k_lod_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, kLodMaxLeaves * 12);
-    if (dev >= 0 && dev < 64) attr_set[dev] = true;
-  }
+    return 1;
+  });
   k_lod_emit<<<1, kLodSortThreads, smem, st>>>(p, leaves, cap, n_pow2, s, d_descs, d_count);
   return p.max_level + 3;
 }

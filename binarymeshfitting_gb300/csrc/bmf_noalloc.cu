@@ -24,7 +24,11 @@
 //    before writing (the contains_mesh flags) is cleared by each call;
 //  - the first call on a device looks up the array's device address for that
 //    device (cudaGetSymbolAddress, with that device current) and caches it;
-//    make that first call before any stream capture.
+//    under CUDA's lazy module loading (the default) that lookup is also when
+//    the driver loads this library's device code on the device and places the
+//    array, so the first call per device can allocate device memory once.
+//    Hosts that forbid any allocation later make that first call at start-up,
+//    and before any stream capture.
 #include <mutex>
 
 #include "../../include/bmf.h"

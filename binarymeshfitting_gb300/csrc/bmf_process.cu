@@ -397,26 +397,24 @@ int launch_process_bwd(int N, int64_t nv, int64_t n_prims, const int64_t* d_coun
                        const ProcessScratch& s, float* g, const StructuredAdj* sa, cudaStream_t st) {
   if (nv == 0 || n_prims == 0 || iters <= 0) return 0;
   if (sa && sa->tot && sa->order && sa->queue) {
-    static int grid[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const int gi = dev >= 0 && dev < 64 ? dev : 0;
-    if (grid[gi] == 0) {
+    // one slot array per primitive size: the two kernels' occupancies may differ
+    static std::atomic<int> grid3[64] = {}, grid4[64] = {};
+    const int grid = per_device_once(N == 3 ? grid3 : grid4, [N](int dev) {
       int sms = 0, per_sm = 0;
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
       if (N == 3)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_bwd_chunks<3>, kBwdChunkThreads, 0);
       else
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_bwd_chunks<4>, kBwdChunkThreads, 0);
-      grid[gi] = sms * (per_sm > 0 ? per_sm : 1);
-    }
+      return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    });
     cudaMemsetAsync(sa->queue, 0, sizeof(int), st);
     if (N == 3)
-      k_sweep_bwd_chunks<3><<<grid[gi], kBwdChunkThreads, 0, st>>>(
+      k_sweep_bwd_chunks<3><<<grid, kBwdChunkThreads, 0, st>>>(
           sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_prims * N, d_counts, s.off,
           valence, s.adj, boundary, process_boundary, idx, g, s.dual_p, iters);
     else
-      k_sweep_bwd_chunks<4><<<grid[gi], kBwdChunkThreads, 0, st>>>(
+      k_sweep_bwd_chunks<4><<<grid, kBwdChunkThreads, 0, st>>>(
           sa->chunks, sa->tot, sa->order, sa->n_chunks, sa->queue, nv, n_prims, n_prims * N, d_counts, s.off,
           valence, s.adj, boundary, process_boundary, idx, g, s.dual_p, iters);
     return 1;

@@ -404,15 +404,14 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
 // The kernels' static + staging shared memory exceeds the 48 KB default: opt
 // in once per device.
 static void fill_terrain_smem_optin() {
-  static bool done[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && done[dev]) return;
-  const int mx = (int)fill_smem_bytes(kCacheOctaves);
-  cudaFuncSetAttribute(k_fill_terrain<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_fill_terrain<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_fill_terrain<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  if (dev >= 0 && dev < 64) done[dev] = true;
+  static std::atomic<int> done[64] = {};
+  per_device_once(done, [](int) {
+    const int mx = (int)fill_smem_bytes(kCacheOctaves);
+    cudaFuncSetAttribute(k_fill_terrain<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    return 1;
+  });
 }
 
 void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,

@@ -248,6 +248,13 @@ class Batch:
                                                    _stream(stream)))
         return int(self.out.n_verts), int(self.out.n_idx)
 
+    def wait(self, timeout_ms):
+        """bmf_batch_wait: waits at most timeout_ms for the last run; returns
+        (vertices, indices).  Raises BmfError(ERR_TIMEOUT) when the update is
+        still running (nothing is cancelled; wait again)."""
+        self.ctx._check(self.ctx.lib.bmf_batch_wait(self.h, ctypes.byref(self.out), int(timeout_ms)))
+        return int(self.out.n_verts), int(self.out.n_idx)
+
     def set_descs(self, descs, stream=None):
         arr = (L.ChunkDesc * self.n)(*descs)
         self.ctx._check(self.ctx.lib.bmf_batch_set_descs(self.h, arr, self.n, _stream(stream)))

@@ -179,7 +179,10 @@ class WorldOctreeNode:
 
 class ChunkGenerator:
     """ChunkGenerator::process_queue (ChunkGenerator.cpp:27-147): the whole
-    queue goes through one batched, graph-captured update."""
+    queue goes through one batched, graph-captured update.  The plan and its
+    output arena are kept while queues keep their shape (same chunk count and
+    resolution): the next queue's descriptors are swapped in with
+    bmf_batch_set_descs and the captured graph replays."""
 
     def __init__(self, properties: WorldProperties, sampler: Sampler, dim=RESOLUTION, mode=L.MODE_R,
                  placement=L.PLACE_CENTER):
@@ -188,6 +191,8 @@ class ChunkGenerator:
         self.dim = dim
         self.mode = mode
         self.placement = placement
+        self._plan: Optional[Batch] = None
+        self.plans_reused = 0
 
     def overlap_for(self, node: WorldOctreeNode):
         """ChunkGenerator.cpp:98."""
@@ -196,26 +201,44 @@ class ChunkGenerator:
             return 0.0
         return p.overlap + 0.005 * float(p.process_iters)
 
-    def process_queue(self, batch: List[WorldOctreeNode]):
-        p = self.properties
-        descs = []
+    def _descs(self, batch):
+        out = []
         for n in batch:
             delta, org = chunk_frame(n.pos, n.size, self.overlap_for(n), self.dim)
-            descs.append(L.ChunkDesc.make(org, delta, self.dim, n.level))
+            out.append(L.ChunkDesc.make(org, delta, self.dim, n.level))
+        return out
+
+    def process_queue(self, batch: List[WorldOctreeNode]):
+        p = self.properties
+        if not batch:
+            return batch
+        descs = self._descs(batch)
         ctx = context()
-        b = Batch(ctx, descs, self.sampler.field, mode=self.mode, placement=self.placement, iters=p.process_iters,
-                  process_boundary=p.boundary_processing, smooth_normals=p.smooth_normals)
-        vcap, icap = max(4096, len(batch) * self.dim ** 2 * 4), max(16384, len(batch) * self.dim ** 2 * 24)
-        for _ in range(3):
+        b = self._plan
+        if b is not None and b.n == len(batch):
+            b.set_descs(descs)
+            self.plans_reused += 1
+        else:
+            self.close()
+            b = Batch(ctx, descs, self.sampler.field, mode=self.mode, placement=self.placement,
+                      iters=p.process_iters, process_boundary=p.boundary_processing, smooth_normals=p.smooth_normals)
+            self._plan = b
+            vcap, icap = max(4096, len(batch) * self.dim ** 2 * 4), max(16384, len(batch) * self.dim ** 2 * 24)
             b.allocate(vcap, icap, normals=p.smooth_normals)
+        for _ in range(3):
             try:
-                b.run(use_graph=False, sync=True)
+                b.run(use_graph=True, sync=True)
                 break
             except L.BmfError as e:
                 if e.status != L.ERR_CAPACITY:
                     raise
-                vcap, icap = int(b.out.n_verts) + 1024, int(b.out.n_idx) + 1024
+                b.allocate(int(b.out.n_verts) + 1024, int(b.out.n_idx) + 1024, normals=p.smooth_normals)
         for i, n in enumerate(batch):
-            n.vi = b.chunk_mesh(i)
-        b.close()
+            # copies: the arena is overwritten by the next queue
+            n.vi = {k: (v.clone() if isinstance(v, torch.Tensor) else v) for k, v in b.chunk_mesh(i).items()}
         return batch
+
+    def close(self):
+        if self._plan is not None:
+            self._plan.close()
+            self._plan = None

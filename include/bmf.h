@@ -43,7 +43,7 @@ typedef enum bmf_status {
   BMF_ERR_INVALID_ARGUMENT = 1,
   BMF_ERR_CUDA = 2,
   BMF_ERR_CAPACITY = 3,      /* output capacity too small; needed counts reported */
-  BMF_ERR_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+  BMF_ERR_TIMEOUT = 4,       /* a bounded host-side wait gave up (bmf_batch_wait); nothing was cancelled */
   BMF_ERR_OUT_OF_MEMORY = 5,
   BMF_ERR_NOT_SUPPORTED = 6
 } bmf_status;
@@ -63,7 +63,10 @@ typedef struct bmf_field {
 } bmf_field;
 
 /* One chunk: DMCChunk's pos/overlap/scale after label_grid set them
- * (DMCChunk.cpp:94-98): origin = overlap_pos, scale = delta. */
+ * (DMCChunk.cpp:94-98): origin = overlap_pos, scale = delta.  Every entry
+ * point that samples a chunk rejects, with BMF_ERR_INVALID_ARGUMENT, a dim
+ * out of range, a non-finite origin, and a scale that is not finite and > 0;
+ * field params must be finite too. */
 typedef struct bmf_chunk_desc {
   float origin[3];
   float scale;
@@ -155,8 +158,14 @@ BMF_API bmf_status bmf_polygonize(bmf_ctx* ctx, int32_t dim, const float* d_dens
  * holds until exit.  dim > BMF_NOALLOC_MAX_DIM returns BMF_ERR_NOT_SUPPORTED.
  * All calls share that array: calls that overlap on the GPU race, so
  * serialise them.  The first call on a device resolves the array's address
- * for that device; make it before any stream capture.  Inputs, outputs and
- * results are those of bmf_polygonize; synchronises the stream. */
+ * for that device; with CUDA's lazy module loading (the default) that first
+ * call is also when the driver loads the library's device code on that device
+ * and places the array, which allocates device memory once.  A host that
+ * forbids any allocation later makes that first call at start-up (and before
+ * any stream capture).  Inputs, outputs and results are those of
+ * bmf_polygonize, including BMF_ERR_CAPACITY with the needed counts when
+ * vcap / icap are too small (nothing is written past them); synchronises the
+ * stream. */
 BMF_API bmf_status bmf_polygonize_noalloc(int32_t dim, const float* d_density, const uint32_t* d_words,
                                           int32_t mode, int32_t placement, bmf_mesh* out, void* stream);
 
@@ -197,6 +206,15 @@ BMF_API bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs,
  * sync != 0 waits and fills out->n_verts / n_idx. */
 BMF_API bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, int32_t sync, void* stream);
 BMF_API bmf_status bmf_batch_destroy(bmf_batch* b);
+/* Waits on the host, for at most timeout_ms milliseconds (0 = poll once), for
+ * the plan's last bmf_batch_run to finish on the GPU -- typically one launched
+ * with sync == 0 -- then fills out->n_verts / n_idx as a synchronous run does
+ * (BMF_ERR_CAPACITY when they exceed the arena).  Returns BMF_ERR_TIMEOUT when
+ * the update is still running at the deadline: nothing is cancelled, the call
+ * may be repeated, and plan and context stay usable.  A host thread that must
+ * not block (the reference's watcher thread, WorldWatcher.cpp) polls with 0.
+ * No counterpart in the reference (its extraction is synchronous). */
+BMF_API bmf_status bmf_batch_wait(bmf_batch* b, bmf_batch_out* out, int32_t timeout_ms);
 /* Replaces the plan's chunk descriptors with those of the next update (same
  * count and the same dim per slot, e.g. the next frame of a streaming world):
  * an asynchronous pinned host->device copy on `stream`, so the captured graph

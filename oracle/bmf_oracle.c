@@ -1153,8 +1153,37 @@ void bmfo_process(int N, int64_t nverts, float* pos, float* nrm, const uint8_t* 
 /* CPU baseline: whole path over a batch, OpenMP over chunks                 */
 /* ======================================================================== */
 
-int64_t bmfo_extract_batch(int n_chunks, const float* desc, int field, const float* params, int mode, int placement,
-                           int iters, int smooth_normals, int64_t* out_counts, int n_threads) {
+/* FNV-1a (64-bit) of a byte range.  f32_canon != 0 reads the range as floats
+ * and hashes every NaN as the canonical quiet NaN 0x7FC00000 (x86, Arm and the
+ * GPU encode a NaN's sign and payload differently). */
+uint64_t bmfo_digest64(const void* data, int64_t n_bytes, int f32_canon) {
+  uint64_t h = 0xcbf29ce484222325ull;
+  const uint8_t* b = (const uint8_t*)data;
+  if (f32_canon) {
+    for (int64_t i = 0; i + 4 <= n_bytes; i += 4) {
+      uint32_t u;
+      memcpy(&u, b + i, 4);
+      if ((u & 0x7F800000u) == 0x7F800000u && (u & 0x007FFFFFu)) u = 0x7FC00000u;
+      for (int k = 0; k < 4; ++k) {
+        h ^= (u >> (8 * k)) & 0xFFu;
+        h *= 0x100000001b3ull;
+      }
+    }
+    return h;
+  }
+  for (int64_t i = 0; i < n_bytes; ++i) {
+    h ^= b[i];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+/* ChunkGenerator::extract_chunk (ChunkGenerator.cpp:80-147): per chunk, fill ->
+ * label_grid -> label_edges + polygonize (Mode R) or the Mode Q emitter ->
+ * MeshProcessor, OpenMP over chunks as the reference's batch loop. */
+int64_t bmfo_extract_batch_digest(int n_chunks, const float* desc, int field, const float* params, int mode,
+                                  int placement, int iters, int process_boundary, int smooth_normals,
+                                  int64_t* out_counts, uint64_t* out_digest, int n_threads) {
   int64_t total = 0;
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
@@ -1170,42 +1199,58 @@ int64_t bmfo_extract_batch(int n_chunks, const float* desc, int field, const flo
     bmfo_fill_field(field, params, dim, d, d[3], dens_buf);
     int cm = bmfo_label_grid(dim, dens_buf, words);
     bmfo_counts c = {0, 0, 0};
+    float* vp = NULL;
+    float* vn = NULL;
+    uint8_t* vb = NULL;
+    uint8_t* vv = NULL;
+    uint32_t* ix = NULL;
     if (cm) {
       bmfo_counts cnt;
+      uint64_t* masks = NULL;
       if (mode == 0) {
-        uint64_t* masks = (uint64_t*)malloc((size_t)dim * dim * 4 * zc * sizeof(uint64_t));
+        masks = (uint64_t*)malloc((size_t)dim * dim * 4 * zc * sizeof(uint64_t));
         bmfo_cell_masks(dim, words, masks);
         bmfo_extract_r(dim, dens_buf, masks, 0, 0, 0, NULL, NULL, NULL, NULL, NULL, NULL, &cnt);
-        int64_t vcap = cnt.n_verts, icap = cnt.n_idx;
-        float* vp = (float*)malloc((size_t)(vcap ? vcap : 1) * 3 * sizeof(float));
-        float* vn = (float*)calloc((size_t)(vcap ? vcap : 1) * 3, sizeof(float));
-        uint8_t* vb = (uint8_t*)malloc((size_t)(vcap ? vcap : 1));
-        uint8_t* vv = (uint8_t*)malloc((size_t)(vcap ? vcap : 1));
-        uint32_t* ix = (uint32_t*)malloc((size_t)(icap ? icap : 1) * sizeof(uint32_t));
-        bmfo_extract_r(dim, dens_buf, masks, vcap, icap, 0, vp, vb, vv, ix, NULL, NULL, &c);
-        if (iters > 0) bmfo_process(3, c.n_verts, vp, vn, vb, vv, c.n_idx, ix, iters, 0, smooth_normals);
-        free(masks); free(vp); free(vn); free(vb); free(vv); free(ix);
       } else {
         bmfo_extract_q(dim, dens_buf, words, placement, 0, 0, NULL, NULL, NULL, NULL, &cnt);
-        int64_t vcap = cnt.n_verts, icap = cnt.n_idx;
-        float* vp = (float*)malloc((size_t)(vcap ? vcap : 1) * 3 * sizeof(float));
-        float* vn = (float*)calloc((size_t)(vcap ? vcap : 1) * 3, sizeof(float));
-        uint8_t* vb = (uint8_t*)malloc((size_t)(vcap ? vcap : 1));
-        uint8_t* vv = (uint8_t*)malloc((size_t)(vcap ? vcap : 1));
-        uint32_t* ix = (uint32_t*)malloc((size_t)(icap ? icap : 1) * sizeof(uint32_t));
-        bmfo_extract_q(dim, dens_buf, words, placement, vcap, icap, vp, vb, vv, ix, &c);
-        if (iters > 0) bmfo_process(4, c.n_verts, vp, vn, vb, vv, c.n_idx, ix, iters, 0, smooth_normals);
-        free(vp); free(vn); free(vb); free(vv); free(ix);
       }
+      int64_t vcap = cnt.n_verts, icap = cnt.n_idx;
+      vp = (float*)malloc((size_t)(vcap ? vcap : 1) * 3 * sizeof(float));
+      vn = (float*)calloc((size_t)(vcap ? vcap : 1) * 3, sizeof(float));
+      vb = (uint8_t*)malloc((size_t)(vcap ? vcap : 1));
+      vv = (uint8_t*)malloc((size_t)(vcap ? vcap : 1));
+      ix = (uint32_t*)malloc((size_t)(icap ? icap : 1) * sizeof(uint32_t));
+      if (mode == 0)
+        bmfo_extract_r(dim, dens_buf, masks, vcap, icap, 0, vp, vb, vv, ix, NULL, NULL, &c);
+      else
+        bmfo_extract_q(dim, dens_buf, words, placement, vcap, icap, vp, vb, vv, ix, &c);
+      if (iters > 0)
+        bmfo_process(mode == 0 ? 3 : 4, c.n_verts, vp, vn, vb, vv, c.n_idx, ix, iters, process_boundary,
+                     smooth_normals);
+      free(masks);
     }
     if (out_counts) {
       out_counts[3 * i] = cm;
       out_counts[3 * i + 1] = c.n_verts;
       out_counts[3 * i + 2] = c.n_idx;
     }
+    if (out_digest) {
+      /* {indices, positions, boundary flags, normals} of the chunk's mesh */
+      out_digest[4 * i + 0] = bmfo_digest64(ix, c.n_idx * 4, 0);
+      out_digest[4 * i + 1] = bmfo_digest64(vp, c.n_verts * 12, 1);
+      out_digest[4 * i + 2] = bmfo_digest64(vb, c.n_verts, 0);
+      out_digest[4 * i + 3] = bmfo_digest64(vn, c.n_verts * 12, 1);
+    }
     total += c.n_verts;
+    free(vp); free(vn); free(vb); free(vv); free(ix);
     free(dens_buf);
     free(words);
   }
   return total;
+}
+
+int64_t bmfo_extract_batch(int n_chunks, const float* desc, int field, const float* params, int mode, int placement,
+                           int iters, int smooth_normals, int64_t* out_counts, int n_threads) {
+  return bmfo_extract_batch_digest(n_chunks, desc, field, params, mode, placement, iters, 0, smooth_normals,
+                                   out_counts, NULL, n_threads);
 }

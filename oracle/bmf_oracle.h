@@ -112,6 +112,14 @@ double bmfo_fit_loss_spheres_f64(int dim, const double* density, int iters, cons
  * vertices; per-chunk counts written to out_counts (3 per chunk). */
 int64_t bmfo_extract_batch(int n_chunks, const float* desc, int field, const float* params, int mode, int placement,
                            int iters, int smooth_normals, int64_t* out_counts, int n_threads);
+/* The same with MeshProcessor's process_boundary and, per chunk, four digests
+ * (bmfo_digest64 of the indices, positions, boundary flags and normals) in
+ * out_digest[4 * i ..] (nullable), for chunk-by-chunk parity checks of a
+ * whole update without keeping its meshes. */
+int64_t bmfo_extract_batch_digest(int n_chunks, const float* desc, int field, const float* params, int mode,
+                                  int placement, int iters, int process_boundary, int smooth_normals,
+                                  int64_t* out_counts, uint64_t* out_digest, int n_threads);
+uint64_t bmfo_digest64(const void* data, int64_t n_bytes, int f32_canon);
 
 #ifdef __cplusplus
 }

@@ -53,6 +53,11 @@ def lib():
         L.bmfo_format.argtypes = [i64, vp, vp, i64, vp, c_int, c_int, vp, vp, vp]
         L.bmfo_extract_batch.restype = i64
         L.bmfo_extract_batch.argtypes = [c_int, vp, c_int, vp, c_int, c_int, c_int, c_int, vp, c_int]
+        L.bmfo_extract_batch_digest.restype = i64
+        L.bmfo_extract_batch_digest.argtypes = [c_int, vp, c_int, vp, c_int, c_int, c_int, c_int, c_int, vp, vp,
+                                                c_int]
+        L.bmfo_digest64.restype = ctypes.c_uint64
+        L.bmfo_digest64.argtypes = [vp, i64, c_int]
         _lib = L
     return _lib
 
@@ -200,6 +205,39 @@ def extract_batch(desc, field, params, mode=0, placement=0, iters=0, smooth_norm
     tot = lib().bmfo_extract_batch(len(desc), _p(desc), field, _p(prm), mode, placement, iters,
                                    int(smooth_normals), _p(counts), n_threads)
     return int(tot), counts
+
+
+def extract_batch_digest(desc, field, params, mode=0, placement=0, iters=0, process_boundary=False,
+                         smooth_normals=False, n_threads=0):
+    """The CPU path over a batch with per-chunk digests.  Returns (counts (n, 3)
+    = {contains_mesh, vertices, indices}, digests (n, 4) uint64 = digest64 of
+    {indices, positions, boundary flags, normals})."""
+    desc = np.ascontiguousarray(desc, np.float32)
+    prm = np.zeros(8, np.float32)
+    prm[: len(params)] = params
+    counts = np.zeros((len(desc), 3), np.int64)
+    dig = np.zeros((len(desc), 4), np.uint64)
+    lib().bmfo_extract_batch_digest(len(desc), _p(desc), field, _p(prm), mode, placement, iters,
+                                    int(process_boundary), int(smooth_normals), _p(counts), _p(dig), n_threads)
+    return counts, dig
+
+
+def digest64(a, f32=None):
+    """The oracle's FNV-1a digest of an array's bytes (floats NaN-canonicalised)."""
+    a = np.ascontiguousarray(a)
+    if f32 is None:
+        f32 = a.dtype == np.float32
+    return int(lib().bmfo_digest64(_p(a) if a.size else None, a.nbytes, int(f32)))
+
+
+def chunk_digests(pos, idx, boundary, nrm):
+    """digest64 of one chunk's {indices, positions, boundary flags, normals} as
+    host arrays, in the order extract_batch_digest reports them."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    nv = pos.size // 3
+    nrm = np.zeros((nv, 3), np.float32) if nrm is None else np.ascontiguousarray(nrm, np.float32)
+    bnd = np.zeros(nv, np.uint8) if boundary is None else np.ascontiguousarray(boundary, np.uint8)
+    return (digest64(np.ascontiguousarray(idx).view(np.uint32)), digest64(pos), digest64(bnd), digest64(nrm))
 
 
 def fit_loss_f64(dim, density, iters, box, want_grad=False, near_branch=None):

@@ -12,7 +12,10 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_ref", "libbmf_ref.so")
-REF_SRC = os.environ.get("BMF_REFERENCE_SRC", "/root/reference/BinaryMeshFitting")
+# The reference sources: $BMF_REFERENCE_SRC, else a checkout named
+# reference/BinaryMeshFitting beside this repository's directory.
+REF_SRC = os.environ.get("BMF_REFERENCE_SRC") or os.path.normpath(
+    os.path.join(_HERE, "..", "..", "reference", "BinaryMeshFitting"))
 _lib = None
 
 

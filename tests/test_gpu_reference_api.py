@@ -63,3 +63,31 @@ def test_chunk_generator_process_queue_matches_per_chunk(ctx):
         np.testing.assert_array_equal(n.vi["pos"].cpu().numpy().view(np.uint32), O["pos"].view(np.uint32))
     assert gen.overlap_for(nodes[0]) == 0.0  # max level, no boundary processing
     assert gen.overlap_for(nodes[3]) == pytest.approx(0.045)
+
+
+def test_process_queue_reuses_its_plan(ctx):
+    """A second queue of the same shape swaps its descriptors into the kept
+    plan and replays the graph; its meshes match the oracle, and the first
+    queue's meshes (copied out of the arena) are unchanged."""
+    props = R.WorldProperties(max_level=3, process_iters=2, boundary_processing=False, smooth_normals=True)
+    gen = R.ChunkGenerator(props, R.Sampler(workloads.terrain_field()), dim=33)
+    q1 = [R.WorldOctreeNode(pos=(1000.0 + 64 * i, 16.0, 2000.0), size=64.0, level=2) for i in range(4)]
+    q2 = [R.WorldOctreeNode(pos=(3000.0, 40.0 - 32 * i, 100.0 + 32 * i), size=32.0, level=3) for i in range(4)]
+    gen.process_queue(q1)
+    first = [n.vi["pos"].clone() for n in q1]
+    gen.process_queue(q2)
+    assert gen.plans_reused == 1
+    for n, p in zip(q1, first):
+        assert n.vi["pos"].equal(p)
+    checked = 0
+    for n in q2:
+        delta, org = R.chunk_frame(n.pos, n.size, gen.overlap_for(n), 33)
+        O = _oracle_chunk(org, delta, 33, iters=2, normals=True)
+        if O is None:
+            assert len(n.vi["pos"]) == 0
+            continue
+        np.testing.assert_array_equal(n.vi["idx"].cpu().numpy().view(np.uint32), O["idx"])
+        np.testing.assert_array_equal(n.vi["pos"].cpu().numpy().view(np.uint32), O["pos"].view(np.uint32))
+        checked += 1
+    assert checked >= 2
+    gen.close()

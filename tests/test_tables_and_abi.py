@@ -10,7 +10,8 @@ from binarymeshfitting_gb300 import _lib, build
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 TABLES = os.path.join(ROOT, "binarymeshfitting_gb300", "csrc", "bmf_case_tables.h")
-REF_SRC = os.environ.get("BMF_REFERENCE_SRC", "/root/reference/BinaryMeshFitting")
+REF_SRC = os.environ.get("BMF_REFERENCE_SRC") or os.path.normpath(
+    os.path.join(ROOT, "..", "reference", "BinaryMeshFitting"))
 
 CORNERS = [(0, 4), (1, 5), (2, 6), (3, 7), (0, 2), (1, 3), (4, 6), (5, 7), (0, 1), (2, 3), (4, 5), (6, 7)]
 
