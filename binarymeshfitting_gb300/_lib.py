@@ -80,7 +80,8 @@ class LodParams(ctypes.Structure):
 
 
 class BatchTuning(ctypes.Structure):
-    _fields_ = [("fill_mode", c_int32), ("fill_run", c_int32), ("sweep_block", c_int32), ("reserved", c_int32 * 5)]
+    _fields_ = [("fill_mode", c_int32), ("fill_run", c_int32), ("sweep_block", c_int32), ("fill_band", c_int32),
+                ("reserved", c_int32 * 4)]
 
 
 class Config(ctypes.Structure):

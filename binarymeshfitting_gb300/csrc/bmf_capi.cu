@@ -89,6 +89,10 @@ struct bmf_batch {
   int fill_grid = 0;
   int fill_mode = 0;
   int fill_run = 16;  // the tile height the autotuner picks on the mixed-LOD update
+  // band fill (Mode R, terrain): exact densities only where the mesh reads
+  // them; d_exact is its per-sample exactness mask (words layout)
+  int fill_band = 0;
+  uint32_t* d_exact = nullptr;
   // Mode R work list, sized by the output capacity (vcap + icap / 3 + 1)
   uint2* d_clist = nullptr;
   int64_t clist_cap = 0;
@@ -608,6 +612,10 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
       return s;
     b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5]);
     b->fill_mode = 2;
+    if (b->opts.mode == BMF_MODE_R && fill_band_supported(b->field)) {
+      if ((s = bail(cudaMalloc(&b->d_exact, sizeof(uint32_t) * words), "exactness mask")) != BMF_OK) return s;
+      b->fill_band = 1;
+    }
   }
   *out = b;
   return BMF_OK;
@@ -637,11 +645,15 @@ bool batch_keys(const bmf_batch* b) {
 }
 
 // Density fill + occupancy words of a whole update.
+bool batch_band(const bmf_batch* b) {
+  return b->fill_band && b->d_exact && b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0;
+}
+
 void batch_fill(bmf_batch* b, cudaStream_t st) {
   if (b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0)
     launch_fill_terrain(b->fill_run, b->d_chunks, b->d_fill_items, b->n_fill_items,
                         b->fill_mode == 2 ? b->d_queue : nullptr, b->fill_grid, b->field, b->d_dens, b->d_words,
-                        b->d_flags, st);
+                        b->d_flags, batch_band(b) ? b->d_exact : nullptr, st);
   else
     launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
                         b->d_words, b->d_flags, st);
@@ -692,12 +704,14 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
   batch_fill(b, st);
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
+  const bool band = batch_band(b);
+  if (band) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_words, b->d_exact, b->d_dens, st);
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
              out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, batch_keys(b) ? b->d_vkey : nullptr};
-  int64_t k = 4 + launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units,
+  int64_t k = (band ? 5 : 4) + launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units,
                               b->d_words, b->d_dens, b->d_flags, b->ws, mo, b->d_totals, st);
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
@@ -839,7 +853,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   const bool proc = b->opts.iters > 0;
   if (batch_keys(b) && (s = batch_proc_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
   if ((s = batch_list_scratch(b, out->vcap, out->icap)) != BMF_OK) return s;
-  cudaEvent_t ev[7];
+  cudaEvent_t ev[8];
   for (auto& e : ev) BMF_CUDA(ctx, cudaEventCreate(&e));
   BMF_CUDA(ctx, cudaEventRecord(ev[0], st));
   BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
@@ -847,6 +861,9 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   BMF_CUDA(ctx, cudaEventRecord(ev[1], st));
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[2], st));
+  // the band fill's exact-density fix-up belongs to the fill stage
+  if (batch_band(b)) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_words, b->d_exact, b->d_dens, st);
+  BMF_CUDA(ctx, cudaEventRecord(ev[7], st));
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   BMF_CUDA(ctx, cudaEventRecord(ev[3], st));
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
@@ -868,9 +885,15 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   BMF_CUDA(ctx, cudaEventRecord(ev[6], st));
   BMF_CUDA(ctx, cudaEventSynchronize(ev[6]));
   BMF_CUDA(ctx, cudaPeekAtLastError());
-  for (int k = 0; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
+  float fix = 0.0f;
+  BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[0], ev[0], ev[1]));
+  BMF_CUDA(ctx, cudaEventElapsedTime(&fix, ev[2], ev[7]));
+  h_stage_ms[0] += fix;
+  BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[1], ev[1], ev[2]));
+  BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[2], ev[7], ev[3]));
+  for (int k = 3; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
-  ctx->launches += 4 + ek + pk;
+  ctx->launches += (batch_band(b) ? 5 : 4) + ek + pk;
   return BMF_OK;
 }
 
@@ -896,6 +919,7 @@ bmf_status bmf_batch_get_tuning(const bmf_batch* b, bmf_batch_tuning* t) {
   t->fill_mode = b->fill_mode;
   t->fill_run = b->fill_run;
   t->sweep_block = b->ps.block > 0 ? b->ps.block : 256;
+  t->fill_band = b->fill_band;
   return BMF_OK;
 }
 
@@ -905,11 +929,13 @@ bmf_status bmf_batch_set_tuning(bmf_batch* b, const bmf_batch_tuning* t) {
   const bool terrain = b->field.kind == BMF_FIELD_TERRAIN_FBM;
   if (t->fill_mode < 0 || t->fill_mode > 2 || (!terrain && t->fill_mode != 0) ||
       (t->fill_run != 4 && t->fill_run != 8 && t->fill_run != 16) ||
-      (t->sweep_block != 128 && t->sweep_block != 256 && t->sweep_block != 512))
+      (t->sweep_block != 128 && t->sweep_block != 256 && t->sweep_block != 512) ||
+      (t->fill_band != 0 && t->fill_band != 1) || (t->fill_band && !b->d_exact))
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
                 "bmf_batch_set_tuning: fill_mode 0..2 (1, 2 for terrain fields only), fill_run 4/8/16, "
-                "sweep_block 128/256/512");
+                "sweep_block 128/256/512, fill_band 0/1 (1 for Mode R terrain plans only)");
   b->fill_mode = t->fill_mode;
+  b->fill_band = t->fill_band;
   if (t->fill_run != b->fill_run) {
     b->fill_run = t->fill_run;
     if (terrain) b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5]);
@@ -1218,7 +1244,7 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
                   b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
                   b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey,
-                  b->d_fill_items, b->d_queue, b->d_order, b->d_pqueue, b->d_clist};
+                  b->d_fill_items, b->d_queue, b->d_order, b->d_pqueue, b->d_clist, b->d_exact};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);

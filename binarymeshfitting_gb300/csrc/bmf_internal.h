@@ -77,9 +77,17 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
 // each; d_items null = chunk 0's items in order).  d_queue non-null: grid
 // persistent CTAs take items from the queue (reset here); else one CTA per item.
 // run = z-samples per step (4, 8, 16 or 32).
+// exact (nullable): the band fill's exactness mask (words layout); with it
+// the fill may leave decided samples inexact (see k_fill_terrain<RUN, true>)
 void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,
                          int grid, const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
-                         cudaStream_t st);
+                         uint32_t* exact, cudaStream_t st);
+// the band fill applies to fields of the form (py - h) - a * FBM with a > 0
+bool fill_band_supported(const FieldDev& field);
+// exact densities at both ends of every crossing of the Mode R busy-word list
+// whose band-fill value is inexact (after launch_count, before launch_emit)
+void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, const uint32_t* words,
+                       const uint32_t* exact, float* dens, cudaStream_t st);
 int fill_terrain_items(int dim);          // items of one chunk
 int fill_terrain_lines();                 // lines per item
 int fill_terrain_resident_ctas(int run, int octaves);  // persistent grid: SMs x resident CTAs per SM

@@ -176,6 +176,25 @@ __device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const float4* _
   s.Zp = Z;
 }
 
+// Band fill (BAND = true).  The terrain density is d = (py - h) - a * FBM with
+// py constant along a line, and every octave's noise is bounded: the corner
+// weights of a sample sum to one and a corner's gradient dot product is at
+// most |dx| + |dy| + |dz|, whose weighted sums are each at most 1/2
+// (x (1 - fade x) + (1 - x) fade x <= 1/2), so |noise| <= 3/2.  Before each
+// octave o a run therefore knows its FBM sums to within
+// T_o = 3/2 * sum_{j >= o} |amp_j|: when every sample's partial sum S lies
+// below (py - h) / a - T_o (all outside) or above (py - h) / a + T_o (all
+// inside), the signs -- the occupancy words -- are final and the run stops.
+// Its samples then hold the partial density (right sign, inexact value) and
+// clear their bits in the `exact` mask (laid out like the words); the mesh
+// only reads densities at the ends of sign-changing edges, and
+// k_fill_fixup recomputes those that are inexact before the emit runs, with
+// the same operations, so the output is bit-identical to a full fill.
+// Lanes take the lines of an item y-major (x fastest), so a warp's lanes
+// share py and mostly stop at the same octave.
+constexpr float kNoiseBound = 1.5f;
+constexpr float kBandMargin = 1e-3f;  // float rounding of the sums, far below this
+
 // Dynamic shared memory: the density stage (16-sample half blocks of the
 // CTA's lines, rows padded to 17 floats) and, for up to kCacheOctaves
 // octaves, each line's lattice-cell state (alpha / beta pairs and Zp) carried
@@ -188,16 +207,18 @@ __host__ __device__ constexpr size_t fill_smem_bytes(int octaves) {
          (octaves <= kCacheOctaves ? (size_t)octaves * kFillLines * (sizeof(float4) + sizeof(int)) : 0);
 }
 
-template <int kFillRun>
+template <int kFillRun, bool BAND>
 __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* __restrict__ chunks,
                                                              const int2* __restrict__ items, int n_items,
                                                              int* __restrict__ queue, FieldDev field,
                                                              float* __restrict__ dens_out,
                                                              uint32_t* __restrict__ words,
-                                                             uint32_t* __restrict__ flags) {
+                                                             uint32_t* __restrict__ flags,
+                                                             uint32_t* __restrict__ exact) {
   __shared__ int perm2[512];
   __shared__ float4 gtab[512];
   __shared__ float4 zt[kZtEntries];
+  __shared__ float s_tail[kMaxOctaves + 1];  // band test: T_o + margin
   // density of the CTA's lines for one 16-sample half block, flushed with
   // coalesced 64-byte row stores (rows padded to 17: conflict-free columns)
   extern __shared__ float4 s_dyn[];
@@ -212,6 +233,18 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
   const bool cache = oct <= kCacheOctaves;
   float4* s_ab = s_dyn + kStageFloats / 4;                      // [octave][line]: a0, b0, a1, b1
   int* s_zp = reinterpret_cast<int*>(s_ab + (size_t)oct * kFillLines);  // [octave][line]: Zp
+  if (BAND && threadIdx.x == 0) {
+    // T_o = 3/2 sum_{j >= o} |amp_j|: the total, then less one octave at a
+    // time (rounding far below the margin)
+    float tot = 0.0f, a = 1.0f;
+    for (int o = 0; o < oct; ++o, a = a * gain) tot += fabsf(a) * kNoiseBound;
+    a = 1.0f;
+    for (int o = 0; o < oct; ++o, a = a * gain) {
+      s_tail[o] = tot + kBandMargin;
+      tot -= fabsf(a) * kNoiseBound;
+    }
+    s_tail[oct] = kBandMargin;
+  }
   for (int pass = 0;; ++pass) {
     __syncthreads();
     if (threadIdx.x == 0) s_item = queue ? atomicAdd(queue, 1) : (pass == 0 ? (int)blockIdx.x : n_items);
@@ -221,11 +254,30 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
     const int2 item = items ? items[it] : make_int2(0, it * kFillLines);
     const ChunkDev ch = chunks[item.x];
     const int dim = ch.dim, zc = ch.zc;
-    const int line = item.y + (int)threadIdx.x;
-    const bool active = line < dim * dim;
-    const int x = active ? line / dim : 0, y = active ? line - x * dim : 0;
+    // the thread's line: item.y + thread in x-major order (line = x * dim + y),
+    // or, for the band fill, in y-major order (x fastest: a warp shares y)
+    const int lidx = item.y + (int)threadIdx.x;
+    const bool active = lidx < dim * dim;
+    int x = 0, y = 0;
+    if (active) {
+      if (BAND) {
+        y = lidx / dim;
+        x = lidx - y * dim;
+      } else {
+        x = lidx / dim;
+        y = lidx - x * dim;
+      }
+    }
+    const int line = x * dim + y;  // in memory
     const float px = ch.ox + (float)x * ch.scale, py = ch.oy + (float)y * ch.scale;
     uint32_t* wline = words + ch.words + (int64_t)line * zc;
+    uint32_t* eline = BAND ? exact + ch.words + (int64_t)line * zc : nullptr;
+    // band test of this line: S below ca - tail (all outside) or above ca + tail (all inside)
+    const float ca = BAND ? (py - h0) / ampl : 0.0f;
+    const float caM = BAND ? 1e-6f * fabsf(ca) : 0.0f;
+    if (BAND && cache) {  // no cell state carried in from the previous item
+      for (int o = 0; o < oct; ++o) s_zp[o * kFillLines + (int)threadIdx.x] = -1;
+    }
     // the z terms depend on the chunk only: all of them once per item when they fit
     const bool whole = oct * dim <= kZtEntries;
     // dim = RUN k + 1 (33, 65, 129, ...): the line's last sample is evaluated
@@ -245,7 +297,7 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
         zt[e] = make_float4(zf, zf - 1.0f, fade(zf), __int_as_float(((int)fz) & 255));
       }
     }
-    uint32_t wacc = 0u, fl = 0u;
+    uint32_t wacc = 0u, eacc = 0u, fl = 0u;
     for (int zr = 0; zr < nruns; ++zr) {
       const int z0 = zr * kFillRun, n = min(kFillRun, dim - z0);
       if (!whole || zr == 0) __syncthreads();
@@ -267,14 +319,18 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
       float* row = s_stage + threadIdx.x * kStageRow + (z0 & 15);
       const bool tail = fold && zr == nruns - 1;  // sample z0 + RUN too
       uint32_t tail_bit = 0u;
+      bool run_exact = true;
       if (n == kFillRun) {
         // a full run: RUN samples per octave, unrolled, no tail guards
         float sum[kFillRun], sum_t = 0.0f;
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) sum[k] = 0.0f;
         float amp = 1.0f, fr = freq;
+        // band: the whole line may be decided before any octave
+        const int o_end = (BAND && (ca - s_tail[0] - caM > 0.0f || ca + s_tail[0] + caM < 0.0f)) ? 0 : oct;
+        if (BAND && o_end == 0) run_exact = false;
 #pragma unroll 1
-        for (int o = 0; o < oct; ++o) {
+        for (int o = 0; o < o_end; ++o) {
           OctLine L;
           oct_line_init(L, px, py, fr, perm2);
           const int si = o * kFillLines + (int)threadIdx.x;
@@ -310,6 +366,24 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
           if (cache) {
             s_ab[si] = make_float4(L.a0, L.b0, L.a1, L.b1);
             s_zp[si] = L.Zp;
+          }
+          if (BAND && o + 1 < oct) {
+            // every sample decided by octaves 0..o: the rest cannot change a sign
+            float mn = sum[0], mx = sum[0];
+#pragma unroll
+            for (int k = 1; k < kFillRun; ++k) {
+              mn = fminf(mn, sum[k]);
+              mx = fmaxf(mx, sum[k]);
+            }
+            if (tail) {
+              mn = fminf(mn, sum_t);
+              mx = fmaxf(mx, sum_t);
+            }
+            const float tb = s_tail[o + 1] + caM;
+            if (mx < ca - tb || mn > ca + tb) {
+              run_exact = false;
+              break;
+            }
           }
           fr = fr * lac;
           amp = amp * gain;
@@ -363,15 +437,23 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
         }
       }
       wacc |= bits << (z0 & 31);
+      const uint32_t ebits = run_exact ? (n >= 32 ? kFull : ((1u << n) - 1u)) : 0u;
+      if (BAND) eacc |= ebits << (z0 & 31);
       const int tz = z0 + kFillRun;  // the folded sample, in this word or the next
-      if (tail && (tz & 31) != 0) wacc |= tail_bit << (tz & 31);
+      if (tail && (tz & 31) != 0) {
+        wacc |= tail_bit << (tz & 31);
+        if (BAND && run_exact) eacc |= 1u << (tz & 31);
+      }
       if (((z0 + kFillRun) & 31) == 0 || zr == nruns - 1) {
         wline[z0 >> 5] = wacc;
+        if (BAND) eline[z0 >> 5] = eacc;
         fl |= (wacc != 0u && wacc != kFull) ? 1u : (wacc == kFull ? 2u : 4u);
         wacc = 0u;
+        eacc = 0u;
       }
       if (tail && (tz & 31) == 0) {
         wline[tz >> 5] = tail_bit;
+        if (BAND) eline[tz >> 5] = run_exact ? 1u : 0u;
         fl |= tail_bit ? 1u : 4u;  // a one-sample word: any value but all-ones
       }
       }  // active
@@ -384,12 +466,27 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
         const int l0 = (int)(threadIdx.x & ~31) + (lane >> 4);  // this lane's first row
         // rows left for this lane (every second row from l0), 0 past the chunk's lines or columns
         const int nrow = col < nz ? min(16, (dim * dim - item.y - l0 + 1) >> 1) : 0;
-        float* gp = dens_out + ch.dens + (int64_t)(item.y + l0) * dim + zh0 + col;
         const float* sp = s_stage + l0 * kStageRow + col;
+        if (BAND) {
+          // y-major rows: row l0 + 2j is line (xr, yr) with xr stepping by 2
+          const int lr = item.y + l0;
+          int yr = lr / dim, xr = lr - yr * dim;
 #pragma unroll 4
-        for (int j = 0; j < 16; ++j) {
-          if (j < nrow) *gp = sp[2 * kStageRow * j];
-          gp += 2 * dim;
+          for (int j = 0; j < 16; ++j) {
+            if (j < nrow) dens_out[ch.dens + ((int64_t)xr * dim + yr) * dim + zh0 + col] = sp[2 * kStageRow * j];
+            xr += 2;
+            if (xr >= dim) {
+              xr -= dim;
+              ++yr;
+            }
+          }
+        } else {
+          float* gp = dens_out + ch.dens + (int64_t)(item.y + l0) * dim + zh0 + col;
+#pragma unroll 4
+          for (int j = 0; j < 16; ++j) {
+            if (j < nrow) *gp = sp[2 * kStageRow * j];
+            gp += 2 * dim;
+          }
         }
         __syncthreads();  // the next half block's rows overwrite the stage
       }
@@ -407,27 +504,138 @@ static void fill_terrain_smem_optin() {
   static std::atomic<int> done[64] = {};
   per_device_once(done, [](int) {
     const int mx = (int)fill_smem_bytes(kCacheOctaves);
-    cudaFuncSetAttribute(k_fill_terrain<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_fill_terrain<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_fill_terrain<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<8, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_fill_terrain<16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     return 1;
   });
 }
 
+template <bool BAND>
+static void fill_terrain_run(int run, int g, size_t sm, cudaStream_t st, const ChunkDev* d_chunks,
+                             const int2* d_items, int n_items, int* d_queue, const FieldDev& field, float* dens_out,
+                             uint32_t* words, uint32_t* flags, uint32_t* exact) {
+  if (run == 4)
+    k_fill_terrain<4, BAND><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words,
+                                                       flags, exact);
+  else if (run == 16)
+    k_fill_terrain<16, BAND><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words,
+                                                        flags, exact);
+  else
+    k_fill_terrain<8, BAND><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words,
+                                                       flags, exact);
+}
+
 void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,
                          int grid, const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
-                         cudaStream_t st) {
+                         uint32_t* exact, cudaStream_t st) {
   if (n_items <= 0) return;
   if (d_queue) cudaMemsetAsync(d_queue, 0, sizeof(int), st);
   const int g = d_queue ? grid : n_items;
   fill_terrain_smem_optin();
   const size_t sm = fill_smem_bytes(min((int)field.p[5], kMaxOctaves));
-  if (run == 4)
-    k_fill_terrain<4><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
-  else if (run == 16)
-    k_fill_terrain<16><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+  if (exact && dens_out)
+    fill_terrain_run<true>(run, g, sm, st, d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags, exact);
   else
-    k_fill_terrain<8><<<g, kFillLines, sm, st>>>(d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags);
+    fill_terrain_run<false>(run, g, sm, st, d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags,
+                            nullptr);
+}
+
+bool fill_band_supported(const FieldDev& field) {
+  return field.kind == BMF_FIELD_TERRAIN_FBM && field.p[1] > 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Exact densities where the band fill left a decided sample inexact but the
+// mesh reads it: the two ends of every sign-changing grid edge.  One thread
+// per busy word of the Mode R work list (entry = chunk, x * dim * zc + word
+// of line): the word owns the crossings X (to x + 1), Y (to y + 1) and Z (to
+// z + 1) of its 32 samples (the same bits as k_count), so it checks both ends
+// of each.  A sample shared by several crossings may be recomputed by
+// several threads; they store the same value.
+// ---------------------------------------------------------------------------
+// The exact terrain density of one sample: per octave the line's x/y terms,
+// the z terms and both z-layers of its lattice cell, combined with the
+// operations of k_fill_terrain's run loop, in the same order.
+__device__ float terrain_exact(const FieldDev& f, const int* __restrict__ perm2, const float4* __restrict__ gtab,
+                               const ChunkDev& ch, int x, int y, int z) {
+  const int oct = min((int)f.p[5], kMaxOctaves);
+  const float h0 = f.p[0], ampl = f.p[1], freq = f.p[2], lac = f.p[3], gain = f.p[4];
+  const float px = ch.ox + (float)x * ch.scale, py = ch.oy + (float)y * ch.scale;
+  const float pz = ch.oz + (float)z * ch.scale;
+  float sum = 0.0f, amp = 1.0f, fr = freq;
+  for (int o = 0; o < oct; ++o) {
+    OctLine L;
+    oct_line_init(L, px, py, fr, perm2);
+    const float zs = pz * fr;
+    const float fz = floorf(zs);
+    const float zf = zs - fz;
+    oct_line_cell(L, ((int)fz) & 255, gtab);
+    const float l0 = __fmaf_rn(L.b0, zf, L.a0);
+    const float l1 = __fmaf_rn(L.b1, zf - 1.0f, L.a1);
+    sum = __fmaf_rn(amp, __fmaf_rn(fade(zf), l1 - l0, l0), sum);
+    fr = fr * lac;
+    amp = amp * gain;
+  }
+  return __fmaf_rn(-ampl, sum, py - h0);
+}
+
+__device__ __forceinline__ uint32_t band_zbits_upto(int hi, int zb) {  // bits l with 32 zb + l <= hi
+  const int n = hi - 32 * zb + 1;
+  return n >= 32 ? kFull : (n <= 0 ? 0u : ((1u << n) - 1u));
+}
+
+__global__ void __launch_bounds__(256) k_fill_fixup(const ChunkDev* __restrict__ chunks, const uint2* __restrict__ list,
+                                                    const uint32_t* __restrict__ count, int64_t cap, FieldDev field,
+                                                    const uint32_t* __restrict__ words,
+                                                    const uint32_t* __restrict__ exact, float* __restrict__ dens) {
+  __shared__ int perm2[512];
+  __shared__ float4 gtab[512];
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) {
+    perm2[i] = field.perm[i & 255];
+    gtab[i] = grad_coeffs(field.perm[i & 255]);
+  }
+  __syncthreads();
+  const int64_t n = min((int64_t)*count, cap);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const uint2 ent = list[e];
+    const ChunkDev ch = chunks[ent.x];
+    const int dim = ch.dim, zc = ch.zc, nw = dim * zc;
+    const int x = (int)(ent.y / (uint32_t)nw), wi = (int)ent.y - x * nw;
+    const int y = wi / zc, zb = wi - y * zc;
+    const int64_t o00 = ch.words + ((int64_t)x * dim + y) * zc + zb;
+    const bool xin = x + 1 < dim, yin = y + 1 < dim, nin = zb + 1 < zc;
+    const uint32_t w00 = words[o00], n00 = nin ? words[o00 + 1] : 0u;
+    const uint32_t X = xin ? (w00 ^ words[o00 + (int64_t)dim * zc]) : 0u;
+    const uint32_t Y = yin ? (w00 ^ words[o00 + zc]) : 0u;
+    const uint32_t Z = (w00 ^ ((w00 >> 1) | (n00 << 31))) & band_zbits_upto(dim - 2, zb);
+    // ends of the crossings that are inexact: this line, line x + 1, line y + 1, next word
+    auto fix = [&](uint32_t m, int xs, int ys, int z0) {
+      for (; m; m &= m - 1u) {
+        const int zs = z0 + __ffs(m) - 1;
+        dens[ch.dens + ((int64_t)xs * dim + ys) * dim + zs] = terrain_exact(field, perm2, gtab, ch, xs, ys, zs);
+      }
+    };
+    fix((X | Y | Z | (Z << 1)) & ~exact[o00], x, y, 32 * zb);
+    if (X) fix(X & ~exact[o00 + (int64_t)dim * zc], x + 1, y, 32 * zb);
+    if (Y) fix(Y & ~exact[o00 + zc], x, y + 1, 32 * zb);
+    if (Z >> 31) fix(~exact[o00 + 1] & 1u, x, y, 32 * zb + 32);
+  }
+}
+
+void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, const uint32_t* words,
+                       const uint32_t* exact, float* dens, cudaStream_t st) {
+  static std::atomic<int> grid[64] = {};
+  const int g = per_device_once(grid, [](int dev) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_fixup, 256, 0);
+    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  });
+  k_fill_fixup<<<g, 256, 0, st>>>(d_chunks, ws.clist, ws.ccount, ws.clist_cap, field, words, exact, dens);
 }
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
@@ -439,11 +647,11 @@ int fill_terrain_resident_ctas(int run, int octaves) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   fill_terrain_smem_optin();
   if (run == 4)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4>, kFillLines, sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4, true>, kFillLines, sm);
   else if (run == 16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16>, kFillLines, sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16, true>, kFillLines, sm);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8>, kFillLines, sm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8, true>, kFillLines, sm);
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 
@@ -484,7 +692,7 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
                          uint32_t* flags, cudaStream_t st) {
   if (field.kind == BMF_FIELD_TERRAIN_FBM && n_chunks == 1) {
     launch_fill_terrain(16, d_chunks, nullptr, fill_terrain_items(max_dim), nullptr, 0, field, dens_out, words, flags,
-                        st);
+                        nullptr, st);
     return;
   }
   const int max_zc = (max_dim + 31) / 32;

@@ -277,9 +277,9 @@ class Batch:
         """The plan's launch tuning as a dict (bmf_batch_tuning)."""
         t = L.BatchTuning()
         self.ctx._check(self.ctx.lib.bmf_batch_get_tuning(self.h, ctypes.byref(t)))
-        return dict(fill_mode=t.fill_mode, fill_run=t.fill_run, sweep_block=t.sweep_block)
+        return dict(fill_mode=t.fill_mode, fill_run=t.fill_run, sweep_block=t.sweep_block, fill_band=t.fill_band)
 
-    def set_tuning(self, fill_mode=None, fill_run=None, sweep_block=None):
+    def set_tuning(self, fill_mode=None, fill_run=None, sweep_block=None, fill_band=None):
         t = L.BatchTuning()
         self.ctx._check(self.ctx.lib.bmf_batch_get_tuning(self.h, ctypes.byref(t)))
         if fill_mode is not None:
@@ -288,6 +288,8 @@ class Batch:
             t.fill_run = fill_run
         if sweep_block is not None:
             t.sweep_block = sweep_block
+        if fill_band is not None:
+            t.fill_band = fill_band
         self.ctx._check(self.ctx.lib.bmf_batch_set_tuning(self.h, ctypes.byref(t)))
 
     def autotune(self, reps=3, stream=None):
@@ -298,7 +300,7 @@ class Batch:
         n = ctypes.c_int32(0)
         self.ctx._check(self.ctx.lib.bmf_batch_autotune(self.h, ctypes.byref(self.out), reps, _stream(stream),
                                                         ctypes.byref(t), ms, 16, ctypes.byref(n)))
-        return (dict(fill_mode=t.fill_mode, fill_run=t.fill_run, sweep_block=t.sweep_block),
+        return (dict(fill_mode=t.fill_mode, fill_run=t.fill_run, sweep_block=t.sweep_block, fill_band=t.fill_band),
                 [float(ms[i]) for i in range(min(n.value, 16))])
 
     def chunk_mesh(self, i):

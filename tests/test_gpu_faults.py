@@ -25,15 +25,25 @@ BAD_DESCS = [((math.nan, 0.0, 0.0), 1.0, 33), ((0.0, math.inf, 0.0), 1.0, 33), (
 
 @pytest.mark.parametrize("origin,scale,dim", BAD_DESCS)
 def test_corrupt_descriptor_is_rejected_everywhere(ctx, origin, scale, dim):
+    """Called straight through the C ABI with small buffers: the library
+    rejects the descriptor before it sizes or touches anything."""
     desc = L.ChunkDesc.make(origin, scale, dim)
     field = workloads.terrain_field()
     good = L.ChunkDesc.make((0.0, 48.0, 0.0), 1.0, 33)  # holds the terrain surface
-    out = torch.empty(33 ** 3, device="cuda")
-    for call in (lambda: ctx.sample_block(desc, field, out=out), lambda: ctx.sample_label(desc, field),
-                 lambda: ctx.extract_chunk(desc, field, iters=2)):
-        with pytest.raises(L.BmfError) as e:
-            call()
-        assert e.value.status == L.ERR_INVALID_ARGUMENT
+    lib, h = ctx.lib, ctx.h
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    buf = torch.empty(33 ** 3, device="cuda")
+    words = torch.empty(33 * 33 * 2, dtype=torch.int32, device="cuda")
+    cm = ctypes.c_int32(0)
+    m, _ = ctx._alloc_mesh(4096, 16384, True)
+    opts = L.ExtractOpts(L.MODE_R, 0, 2, 0, 1, 0)
+    for status in (lib.bmf_sample_block(h, ctypes.byref(desc), ctypes.byref(field), ctypes.c_void_p(buf.data_ptr()),
+                                        st),
+                   lib.bmf_sample_label(h, ctypes.byref(desc), ctypes.byref(field), ctypes.c_void_p(buf.data_ptr()),
+                                        ctypes.c_void_p(words.data_ptr()), ctypes.byref(cm), st),
+                   lib.bmf_extract_chunk(h, ctypes.byref(desc), ctypes.byref(field), ctypes.byref(opts),
+                                         ctypes.byref(m), st)):
+        assert status == L.ERR_INVALID_ARGUMENT
     # one bad descriptor among good ones fails the whole plan, naming the chunk
     with pytest.raises(L.BmfError) as e:
         Batch(ctx, [good, good, desc, good], field)

@@ -319,17 +319,19 @@ def test_batch_tunings_give_identical_results(ctx):
     descs, rows = _small_batch()
     b = Batch(ctx, descs, workloads.terrain_field(), mode=L.MODE_R, iters=4, smooth_normals=True)
     bufs = b.allocate(400000, 2400000, normals=True)
-    assert b.tuning() == dict(fill_mode=2, fill_run=16, sweep_block=256)
+    assert b.tuning() == dict(fill_mode=2, fill_run=16, sweep_block=256, fill_band=1)
+    b.set_tuning(fill_band=0)  # the reference arena: every density exact
     nv, ni = b.run(use_graph=True)
     ref = [bufs[k][:n].clone() for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"].clone()]
-    for fm, fr, sb in [(0, 8, 256), (1, 4, 128), (1, 16, 512), (2, 4, 256), (2, 16, 128), (1, 8, 512)]:
-        b.set_tuning(fill_mode=fm, fill_run=fr, sweep_block=sb)
+    for fm, fr, sb, band in [(0, 8, 256, 0), (1, 4, 128, 1), (1, 16, 512, 0), (2, 4, 256, 1), (2, 16, 128, 1),
+                             (1, 8, 512, 1), (2, 8, 256, 1), (2, 16, 256, 0)]:
+        b.set_tuning(fill_mode=fm, fill_run=fr, sweep_block=sb, fill_band=band)
         for use_graph in (False, True):
             assert b.run(use_graph=use_graph) == (nv, ni)
             got = [bufs[k][:n] for k, n in (("pos", nv), ("nrm", nv), ("idx", ni))] + [bufs["info"]]
             for r, g_ in zip(ref, got):
                 assert torch.equal(r.view(torch.int32) if r.is_floating_point() else r,
-                                   g_.view(torch.int32) if g_.is_floating_point() else g_), (fm, fr, sb)
+                                   g_.view(torch.int32) if g_.is_floating_point() else g_), (fm, fr, sb, band)
     chosen, ms = b.autotune(reps=2)
     assert len(ms) == 10 and all(m > 0 for m in ms)
     assert chosen["fill_mode"] in (0, 1, 2) and chosen["sweep_block"] in (128, 256, 512)
