@@ -610,12 +610,12 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
     if ((s = bail(cudaMemcpy(b->d_fill_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice),
                   "upload fill items")) != BMF_OK)
       return s;
-    b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5]);
     b->fill_mode = 2;
     if (b->opts.mode == BMF_MODE_R && fill_band_supported(b->field)) {
       if ((s = bail(cudaMalloc(&b->d_exact, sizeof(uint32_t) * words), "exactness mask")) != BMF_OK) return s;
       b->fill_band = 1;
     }
+    b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5], b->fill_band != 0);
   }
   *out = b;
   return BMF_OK;
@@ -935,10 +935,10 @@ bmf_status bmf_batch_set_tuning(bmf_batch* b, const bmf_batch_tuning* t) {
                 "bmf_batch_set_tuning: fill_mode 0..2 (1, 2 for terrain fields only), fill_run 4/8/16, "
                 "sweep_block 128/256/512, fill_band 0/1 (1 for Mode R terrain plans only)");
   b->fill_mode = t->fill_mode;
-  b->fill_band = t->fill_band;
-  if (t->fill_run != b->fill_run) {
+  if (t->fill_run != b->fill_run || t->fill_band != b->fill_band) {
     b->fill_run = t->fill_run;
-    if (terrain) b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5]);
+    b->fill_band = t->fill_band;
+    if (terrain) b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5], b->fill_band != 0);
   }
   b->ps.block = t->sweep_block;
   if (b->exec) {

@@ -90,7 +90,7 @@ void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const Fi
                        const uint32_t* exact, float* dens, cudaStream_t st);
 int fill_terrain_items(int dim);          // items of one chunk
 int fill_terrain_lines();                 // lines per item
-int fill_terrain_resident_ctas(int run, int octaves);  // persistent grid: SMs x resident CTAs per SM
+int fill_terrain_resident_ctas(int run, int octaves, bool band);  // persistent grid: SMs x resident CTAs per SM
 void launch_cell_masks(int dim, const uint32_t* W, uint8_t* masks, cudaStream_t st);
 // contains_mesh flags of chunks whose words were produced elsewhere.
 void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, uint32_t* flags,

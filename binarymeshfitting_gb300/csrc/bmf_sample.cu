@@ -192,23 +192,29 @@ __device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const float4* _
 // the same operations, so the output is bit-identical to a full fill.
 // Lanes take the lines of an item y-major (x fastest), so a warp's lanes
 // share py and mostly stop at the same octave.
+#ifndef BMF_BAND_CTAS
+#define BMF_BAND_CTAS 3
+#endif
+constexpr int kBandCtas = BMF_BAND_CTAS;  // resident CTAs per SM the band fill's registers are sized for
 constexpr float kNoiseBound = 1.5f;
 constexpr float kBandMargin = 1e-3f;  // float rounding of the sums, far below this
 
 // Dynamic shared memory: the density stage (16-sample half blocks of the
-// CTA's lines, rows padded to 17 floats) and, for up to kCacheOctaves
-// octaves, each line's lattice-cell state (alpha / beta pairs and Zp) carried
-// from one run to the next, so a run re-enters a cell only when Z changes.
+// CTA's lines, rows padded to 17 floats; not used by the band fill, which
+// stores only its exact runs, straight from registers) and, for up to
+// kCacheOctaves octaves, each line's lattice-cell state (alpha / beta pairs
+// and Zp) carried from one run to the next, so a run re-enters a cell only
+// when Z changes.
 constexpr int kStageRow = 17;
 constexpr int kCacheOctaves = 8;
 constexpr size_t kStageFloats = (size_t)kFillLines * kStageRow;
-__host__ __device__ constexpr size_t fill_smem_bytes(int octaves) {
-  return sizeof(float) * kStageFloats +
+__host__ __device__ constexpr size_t fill_smem_bytes(int octaves, bool band) {
+  return (band ? 0 : sizeof(float) * kStageFloats) +
          (octaves <= kCacheOctaves ? (size_t)octaves * kFillLines * (sizeof(float4) + sizeof(int)) : 0);
 }
 
 template <int kFillRun, bool BAND>
-__global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* __restrict__ chunks,
+__global__ void __launch_bounds__(kFillLines, BAND ? kBandCtas : 3) k_fill_terrain(const ChunkDev* __restrict__ chunks,
                                                              const int2* __restrict__ items, int n_items,
                                                              int* __restrict__ queue, FieldDev field,
                                                              float* __restrict__ dens_out,
@@ -231,7 +237,7 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
   const int oct = min((int)field.p[5], kMaxOctaves);
   const float h0 = field.p[0], ampl = field.p[1], freq = field.p[2], lac = field.p[3], gain = field.p[4];
   const bool cache = oct <= kCacheOctaves;
-  float4* s_ab = s_dyn + kStageFloats / 4;                      // [octave][line]: a0, b0, a1, b1
+  float4* s_ab = s_dyn + (BAND ? 0 : kStageFloats / 4);          // [octave][line]: a0, b0, a1, b1
   int* s_zp = reinterpret_cast<int*>(s_ab + (size_t)oct * kFillLines);  // [octave][line]: Zp
   if (BAND && threadIdx.x == 0) {
     // T_o = 3/2 sum_{j >= o} |amp_j|: the total, then less one octave at a
@@ -317,6 +323,7 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
       if (active) {
       uint32_t bits = 0u;
       float* row = s_stage + threadIdx.x * kStageRow + (z0 & 15);
+      float* grow = BAND ? dens_out + ch.dens + (int64_t)line * dim + z0 : nullptr;  // band: direct stores
       const bool tail = fold && zr == nruns - 1;  // sample z0 + RUN too
       uint32_t tail_bit = 0u;
       bool run_exact = true;
@@ -391,12 +398,15 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
 #pragma unroll
         for (int k = 0; k < kFillRun; ++k) {
           const float d = __fmaf_rn(-ampl, sum[k], py - h0);
-          row[k] = d;
+          if (!BAND)
+            row[k] = d;
+          else if (run_exact)  // a decided run's inexact densities are never read: not stored
+            grow[k] = d;
           if (d < 0.0f) bits |= 1u << k;
         }
         if (tail) {  // outside the staged half block: stored directly
           const float d = __fmaf_rn(-ampl, sum_t, py - h0);
-          if (dens_out) dens_out[ch.dens + (int64_t)line * dim + z0 + kFillRun] = d;
+          if (dens_out && (!BAND || run_exact)) dens_out[ch.dens + (int64_t)line * dim + z0 + kFillRun] = d;
           tail_bit = d < 0.0f ? 1u : 0u;
         }
       } else {
@@ -432,7 +442,10 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
             amp = amp * gain;
           }
           const float d = __fmaf_rn(-ampl, sum, py - h0);
-          row[k] = d;
+          if (BAND)
+            grow[k] = d;
+          else
+            row[k] = d;
           if (d < 0.0f) bits |= 1u << k;
         }
       }
@@ -457,7 +470,7 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
         fl |= tail_bit ? 1u : 4u;  // a one-sample word: any value but all-ones
       }
       }  // active
-      if (dens_out && (((z0 + kFillRun) & 15) == 0 || zr == nruns - 1)) {
+      if (!BAND && dens_out && (((z0 + kFillRun) & 15) == 0 || zr == nruns - 1)) {
         // flush the half block: warp w writes rows [32w, 32w + 32), two
         // 16-sample row segments per instruction
         __syncthreads();
@@ -467,26 +480,11 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
         // rows left for this lane (every second row from l0), 0 past the chunk's lines or columns
         const int nrow = col < nz ? min(16, (dim * dim - item.y - l0 + 1) >> 1) : 0;
         const float* sp = s_stage + l0 * kStageRow + col;
-        if (BAND) {
-          // y-major rows: row l0 + 2j is line (xr, yr) with xr stepping by 2
-          const int lr = item.y + l0;
-          int yr = lr / dim, xr = lr - yr * dim;
+        float* gp = dens_out + ch.dens + (int64_t)(item.y + l0) * dim + zh0 + col;
 #pragma unroll 4
-          for (int j = 0; j < 16; ++j) {
-            if (j < nrow) dens_out[ch.dens + ((int64_t)xr * dim + yr) * dim + zh0 + col] = sp[2 * kStageRow * j];
-            xr += 2;
-            if (xr >= dim) {
-              xr -= dim;
-              ++yr;
-            }
-          }
-        } else {
-          float* gp = dens_out + ch.dens + (int64_t)(item.y + l0) * dim + zh0 + col;
-#pragma unroll 4
-          for (int j = 0; j < 16; ++j) {
-            if (j < nrow) *gp = sp[2 * kStageRow * j];
-            gp += 2 * dim;
-          }
+        for (int j = 0; j < 16; ++j) {
+          if (j < nrow) *gp = sp[2 * kStageRow * j];
+          gp += 2 * dim;
         }
         __syncthreads();  // the next half block's rows overwrite the stage
       }
@@ -503,7 +501,7 @@ __global__ void __launch_bounds__(kFillLines, 3) k_fill_terrain(const ChunkDev* 
 static void fill_terrain_smem_optin() {
   static std::atomic<int> done[64] = {};
   per_device_once(done, [](int) {
-    const int mx = (int)fill_smem_bytes(kCacheOctaves);
+    const int mx = (int)fill_smem_bytes(kCacheOctaves, false);
     cudaFuncSetAttribute(k_fill_terrain<4, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fill_terrain<8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     cudaFuncSetAttribute(k_fill_terrain<16, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -536,8 +534,9 @@ void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items,
   if (d_queue) cudaMemsetAsync(d_queue, 0, sizeof(int), st);
   const int g = d_queue ? grid : n_items;
   fill_terrain_smem_optin();
-  const size_t sm = fill_smem_bytes(min((int)field.p[5], kMaxOctaves));
-  if (exact && dens_out)
+  const bool band = exact && dens_out;
+  const size_t sm = fill_smem_bytes(min((int)field.p[5], kMaxOctaves), band);
+  if (band)
     fill_terrain_run<true>(run, g, sm, st, d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags, exact);
   else
     fill_terrain_run<false>(run, g, sm, st, d_chunks, d_items, n_items, d_queue, field, dens_out, words, flags,
@@ -640,18 +639,27 @@ void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const Fi
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
 int fill_terrain_lines() { return kFillLines; }
-int fill_terrain_resident_ctas(int run, int octaves) {
-  const size_t sm = fill_smem_bytes(min(octaves, kMaxOctaves));
+int fill_terrain_resident_ctas(int run, int octaves, bool band) {
+  const size_t sm = fill_smem_bytes(min(octaves, kMaxOctaves), band);
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   fill_terrain_smem_optin();
-  if (run == 4)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4, true>, kFillLines, sm);
-  else if (run == 16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16, true>, kFillLines, sm);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8, true>, kFillLines, sm);
+  if (band) {
+    if (run == 4)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4, true>, kFillLines, sm);
+    else if (run == 16)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16, true>, kFillLines, sm);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8, true>, kFillLines, sm);
+  } else {
+    if (run == 4)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<4, false>, kFillLines, sm);
+    else if (run == 16)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<16, false>, kFillLines, sm);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_terrain<8, false>, kFillLines, sm);
+  }
   return sms * (per_sm > 0 ? per_sm : 1);
 }
 
