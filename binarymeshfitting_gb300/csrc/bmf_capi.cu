@@ -93,6 +93,8 @@ struct bmf_batch {
   // them; d_exact is its per-sample exactness mask (words layout)
   int fill_band = 0;
   uint32_t* d_exact = nullptr;
+  uint2* d_fix = nullptr;  // samples to make exact (+ counter), sized 2 vcap + 1
+  int64_t fix_cap = 0;
   // Mode R work list, sized by the output capacity (vcap + icap / 3 + 1)
   uint2* d_clist = nullptr;
   int64_t clist_cap = 0;
@@ -636,6 +638,22 @@ bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   b->ws.clist = b->d_clist;
   b->ws.ccount = (uint32_t*)(b->d_clist + b->clist_cap);
   b->ws.clist_cap = b->clist_cap;
+  if (b->d_exact) {
+    // band fill: every crossing (one vertex each in Mode R) lists at most its two ends
+    const int64_t fcap = 2 * vcap + 1;
+    if (fcap > b->fix_cap) {
+      if (b->d_fix) cudaFree(b->d_fix);
+      b->d_fix = nullptr;
+      b->fix_cap = 0;
+      BMF_CUDA(b->ctx, cudaMalloc(&b->d_fix, sizeof(uint2) * (fcap + 1)));
+      b->fix_cap = fcap;
+    }
+    b->ws.fix = b->d_fix;
+    b->ws.fcount = (uint32_t*)(b->d_fix + b->fix_cap);
+    b->ws.fix_cap = b->fix_cap;
+  }
+  const bool band = b->fill_band && b->d_exact && b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0;
+  b->ws.exact = band ? b->d_exact : nullptr;
   return BMF_OK;
 }
 
@@ -705,7 +723,7 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   batch_fill(b, st);
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   const bool band = batch_band(b);
-  if (band) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_words, b->d_exact, b->d_dens, st);
+  if (band) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st);
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);
@@ -862,7 +880,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[2], st));
   // the band fill's exact-density fix-up belongs to the fill stage
-  if (batch_band(b)) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_words, b->d_exact, b->d_dens, st);
+  if (batch_band(b)) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[7], st));
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   BMF_CUDA(ctx, cudaEventRecord(ev[3], st));
@@ -1244,7 +1262,7 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
                   b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
                   b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey,
-                  b->d_fill_items, b->d_queue, b->d_order, b->d_pqueue, b->d_clist, b->d_exact};
+                  b->d_fill_items, b->d_queue, b->d_order, b->d_pqueue, b->d_clist, b->d_exact, b->d_fix};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);

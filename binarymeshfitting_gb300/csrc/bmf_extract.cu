@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
   for (int base = 0; base < nw; base += kCountThreads) {
     const int wi = base + threadIdx.x;
     uint32_t vc = 0u, ic = 0u, p0 = 0u, p1 = 0u, p2 = 0u, act = 0u;
+    uint32_t f00 = 0u, f10 = 0u, f01 = 0u, fnx = 0u;  // band fill: samples to make exact
     if (wi < nw && cm) {
       const int y = wi / zc, zb = wi - y * zc;
       const bool yin = y + 1 < dim, nin = zb + 1 < zc;
@@ -222,6 +223,16 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         vc = __popc(X) + __popc(Y) + __popc(Z);
         ic = 3u * t;
         act = p0 | p1 | p2 | X | Y | Z;
+        if (ws.exact && (X | Y | Z)) {
+          // the band fill's inexact samples at the ends of this word's crossings:
+          // own samples (X, Y, Z starts, Z ends), line x + 1 (X), line y + 1 (Y),
+          // and bit 0 of the next word (the end of a crossing from bit 31)
+          const uint32_t* E = ws.exact + ch.words + ((int64_t)x * dim + y) * zc + zb;
+          f00 = (X | Y | Z | (Z << 1)) & ~__ldg(E);
+          f10 = X ? (X & ~__ldg(E + (int64_t)dim * zc)) : 0u;
+          f01 = Y ? (Y & ~__ldg(E + zc)) : 0u;
+          fnx = (Z >> 31) ? (~__ldg(E + 1) & 1u) : 0u;
+        }
       } else {
         // interior quad edges: the four cells around the edge exist
         const bool yi = y >= 1 && y <= dim - 2, xi = x >= 1 && x <= dim - 2;
@@ -242,6 +253,35 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         ws.gpl[3 * o] = p0;
         ws.gpl[3 * o + 1] = p1;
         ws.gpl[3 * o + 2] = p2;
+      }
+    }
+    if (MODE == 0 && ws.exact) {
+      // one global reservation per warp for the samples to make exact
+      const int nf = __popc(f00) + __popc(f10) + __popc(f01) + __popc(fnx);
+      int incl = nf;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += v;
+      }
+      const int tot = __shfl_sync(kFull, incl, 31);
+      if (tot) {
+        uint32_t fbase = 0u;
+        if (lane == 31) fbase = atomicAdd(ws.fcount, (uint32_t)tot);
+        fbase = __shfl_sync(kFull, fbase, 31);
+        if (nf) {
+          int64_t slot = (int64_t)fbase + incl - nf;
+          const int y = wi / zc, zb = wi - y * zc;
+          const uint32_t s00 = (uint32_t)((((int64_t)x * dim + y) * dim) + 32 * zb);
+          auto put = [&](uint32_t m, uint32_t sbase) {
+            for (; m; m &= m - 1u, ++slot)
+              if (slot < ws.fix_cap) ws.fix[slot] = make_uint2((uint32_t)c, sbase + (uint32_t)(__ffs(m) - 1));
+          };
+          put(f00, s00);
+          put(f10, s00 + (uint32_t)dim * (uint32_t)dim);
+          put(f01, s00 + (uint32_t)dim);
+          put(fnx, s00 + 32u);
+        }
       }
     }
     if (listing) {
@@ -960,6 +1000,7 @@ void launch_sweep_chunks(const StructuredAdj& sa, int N, int64_t nv, int64_t n_p
 void launch_count(int mode, const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
                   const uint32_t* words, const uint32_t* flags, WordScratch ws, cudaStream_t st) {
   if (ws.clist) cudaMemsetAsync(ws.ccount, 0, sizeof(uint32_t), st);
+  if (ws.exact) cudaMemsetAsync(ws.fcount, 0, sizeof(uint32_t), st);
   if (mode == 0) k_count<0><<<n_units, kCountThreads, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
   else k_count<1><<<n_units, kCountThreads, 0, st>>>(d_chunks, n_chunks, d_unit_start, words, flags, ws);
 }

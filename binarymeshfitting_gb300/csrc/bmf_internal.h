@@ -65,6 +65,15 @@ struct WordScratch {
   uint2* clist;
   uint32_t* ccount;
   int64_t clist_cap;
+  // Band fill (Mode R, nullable): its exactness mask, and the list of samples
+  // the count kernel finds at an end of a crossing with an inexact density,
+  // as {chunk, sample index in the chunk}; *fcount (zeroed before the count
+  // kernel) entries, at most fix_cap kept.  A crossing has two ends, so the
+  // list holds at most twice the vertex count (2 vcap + 1 suffices).
+  const uint32_t* exact = nullptr;
+  uint2* fix = nullptr;
+  uint32_t* fcount = nullptr;
+  int64_t fix_cap = 0;
 };
 
 // Fill + label.  A terrain field of a single chunk goes through the line
@@ -84,10 +93,10 @@ void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items,
                          uint32_t* exact, cudaStream_t st);
 // the band fill applies to fields of the form (py - h) - a * FBM with a > 0
 bool fill_band_supported(const FieldDev& field);
-// exact densities at both ends of every crossing of the Mode R busy-word list
-// whose band-fill value is inexact (after launch_count, before launch_emit)
-void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, const uint32_t* words,
-                       const uint32_t* exact, float* dens, cudaStream_t st);
+// exact densities for the samples the count kernel listed in ws.fix (the
+// inexact ends of crossings; after launch_count, before launch_emit)
+void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, float* dens,
+                       cudaStream_t st);
 int fill_terrain_items(int dim);          // items of one chunk
 int fill_terrain_lines();                 // lines per item
 int fill_terrain_resident_ctas(int run, int octaves, bool band);  // persistent grid: SMs x resident CTAs per SM

@@ -549,12 +549,10 @@ bool fill_band_supported(const FieldDev& field) {
 
 // ---------------------------------------------------------------------------
 // Exact densities where the band fill left a decided sample inexact but the
-// mesh reads it: the two ends of every sign-changing grid edge.  One thread
-// per busy word of the Mode R work list (entry = chunk, x * dim * zc + word
-// of line): the word owns the crossings X (to x + 1), Y (to y + 1) and Z (to
-// z + 1) of its 32 samples (the same bits as k_count), so it checks both ends
-// of each.  A sample shared by several crossings may be recomputed by
-// several threads; they store the same value.
+// mesh reads it: the two ends of every sign-changing grid edge.  k_count
+// lists those samples ({chunk, sample index}); one thread per listed sample.
+// A sample at the end of several crossings may be listed more than once;
+// every copy stores the same value.
 // ---------------------------------------------------------------------------
 // The exact terrain density of one sample: per octave the line's x/y terms,
 // the z terms and both z-layers of its lattice cell, combined with the
@@ -582,15 +580,9 @@ __device__ float terrain_exact(const FieldDev& f, const int* __restrict__ perm2,
   return __fmaf_rn(-ampl, sum, py - h0);
 }
 
-__device__ __forceinline__ uint32_t band_zbits_upto(int hi, int zb) {  // bits l with 32 zb + l <= hi
-  const int n = hi - 32 * zb + 1;
-  return n >= 32 ? kFull : (n <= 0 ? 0u : ((1u << n) - 1u));
-}
-
 __global__ void __launch_bounds__(256) k_fill_fixup(const ChunkDev* __restrict__ chunks, const uint2* __restrict__ list,
                                                     const uint32_t* __restrict__ count, int64_t cap, FieldDev field,
-                                                    const uint32_t* __restrict__ words,
-                                                    const uint32_t* __restrict__ exact, float* __restrict__ dens) {
+                                                    float* __restrict__ dens) {
   __shared__ int perm2[512];
   __shared__ float4 gtab[512];
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
@@ -602,31 +594,14 @@ __global__ void __launch_bounds__(256) k_fill_fixup(const ChunkDev* __restrict__
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
     const uint2 ent = list[e];
     const ChunkDev ch = chunks[ent.x];
-    const int dim = ch.dim, zc = ch.zc, nw = dim * zc;
-    const int x = (int)(ent.y / (uint32_t)nw), wi = (int)ent.y - x * nw;
-    const int y = wi / zc, zb = wi - y * zc;
-    const int64_t o00 = ch.words + ((int64_t)x * dim + y) * zc + zb;
-    const bool xin = x + 1 < dim, yin = y + 1 < dim, nin = zb + 1 < zc;
-    const uint32_t w00 = words[o00], n00 = nin ? words[o00 + 1] : 0u;
-    const uint32_t X = xin ? (w00 ^ words[o00 + (int64_t)dim * zc]) : 0u;
-    const uint32_t Y = yin ? (w00 ^ words[o00 + zc]) : 0u;
-    const uint32_t Z = (w00 ^ ((w00 >> 1) | (n00 << 31))) & band_zbits_upto(dim - 2, zb);
-    // ends of the crossings that are inexact: this line, line x + 1, line y + 1, next word
-    auto fix = [&](uint32_t m, int xs, int ys, int z0) {
-      for (; m; m &= m - 1u) {
-        const int zs = z0 + __ffs(m) - 1;
-        dens[ch.dens + ((int64_t)xs * dim + ys) * dim + zs] = terrain_exact(field, perm2, gtab, ch, xs, ys, zs);
-      }
-    };
-    fix((X | Y | Z | (Z << 1)) & ~exact[o00], x, y, 32 * zb);
-    if (X) fix(X & ~exact[o00 + (int64_t)dim * zc], x + 1, y, 32 * zb);
-    if (Y) fix(Y & ~exact[o00 + zc], x, y + 1, 32 * zb);
-    if (Z >> 31) fix(~exact[o00 + 1] & 1u, x, y, 32 * zb + 32);
+    const uint32_t dim = (uint32_t)ch.dim, line = ent.y / dim;
+    const int z = (int)(ent.y - line * dim), x = (int)(line / dim), y = (int)(line - (uint32_t)x * dim);
+    dens[ch.dens + (int64_t)ent.y] = terrain_exact(field, perm2, gtab, ch, x, y, z);
   }
 }
 
-void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, const uint32_t* words,
-                       const uint32_t* exact, float* dens, cudaStream_t st) {
+void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, float* dens,
+                       cudaStream_t st) {
   static std::atomic<int> grid[64] = {};
   const int g = per_device_once(grid, [](int dev) {
     int sms = 0, per_sm = 0;
@@ -634,7 +609,7 @@ void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const Fi
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_fixup, 256, 0);
     return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   });
-  k_fill_fixup<<<g, 256, 0, st>>>(d_chunks, ws.clist, ws.ccount, ws.clist_cap, field, words, exact, dens);
+  k_fill_fixup<<<g, 256, 0, st>>>(d_chunks, ws.fix, ws.fcount, ws.fix_cap, field, dens);
 }
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }

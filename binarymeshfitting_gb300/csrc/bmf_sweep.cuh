@@ -150,7 +150,31 @@ __device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t
   if (n == 0 || (!process_boundary && boundary[v])) return;
   const uint32_t* a = adj + ov;
   float p[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
-  for (uint32_t k = 0; k < n; ++k) {
+  uint32_t k0 = 0;
+  if (PACKED) {
+    // two primitives per step: both gathers are issued before the sums,
+    // which keep the one-by-one order (the same rounding)
+    for (; k0 + 2 <= n; k0 += 2) {
+      const uint32_t t0 = sweep_ld<COH>(a + k0), t1 = sweep_ld<COH>(a + k0 + 1);
+      const bool ok0 = (int64_t)t0 < np_lim, ok1 = (int64_t)t1 < np_lim;
+      const float4 q0 = ok0 ? sweep_ld<COH>(reinterpret_cast<const float4*>(dual_p) + t0) : make_float4(0, 0, 0, 0);
+      const float4 q1 = ok1 ? sweep_ld<COH>(reinterpret_cast<const float4*>(dual_p) + t1) : make_float4(0, 0, 0, 0);
+      float2 r0 = make_float2(0.0f, 0.0f), r1 = make_float2(0.0f, 0.0f);
+      if (smooth_normals) {
+        if (ok0) r0 = sweep_ld<COH>(reinterpret_cast<const float2*>(dual_n) + t0);
+        if (ok1) r1 = sweep_ld<COH>(reinterpret_cast<const float2*>(dual_n) + t1);
+      }
+      if (ok0) {
+        p[0] = p[0] + q0.x; p[1] = p[1] + q0.y; p[2] = p[2] + q0.z;
+        if (smooth_normals) { nn[0] = nn[0] + q0.w; nn[1] = nn[1] + r0.x; nn[2] = nn[2] + r0.y; }
+      }
+      if (ok1) {
+        p[0] = p[0] + q1.x; p[1] = p[1] + q1.y; p[2] = p[2] + q1.z;
+        if (smooth_normals) { nn[0] = nn[0] + q1.w; nn[1] = nn[1] + r1.x; nn[2] = nn[2] + r1.y; }
+      }
+    }
+  }
+  for (uint32_t k = k0; k < n; ++k) {
     const uint32_t t = sweep_ld<COH>(a + k);
     if ((int64_t)t >= np_lim) continue;  // never read past the dual points
     if (PACKED) {
