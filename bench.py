@@ -37,11 +37,16 @@ OPS_PER_SAMPLE = 1          # fma(-a, sum, py - h)
 OPS_PER_LINE_OCTAVE = 20    # xs, ys, 2 floor, xf, yf, 2 fade (5 each), x1, y1, fr, amp
 OPS_PER_LINE = 1            # py - h
 OPS_PER_LAYER = 20          # 4 corners (mul + fma), alpha and beta (3 lerps of 2 each)
-# DRAM bytes (read + write) per sample of k_fill_terrain from one ncu capture on
-# the 256-chunk update (110,890,368 samples, 80.04 MB read + 484.17 MB written):
-# traffic grows with the samples, so a full launch is scaled from it
-# (profiles/k_fill_terrain_lod_update_256.txt)
-FILL_DRAM_BYTES_PER_SAMPLE = (80.04e6 + 484.17e6) / 110_890_368
+# DRAM bytes (read + write) of one launch of each kernel on the 4096-chunk update
+# (seed 2024, Mode R, 4 sweeps + normals), from one ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum (one pass; profiles/
+# dram_bytes_lod_update_4096.txt).  Other workloads scale them: the fill and
+# count by samples, the emit, scan and sweeps by output indices.
+DRAM_UPDATE_SAMPLES = 1_785_478_272
+DRAM_UPDATE_INDICES = 167_847_141
+DRAM_BYTES = {"fill": 415.3e6 + 1405.9e6 + 9.0e6 + 3.8e6,     # k_fill_terrain<16, band> + k_fill_fixup
+              "count": 331.1e6 + 1458.8e6, "scan": 590.5e6 + 531.0e6, "emit": 1774.8e6 + 2410.4e6,
+              "sweeps": 12763.1e6 + 8367.6e6}
 
 
 def fill_fp32_ops(rows, params):
@@ -443,13 +448,15 @@ def run_gb300(args):
     clock_mhz = clk["sm_mhz"] or sm_max
     fp32_peak = 152 * 128 * sm_max * 1e6 / 1e12  # nominal FP32 instruction rate at max clock, Tops/s
     fill_ops = fill_fp32_ops(rows, workloads.TERRAIN_PARAMS)
-    fill_achieved = fill_ops / (st_ms[0] / 1000.0) / 1e12
+    s_scale, i_scale = samples / DRAM_UPDATE_SAMPLES, ni / DRAM_UPDATE_INDICES
+    dram = {k: v * (s_scale if k in ("fill", "count") else i_scale) for k, v in DRAM_BYTES.items()}
     # algorithmic HBM bytes of the extraction kernels (count + scan + offsets + emit)
     per_vertex = 12 + 1 + 1 + 8 + (12 if normals else 0)
     ext_bytes = words * (4 + 8 + 8 + 4) + nv * per_vertex + ni * 4
     ext_ms = st_ms[1] + st_ms[2] + st_ms[3] + st_ms[4]
     ext_gbs = ext_bytes / (ext_ms / 1000.0) / 1e9
-    # algorithmic HBM bytes of the mesh processing (CSR scan + adjacency + iters x (dual, primal)),
+    ext_dram = dram["count"] + dram["scan"] + dram["emit"]
+    # logical bytes of the mesh processing (CSR scan + adjacency + iters x (dual, primal)),
     # each array counted once per pass: dual reads indices + positions (+ normals) and writes
     # dual points + normals; primal reads offsets, adjacency, dual points + normals, flags and
     # writes positions + normals
@@ -459,21 +466,37 @@ def run_gb300(args):
     primal_b = 4 * nv + 4 * ni + (12 + nb) * n_prims + 2 * nv + (12 + nb) * nv
     proc_bytes = args.iters * (dual_b + primal_b) + (1 + 4) * nv + (4 + 4) * nv + 4 * ni
     proc_gbs = proc_bytes / (st_ms[5] / 1000.0) / 1e9 if st_ms[5] > 0 else 0.0
-    roofline = {"kernel": "k_fill_terrain (density FBM + occupancy words)", "bound": "fp32",
-                "achieved": fill_achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fill_achieved / fp32_peak,
-                "peak_kind": "nominal 152 SM x 128 FP32 lanes x %.0f MHz (no measured FP32 peak exists)" % sm_max,
-                "traffic": FILL_DRAM_BYTES_PER_SAMPLE * samples, "traffic_unit": "bytes per launch (scaled ncu)",
-                "algorithmic_bytes": 4 * samples + 4 * words, "ms_per_launch": st_ms[0],
-                "flops_per_launch": fill_ops, "flops_per_sample": fill_ops / samples,
+    sweep_name = ("k_sweep_chunks (CSR scan, adjacency, %d x (dual, primal), chunk by chunk)" if args.chunks >= 2048
+                  else "scan + adj_build + %d x (dual, primal)") % args.iters
+    # the dominant kernel: the mesh-processing sweeps (HBM-bound gathers)
+    roofline = {"kernel": sweep_name, "bound": "hbm", "achieved": proc_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": proc_gbs / hbm_peak, "peak_kind": peak_kind,
+                "achieved_bytes": "logical: every array of every pass counted once (%.2f GB per launch)"
+                                  % (proc_bytes / 1e9),
+                "traffic": dram["sweeps"], "traffic_unit": "DRAM bytes per launch (ncu, scaled to this update)",
+                "dram_achieved": dram["sweeps"] / (st_ms[5] / 1000.0) / 1e9,
+                "dram_frac": dram["sweeps"] / (st_ms[5] / 1000.0) / 1e9 / hbm_peak,
+                "ms_per_launch": st_ms[5],
+                "fill": {"kernels": "k_fill_terrain<16, band> + k_fill_fixup (terrain FBM, occupancy words, exact "
+                                    "densities at the ends of crossings)" if args.mode == "R" else
+                                    "k_fill_terrain<16> (every density exact)",
+                         "ms": st_ms[0], "samples_per_s": samples / (st_ms[0] / 1000.0),
+                         "dram_bytes": dram["fill"] if args.mode == "R" else None,
+                         "full_fill_fp32_ops": fill_ops, "full_fill_fp32_ops_per_sample": fill_ops / samples,
+                         "full_fill_equivalent_tops": fill_ops / (st_ms[0] / 1000.0) / 1e12,
+                         "full_fill_equivalent_frac": fill_ops / (st_ms[0] / 1000.0) / 1e12 / fp32_peak,
+                         "fp32_peak": fp32_peak,
+                         "peak_kind": "nominal 152 SM x 128 FP32 lanes x %.0f MHz (no measured FP32 peak exists)"
+                                      % sm_max,
+                         "note": "the band fill stops a run's octaves once their bound fixes every sign, so its "
+                                 "own FP32 work is data-dependent; full_fill_* is the work of evaluating every "
+                                 "octave of every sample, divided by the band fill's time"},
                 "extraction_hbm": {"kernels": "count+scan+offsets+emit", "achieved": ext_gbs, "peak": hbm_peak,
                                    "unit": "GB/s", "frac": ext_gbs / hbm_peak, "bytes": ext_bytes,
-                                   "ms": ext_ms, "peak_kind": peak_kind},
-                "processing_hbm": {"kernels": ("k_sweep_chunks (CSR scan, adjacency, %d x (dual, primal), chunk by chunk)"
-                                               if args.chunks >= 2048 else "scan+adj_build+%d x (dual, primal)")
-                                              % args.iters,
-                                   "achieved": proc_gbs, "peak": hbm_peak, "unit": "GB/s",
-                                   "frac": proc_gbs / hbm_peak, "bytes": proc_bytes, "ms": st_ms[5],
-                                   "peak_kind": peak_kind},
+                                   "dram_bytes": ext_dram, "dram_frac": ext_dram / (ext_ms / 1000.0) / 1e9 / hbm_peak,
+                                   "ms": ext_ms, "peak_kind": peak_kind,
+                                   "note": "issue-bound bit arithmetic: too few bytes per unit of work for HBM to "
+                                           "bind"},
                 "stage_ms": {"fill_label": st_ms[0], "count": st_ms[1], "scan": st_ms[2], "offsets": st_ms[3],
                              "emit": st_ms[4], "process": st_ms[5]}}
 
