@@ -81,6 +81,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--mode", default="R", choices=["R", "Q"])
+    p.add_argument("--field", default="fbm", choices=["fbm", "2d"],
+                   help="fbm: the configs' 3D terrain FBM; 2d: the reference's default perturbed heightmap sampler")
     p.add_argument("--placement", type=int, default=1)
     p.add_argument("--iters", type=int, default=4)
     p.add_argument("--no-normals", action="store_true")
@@ -171,12 +173,34 @@ def cpu_sample_rows(rows, n, seed):
     return np.sort(np.concatenate(pick))
 
 
+def update_rows(args, seed=2024):
+    """The update's chunk descriptors and rows (origin xyz, scale, dim, level);
+    for the 2D heightmap the origins move down by 128 into its band."""
+    from binarymeshfitting_gb300 import workloads
+    descs, rows = workloads.lod_update(n=args.chunks, seed=seed)
+    if args.field == "2d":
+        for d, r in zip(descs, rows):
+            d.origin[1] = float(r[1]) - 128.0
+            r[1] = d.origin[1]
+    return descs, rows
+
+
+def field_spec(args):
+    """(kind, params) of the update's density field."""
+    from binarymeshfitting_gb300 import _lib as L
+    from binarymeshfitting_gb300 import workloads
+    if args.field == "2d":
+        return L.FIELD_TERRAIN_2D, list(workloads.TERRAIN_2D_PARAMS)
+    return L.FIELD_TERRAIN_FBM, list(workloads.TERRAIN_PARAMS)
+
+
 def cpu_run(rows, args, threads):
     from binarymeshfitting_gb300 import workloads
     from oracle import cpu
     mode = 0 if args.mode == "R" else 1
     t0 = time.perf_counter()
-    tot, counts = cpu.extract_batch(rows[:, :5].astype(np.float32), 2, list(workloads.TERRAIN_PARAMS), mode,
+    kind, params = field_spec(args)
+    tot, counts = cpu.extract_batch(rows[:, :5].astype(np.float32), kind, params, mode,
                                     args.placement, args.iters, not args.no_normals, n_threads=threads)
     return time.perf_counter() - t0, tot
 
@@ -190,7 +214,7 @@ def run_reference(args):
     from oracle import cpu
     cpu.build()
     threads = os.cpu_count() or 1
-    _, rows = workloads.lod_update(n=args.chunks)
+    _, rows = update_rows(args)
     for w in range(args.warmup):
         cpu_run(rows[cpu_sample_rows(rows, args.cpu_sample, 100 + w)], args, threads)
     times, chunks = [], 0
@@ -215,7 +239,11 @@ def run_reference(args):
 def config(args):
     return {"workload": "lod_update_%d" % args.chunks,
             "chunks": args.chunks, "chunk_samples": "2048x33^3 + 1434x65^3 + 614x129^3",
-            "field": "terrain y-64-40*FBM(p), 5 octaves perlin, freq 0.01, lacunarity 2, gain 0.5, seed 1337",
+            "field": ("terrain y-64-40*FBM(p), 5 octaves perlin, freq 0.01, lacunarity 2, gain 0.5, seed 1337"
+                      if args.field == "fbm" else
+                      "perturbed 2D heightmap -(0.25 y) - 75 n(x, z) (the reference's default world sampler shape): "
+                      "13 gradient-noise perturb octaves amp 0.87 freq 0.585 gain 0.488, 3 value-noise octaves, "
+                      "seed 1337; chunk origins lowered by 128 to its band"),
             "topology": "mode R (reference Marching-Cubes triangles)" if args.mode == "R" else
             "mode Q (DMC quads, placement %d)" % args.placement,
             "smoothing_iters": args.iters, "smoothed_normals": not args.no_normals,
@@ -268,7 +296,8 @@ def check_parity(sub, gpu_chunks, args):
     from binarymeshfitting_gb300 import workloads
     from oracle import cpu
     mode = 0 if args.mode == "R" else 1
-    counts, want = cpu.extract_batch_digest(sub[:, :5].astype(np.float32), 2, list(workloads.TERRAIN_PARAMS), mode,
+    kind, params = field_spec(args)
+    counts, want = cpu.extract_batch_digest(sub[:, :5].astype(np.float32), kind, params, mode,
                                             args.placement, args.iters, False, not args.no_normals)
     bad, with_mesh, verts = [], 0, 0
     for k, (info, pos, idx, bnd, nrm) in enumerate(gpu_chunks):
@@ -386,8 +415,8 @@ def run_gb300(args):
     ctx = Context(local)
     mode = L.MODE_R if args.mode == "R" else L.MODE_Q
     normals = not args.no_normals
-    descs, rows = workloads.lod_update(n=args.chunks, seed=2024 + rank)
-    field = workloads.terrain_field()
+    descs, rows = update_rows(args, seed=2024 + rank)
+    field = workloads.terrain_field() if args.field == "fbm" else workloads.terrain2d_field()
     b = Batch(ctx, descs, field, mode=mode, placement=args.placement, iters=args.iters, smooth_normals=normals)
     # size the output arena from one sizing pass (counts are exact), then keep it
     vcap, icap = 40_000_000, 240_000_000
@@ -447,7 +476,7 @@ def run_gb300(args):
     hbm_peak, sm_max, peak_kind = measured_peaks()
     clock_mhz = clk["sm_mhz"] or sm_max
     fp32_peak = 152 * 128 * sm_max * 1e6 / 1e12  # nominal FP32 instruction rate at max clock, Tops/s
-    fill_ops = fill_fp32_ops(rows, workloads.TERRAIN_PARAMS)
+    fill_ops = fill_fp32_ops(rows, workloads.TERRAIN_PARAMS) if args.field == "fbm" else 0
     s_scale, i_scale = samples / DRAM_UPDATE_SAMPLES, ni / DRAM_UPDATE_INDICES
     dram = {k: v * (s_scale if k in ("fill", "count") else i_scale) for k, v in DRAM_BYTES.items()}
     # algorithmic HBM bytes of the extraction kernels (count + scan + offsets + emit)
@@ -477,11 +506,15 @@ def run_gb300(args):
                 "dram_achieved": dram["sweeps"] / (st_ms[5] / 1000.0) / 1e9,
                 "dram_frac": dram["sweeps"] / (st_ms[5] / 1000.0) / 1e9 / hbm_peak,
                 "ms_per_launch": st_ms[5],
-                "fill": {"kernels": "k_fill_terrain<16, band> + k_fill_fixup (terrain FBM, occupancy words, exact "
-                                    "densities at the ends of crossings)" if args.mode == "R" else
-                                    "k_fill_terrain<16> (every density exact)",
+                "fill": {"kernels": ("k_sample_label (x-plane CTAs; one height evaluation per (x, z) column)"
+                                     if args.field == "2d" else
+                                     "k_fill_terrain<16, band> + k_fill_fixup (terrain FBM, occupancy words, exact "
+                                     "densities at the ends of crossings)" if args.mode == "R" else
+                                     "k_fill_terrain<16> (every density exact)"),
                          "ms": st_ms[0], "samples_per_s": samples / (st_ms[0] / 1000.0),
-                         "dram_bytes": dram["fill"] if args.mode == "R" else None,
+                         "dram_bytes": dram["fill"] if (args.mode == "R" and args.field == "fbm") else None,
+                         "density_write_gbs": (4 * samples + 4 * words) / (st_ms[0] / 1000.0) / 1e9
+                         if args.field == "2d" else None,
                          "full_fill_fp32_ops": fill_ops, "full_fill_fp32_ops_per_sample": fill_ops / samples,
                          "full_fill_equivalent_tops": fill_ops / (st_ms[0] / 1000.0) / 1e12,
                          "full_fill_equivalent_frac": fill_ops / (st_ms[0] / 1000.0) / 1e12 / fp32_peak,

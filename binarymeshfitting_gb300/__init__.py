@@ -5,10 +5,11 @@ the Python host layer over it: ``engine`` (tensors in, tensors out) and
 ``reference_api`` (the reference's Sampler / DMCChunk / MeshProcessor /
 ChunkGenerator call surface).
 """
-from ._lib import (BmfError, ChunkDesc, Field, FIELD_GRID, FIELD_SPHERE_WAVE, FIELD_TERRAIN_FBM, FIELD_TORUS_Z,
+from ._lib import (BmfError, ChunkDesc, Field, FIELD_GRID, FIELD_SPHERE_WAVE, FIELD_TERRAIN_FBM, FIELD_TERRAIN_2D,
+                   FIELD_TORUS_Z,
                    FIELD_SPHERE, FIELD_CUBOID, FIELD_PLANE_Y, MODE_R, MODE_Q, PLACE_CENTER, PLACE_MASSPOINT,
                    PLACE_QEF)
 
-__all__ = ["BmfError", "ChunkDesc", "Field", "FIELD_GRID", "FIELD_SPHERE_WAVE", "FIELD_TERRAIN_FBM",
+__all__ = ["BmfError", "ChunkDesc", "Field", "FIELD_GRID", "FIELD_SPHERE_WAVE", "FIELD_TERRAIN_FBM", "FIELD_TERRAIN_2D",
            "FIELD_TORUS_Z", "FIELD_SPHERE", "FIELD_CUBOID", "FIELD_PLANE_Y", "MODE_R", "MODE_Q", "PLACE_CENTER",
            "PLACE_MASSPOINT", "PLACE_QEF"]

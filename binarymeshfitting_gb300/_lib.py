@@ -13,6 +13,7 @@ c_int32, c_int64, c_float, c_void_p = ctypes.c_int32, ctypes.c_int64, ctypes.c_f
 # bmf_fields.h
 FIELD_GRID, FIELD_SPHERE_WAVE, FIELD_TERRAIN_FBM = 0, 1, 2
 FIELD_TORUS_Z, FIELD_SPHERE, FIELD_CUBOID, FIELD_PLANE_Y = 3, 4, 5, 6
+FIELD_TERRAIN_2D = 7
 MODE_R, MODE_Q = 0, 1
 PLACE_CENTER, PLACE_MASSPOINT, PLACE_QEF = 0, 1, 2
 FIT_ADJOINT_F64 = 1

@@ -155,7 +155,7 @@ FieldDev make_field(const bmf_field* f) {
   d.kind = f->kind;
   for (int i = 0; i < BMF_FIELD_MAX_PARAMS; ++i) d.p[i] = f->params[i];
   for (int i = 0; i < 256; ++i) d.perm[i] = (uint8_t)i;
-  if (f->kind == BMF_FIELD_TERRAIN_FBM) {
+  if (f->kind == BMF_FIELD_TERRAIN_FBM || f->kind == BMF_FIELD_TERRAIN_2D) {
     uint64_t st = (uint64_t)(int64_t)f->params[6];
     for (int i = 255; i > 0; --i) {
       const int j = (int)(splitmix64(&st) % (uint64_t)(i + 1));
@@ -168,9 +168,11 @@ FieldDev make_field(const bmf_field* f) {
 }
 
 bool field_ok(const bmf_field* f) {
-  if (!f || f->kind < BMF_FIELD_GRID || f->kind > BMF_FIELD_PLANE_Y) return false;
+  if (!f || f->kind < BMF_FIELD_GRID || f->kind > BMF_FIELD_TERRAIN_2D) return false;
   for (int i = 0; i < BMF_FIELD_MAX_PARAMS; ++i)
     if (!std::isfinite(f->params[i])) return false;
+  if (f->kind == BMF_FIELD_TERRAIN_2D)
+    return f->params[2] >= 0 && f->params[2] <= 32 && f->params[7] >= 0 && f->params[7] <= 32;
   return f->kind != BMF_FIELD_TERRAIN_FBM || (f->params[5] >= 0 && f->params[5] <= 32);
 }
 

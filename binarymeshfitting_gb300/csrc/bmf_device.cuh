@@ -240,6 +240,69 @@ __device__ __forceinline__ float len3(float x, float y, float z) {
 }
 
 // Evaluates a density field at world position (px, py, pz).
+// ---------------------------------------------------------------------------
+// BMF_FIELD_TERRAIN_2D (bmf_fields.h): 2D gradient noise (8 directions) and 2D
+// value noise on the permutation, quintic fade, every lerp fma(t, b - a, a).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float grad2_dot(int h, float x, float z) {
+  h &= 7;
+  const float gx = (h < 4) ? ((h & 1) ? -1.0f : 1.0f) : ((h & 2) ? 0.0f : ((h & 1) ? -1.0f : 1.0f));
+  const float gz = (h < 4) ? ((h & 2) ? -1.0f : 1.0f) : ((h & 2) ? ((h & 1) ? -1.0f : 1.0f) : 0.0f);
+  return __fmaf_rn(gz, z, gx * x);
+}
+// component c (0 or 1) hashes its lattice column with an offset of 73 c
+__device__ __forceinline__ float noise2_grad(const int* __restrict__ perm2, int c, float x, float z) {
+  const float fx = floorf(x), fz = floorf(z);
+  const int X = ((int)fx) & 255, Z = ((int)fz) & 255;
+  const float xf = x - fx, zf = z - fz, x1 = xf - 1.0f, z1 = zf - 1.0f;
+  const float u = fade(xf), w = fade(zf);
+  const int A = perm2[X + 73 * c] + Z, B = perm2[X + 1 + 73 * c] + Z;
+  const float g00 = grad2_dot(perm2[A], xf, zf), g10 = grad2_dot(perm2[B], x1, zf);
+  const float g01 = grad2_dot(perm2[A + 1], xf, z1), g11 = grad2_dot(perm2[B + 1], x1, z1);
+  return lerp_t(w, lerp_t(u, g00, g10), lerp_t(u, g01, g11));
+}
+__device__ __forceinline__ float noise2_value(const int* __restrict__ perm2, float x, float z) {
+  const float fx = floorf(x), fz = floorf(z);
+  const int X = ((int)fx) & 255, Z = ((int)fz) & 255;
+  const float xf = x - fx, zf = z - fz;
+  const float u = fade(xf), w = fade(zf);
+  const int A = perm2[X] + Z, B = perm2[X + 1] + Z;
+  const float k = 2.0f / 255.0f;
+  const float v00 = (float)perm2[A] * k - 1.0f, v10 = (float)perm2[B] * k - 1.0f;
+  const float v01 = (float)perm2[A + 1] * k - 1.0f, v11 = (float)perm2[B + 1] * k - 1.0f;
+  return lerp_t(w, lerp_t(u, v00, v10), lerp_t(u, v01, v11));
+}
+// the height noise n(x, z) in [-1, 1] of one (x, z) column
+__device__ __forceinline__ float terrain2d_height(const FieldDev& f, const int* __restrict__ perm2, float px,
+                                                  float pz) {
+  const float g = f.p[0];
+  float xn = (px * g) * 0.01f, zn = (pz * g) * 0.01f;
+  const int poct = (int)f.p[2];
+  float a = f.p[3], fr = f.p[4];
+  for (int k = 0; k < poct; ++k) {
+    const float sx = xn * fr, sz = zn * fr;
+    const float dx = noise2_grad(perm2, 0, sx, sz), dz = noise2_grad(perm2, 1, sx, sz);
+    xn = __fmaf_rn(a, dx, xn);
+    zn = __fmaf_rn(a, dz, zn);
+    fr = fr * 2.0f;
+    a = a * f.p[5];
+  }
+  const int voct = (int)f.p[7];
+  float sum = 0.0f, bound = 0.0f, amp = 1.0f, vf = 1.0f;
+  for (int o = 0; o < voct; ++o) {
+    sum = __fmaf_rn(amp, noise2_value(perm2, xn * vf, zn * vf), sum);
+    bound = bound + amp;
+    vf = vf * 2.0f;
+    amp = amp * 0.5f;
+  }
+  return voct > 0 ? sum / bound : 0.0f;
+}
+// density of one sample given its column's height noise n
+__device__ __forceinline__ float terrain2d_density(const FieldDev& f, float py, float n) {
+  const float dy = py * f.p[0];
+  return -dy - n * f.p[1];
+}
+
 __device__ __forceinline__ float eval_field(const FieldDev& f, const int* __restrict__ perm,
                                             const float4* __restrict__ gtab, float px, float py,
                                             float pz) {
@@ -261,6 +324,8 @@ __device__ __forceinline__ float eval_field(const FieldDev& f, const int* __rest
       }
       return __fmaf_rn(-f.p[1], sum, py - f.p[0]);
     }
+    case BMF_FIELD_TERRAIN_2D:
+      return terrain2d_density(f, py, terrain2d_height(f, perm, px, pz));
     case BMF_FIELD_TORUS_Z: {  // ImplicitSampler.cpp:27-34
       const float r1 = f.p[0] / 4.0f, r2 = f.p[0] / 10.0f;
       const float q_x = fabsf(sqrtf(px * px + py * py)) - r1;

@@ -22,6 +22,8 @@ __device__ __forceinline__ int find_chunk(const int* __restrict__ unit_start, in
   return lo;
 }
 
+constexpr int kMaxColumn = 1024;  // samples per axis (kMaxDim)
+
 // flags bits: 1 = a word that is neither empty nor full, 2 = a full word,
 // 4 = an empty word.  contains_mesh = (f & 1) || ((f & 6) == 6), the
 // reference's mesh / negative / positive logic (DMCChunk.cpp:141-162).
@@ -32,13 +34,14 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
   extern __shared__ uint32_t sw[];
   __shared__ int perm2[512];
   __shared__ float4 gtab[512];
+  __shared__ float s_col[kMaxColumn];  // BMF_FIELD_TERRAIN_2D: the height noise of the plane's (x, z) columns
   const int u = blockIdx.x;
   const int c = find_chunk(unit_start, n_chunks, u);
   const ChunkDev ch = chunks[c];
   const int x = u - __ldg(unit_start + c);
   const int dim = ch.dim, zc = ch.zc;
   const int nw = dim * zc;
-  if (field.kind == BMF_FIELD_TERRAIN_FBM) {  // the noise tables; no other field reads them
+  if (field.kind == BMF_FIELD_TERRAIN_FBM || field.kind == BMF_FIELD_TERRAIN_2D) {  // the noise tables
     for (int i = threadIdx.x; i < 512; i += blockDim.x) {
       perm2[i] = field.perm[i & 255];
       gtab[i] = grad_coeffs(field.perm[i & 255]);
@@ -46,6 +49,13 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
   }
   for (int i = threadIdx.x; i < nw; i += blockDim.x) sw[i] = 0u;
   __syncthreads();
+  const bool col2d = field.kind == BMF_FIELD_TERRAIN_2D && dim <= kMaxColumn;
+  if (col2d) {  // one height evaluation per column, shared by the plane's dim samples of it
+    const float pxc = ch.ox + (float)x * ch.scale;
+    for (int z = threadIdx.x; z < dim; z += blockDim.x)
+      s_col[z] = terrain2d_height(field, perm2, pxc, ch.oz + (float)z * ch.scale);
+    __syncthreads();
+  }
 
   // Work item = a run of kRun consecutive z-samples of one (x, y) line; runs
   // start at multiples of kRun (which divides 32), so a run's inside bits land
@@ -71,6 +81,10 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
       for (int k = 0; k < kRun; ++k) pz[k] = ch.oz + (float)(z0 + k) * ch.scale;
       if (field.kind == BMF_FIELD_TERRAIN_FBM) {
         terrain_run(field, perm2, gtab, px, py, pz, n, v);
+      } else if (col2d) {
+#pragma unroll
+        for (int k = 0; k < kRun; ++k)
+          if (k < n) v[k] = terrain2d_density(field, py, s_col[z0 + k]);
       } else {
 #pragma unroll
         for (int k = 0; k < kRun; ++k)

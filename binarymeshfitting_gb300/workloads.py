@@ -11,11 +11,15 @@
 """
 import numpy as np
 
-from ._lib import ChunkDesc, Field, FIELD_SPHERE_WAVE, FIELD_TERRAIN_FBM
+from ._lib import ChunkDesc, Field, FIELD_SPHERE_WAVE, FIELD_TERRAIN_2D, FIELD_TERRAIN_FBM
 
 WORLD = 4096.0
 TERRAIN_PARAMS = (64.0, 40.0, 0.01, 2.0, 0.5, 5, 1337)
 SPHERE_WAVE_PARAMS = (32.0, 32.0, 32.0, 20.0, 1.5, 0.3)
+# the reference's default world sampler settings (WorldOctree.cpp:49-55): g_scale
+# 0.25, height 75, 13 perturb octaves, amp 0.87, freq 0.585, gain 0.488; seed;
+# 3 value-noise octaves (FastNoiseSIMD's default fractal)
+TERRAIN_2D_PARAMS = (0.25, 75.0, 13, 0.87, 0.585, 0.488, 1337, 3)
 
 
 def sphere_wave_field():
@@ -24,6 +28,11 @@ def sphere_wave_field():
 
 def terrain_field():
     return Field.make(FIELD_TERRAIN_FBM, TERRAIN_PARAMS)
+
+
+def terrain2d_field(params=TERRAIN_2D_PARAMS):
+    """The perturbed 2D heightmap: -(y g) - height n(x, z) (bmf_fields.h)."""
+    return Field.make(FIELD_TERRAIN_2D, params)
 
 
 def lod_update(n=4096, seed=2024, tiers=((32, 0.50), (64, 0.35), (128, 0.15))):

@@ -215,6 +215,66 @@ float bmfo_fbm(const uint8_t perm[256], float x, float y, float z, int octaves, 
 /* density fields                                                            */
 /* ======================================================================== */
 
+/* BMF_FIELD_TERRAIN_2D (include/bmf_fields.h): the project's restatement of
+ * the reference's 2D perturbed heightmap sampler (NoiseSampler.cpp:148-194).
+ * 2D gradient noise with 8 directions (component c hashes its lattice column
+ * with an offset of 73 c) and 2D value noise, quintic fade, fmaf at the same
+ * places as the kernels (grad2_dot, every lerp, the perturbation and the FBM
+ * sum). */
+static float grad2_dot(int h, float x, float z) {
+  h &= 7;
+  const float gx = (h < 4) ? ((h & 1) ? -1.0f : 1.0f) : ((h & 2) ? 0.0f : ((h & 1) ? -1.0f : 1.0f));
+  const float gz = (h < 4) ? ((h & 2) ? -1.0f : 1.0f) : ((h & 2) ? ((h & 1) ? -1.0f : 1.0f) : 0.0f);
+  return fmaf(gz, z, gx * x);
+}
+static int perm2_at(const uint8_t perm[256], int i) { return perm[i & 255]; }
+static float noise2_grad(const uint8_t perm[256], int c, float x, float z) {
+  const float fx = floorf(x), fz = floorf(z);
+  const int X = ((int)fx) & 255, Z = ((int)fz) & 255;
+  const float xf = x - fx, zf = z - fz, x1 = xf - 1.0f, z1 = zf - 1.0f;
+  const float u = fade_fma(xf), w = fade_fma(zf);
+  const int A = perm2_at(perm, X + 73 * c) + Z, B = perm2_at(perm, X + 1 + 73 * c) + Z;
+  const float g00 = grad2_dot(perm2_at(perm, A), xf, zf), g10 = grad2_dot(perm2_at(perm, B), x1, zf);
+  const float g01 = grad2_dot(perm2_at(perm, A + 1), xf, z1), g11 = grad2_dot(perm2_at(perm, B + 1), x1, z1);
+  return lerp_fma(w, lerp_fma(u, g00, g10), lerp_fma(u, g01, g11));
+}
+static float noise2_value(const uint8_t perm[256], float x, float z) {
+  const float fx = floorf(x), fz = floorf(z);
+  const int X = ((int)fx) & 255, Z = ((int)fz) & 255;
+  const float xf = x - fx, zf = z - fz;
+  const float u = fade_fma(xf), w = fade_fma(zf);
+  const int A = perm2_at(perm, X) + Z, B = perm2_at(perm, X + 1) + Z;
+  const float k = 2.0f / 255.0f;
+  const float v00 = (float)perm2_at(perm, A) * k - 1.0f, v10 = (float)perm2_at(perm, B) * k - 1.0f;
+  const float v01 = (float)perm2_at(perm, A + 1) * k - 1.0f, v11 = (float)perm2_at(perm, B + 1) * k - 1.0f;
+  return lerp_fma(w, lerp_fma(u, v00, v10), lerp_fma(u, v01, v11));
+}
+float bmfo_terrain2d_height(const uint8_t perm[256], const float* p, float px, float pz) {
+  const float g = p[0];
+  float xn = (px * g) * 0.01f, zn = (pz * g) * 0.01f;
+  const int poct = (int)p[2];
+  float a = p[3], fr = p[4];
+  for (int k = 0; k < poct; ++k) {
+    const float sx = xn * fr, sz = zn * fr;
+    const float dx = noise2_grad(perm, 0, sx, sz), dz = noise2_grad(perm, 1, sx, sz);
+    xn = fmaf(a, dx, xn);
+    zn = fmaf(a, dz, zn);
+    fr = fr * 2.0f;
+    a = a * p[5];
+  }
+  const int voct = (int)p[7];
+  float sum = 0.0f, bound = 0.0f, amp = 1.0f, vf = 1.0f;
+  for (int o = 0; o < voct; ++o) {
+    sum = fmaf(amp, noise2_value(perm, xn * vf, zn * vf), sum);
+    bound = bound + amp;
+    vf = vf * 2.0f;
+    amp = amp * 0.5f;
+  }
+  return voct > 0 ? sum / bound : 0.0f;
+}
+float bmfo_noise2_grad(const uint8_t perm[256], int c, float x, float z) { return noise2_grad(perm, c, x, z); }
+float bmfo_noise2_value(const uint8_t perm[256], float x, float z) { return noise2_value(perm, x, z); }
+
 static float len3(float x, float y, float z) {
   float a = x * x, b = y * y, c = z * z;
   return sqrtf((a + b) + c);
@@ -247,7 +307,7 @@ static float ref_field(int kind, float res, float px, float py, float pz) {
 
 void bmfo_fill_field(int kind, const float* params, int dim, const float origin[3], float scale, float* out) {
   uint8_t perm[256];
-  if (kind == BMF_FIELD_TERRAIN_FBM) bmfo_perm_init((uint64_t)(int64_t)params[6], perm);
+  if (kind == BMF_FIELD_TERRAIN_FBM || kind == BMF_FIELD_TERRAIN_2D) bmfo_perm_init((uint64_t)(int64_t)params[6], perm);
   for (int x = 0; x < dim; ++x) {
     float px = origin[0] + (float)x * scale;
     for (int y = 0; y < dim; ++y) {
@@ -263,6 +323,10 @@ void bmfo_fill_field(int kind, const float* params, int dim, const float origin[
         } else if (kind == BMF_FIELD_TERRAIN_FBM) {
           float n = bmfo_fbm(perm, px, py, pz, (int)params[5], params[2], params[3], params[4]);
           v = fmaf(-params[1], n, py - params[0]);
+        } else if (kind == BMF_FIELD_TERRAIN_2D) {
+          const float n = bmfo_terrain2d_height(perm, params, px, pz);
+          const float dy = py * params[0];
+          v = -dy - n * params[1];
         } else {
           v = ref_field(kind, params[0], px, py, pz);
         }

@@ -34,6 +34,12 @@ float bmfo_perlin_textbook(const uint8_t perm[256], float x, float y, float z);
 float bmfo_fbm(const uint8_t perm[256], float x, float y, float z, int octaves, float freq, float lacunarity,
                float gain);
 
+/* BMF_FIELD_TERRAIN_2D pieces: the height noise of an (x, z) column and the
+ * 2D gradient / value noises it is built from. */
+float bmfo_terrain2d_height(const uint8_t perm[256], const float* params, float px, float pz);
+float bmfo_noise2_grad(const uint8_t perm[256], int c, float x, float z);
+float bmfo_noise2_value(const uint8_t perm[256], float x, float z);
+
 /* ---- density fields (Sampler::block equivalents) ----
  * out[x*dim*dim + y*dim + z] = f(origin + (x,y,z)*scale), z fastest
  * (ImplicitSampler.hpp:14-36).  params: see bmf.h (BMF_FIELD_*). */

@@ -56,6 +56,13 @@ def lib():
         L.bmfo_extract_batch_digest.restype = i64
         L.bmfo_extract_batch_digest.argtypes = [c_int, vp, c_int, vp, c_int, c_int, c_int, c_int, c_int, vp, vp,
                                                 c_int]
+        L.bmfo_terrain2d_height.restype = c_float
+        L.bmfo_terrain2d_height.argtypes = [vp, vp, c_float, c_float]
+        for fn in (L.bmfo_noise2_grad,):
+            fn.restype = c_float
+            fn.argtypes = [vp, c_int, c_float, c_float]
+        L.bmfo_noise2_value.restype = c_float
+        L.bmfo_noise2_value.argtypes = [vp, c_float, c_float]
         L.bmfo_digest64.restype = ctypes.c_uint64
         L.bmfo_digest64.argtypes = [vp, i64, c_int]
         _lib = L
@@ -81,6 +88,19 @@ def perlin(p, x, y, z, textbook=False):
     """One noise value: the line-separable form, or the textbook order."""
     fn = lib().bmfo_perlin_textbook if textbook else lib().bmfo_perlin
     return fn(_p(p), x, y, z)
+
+
+def noise2(p, x, z, kind="grad", c=0):
+    """One 2D gradient (component c) or value noise value of BMF_FIELD_TERRAIN_2D."""
+    if kind == "grad":
+        return lib().bmfo_noise2_grad(_p(p), c, x, z)
+    return lib().bmfo_noise2_value(_p(p), x, z)
+
+
+def terrain2d_height(params, px, pz):
+    prm = np.zeros(8, np.float32)
+    prm[: len(params)] = params
+    return lib().bmfo_terrain2d_height(_p(perm(int(params[6]))), _p(prm), px, pz)
 
 
 def fill_field(kind, params, dim, origin=(0.0, 0.0, 0.0), scale=1.0):

@@ -73,7 +73,8 @@ ALL = CASES + EXTRA
 
 @pytest.mark.parametrize("kind,params", [
     (L.FIELD_SPHERE_WAVE, workloads.SPHERE_WAVE_PARAMS), (L.FIELD_TERRAIN_FBM, workloads.TERRAIN_PARAMS),
-    (L.FIELD_TORUS_Z, [64.0]), (L.FIELD_SPHERE, [64.0]), (L.FIELD_CUBOID, [64.0]), (L.FIELD_PLANE_Y, [64.0])])
+    (L.FIELD_TORUS_Z, [64.0]), (L.FIELD_SPHERE, [64.0]), (L.FIELD_CUBOID, [64.0]), (L.FIELD_PLANE_Y, [64.0]),
+    (L.FIELD_TERRAIN_2D, workloads.TERRAIN_2D_PARAMS)])
 @pytest.mark.parametrize("dim,origin,scale", [(33, (-16.5, 3.25, -8.0), 1.0), (65, (0.0, 0.0, 0.0), 1.0),
                                               (65, (1024.0, 0.0, 512.0), 4.0)])
 def test_field_fill_bit_exact(ctx, kind, params, dim, origin, scale):

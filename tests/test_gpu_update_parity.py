@@ -67,18 +67,19 @@ def oracle_chunk(r, mode, placement, iters, process_boundary, normals):
     return O, p, n
 
 
-def compare_update(b, rows, mode, placement, iters, process_boundary, normals):
+def compare_update(b, rows, mode, placement, iters, process_boundary, normals, field=L.FIELD_TERRAIN_FBM,
+                   params=TERRAIN):
     """Every chunk of the update against the oracle; returns the number of
     chunks with a mesh."""
     info, got = arena_digests(b, normals)
-    counts, want = cpu.extract_batch_digest(rows[:, :5].astype(np.float32), L.FIELD_TERRAIN_FBM, TERRAIN, mode,
+    counts, want = cpu.extract_batch_digest(rows[:, :5].astype(np.float32), field, list(params), mode,
                                             placement, iters, process_boundary, normals)
     assert (info[:, 5] == 0).all(), "a chunk reported a capacity overflow"
     np.testing.assert_array_equal(info[:, 4], counts[:, 0], "contains_mesh")
     np.testing.assert_array_equal(info[:, 1], counts[:, 1], "vertex counts")
     np.testing.assert_array_equal(info[:, 3], counts[:, 2], "index counts")
     bad = np.flatnonzero((got != want).any(axis=1))
-    for i in bad[:3]:  # readable diff of the first mismatching chunks
+    for i in (bad[:3] if field == L.FIELD_TERRAIN_FBM else []):  # readable diff of the first mismatching chunks
         O, p, n = oracle_chunk(rows[i], mode, placement, iters, process_boundary, normals)
         m = b.chunk_mesh(int(i))
         np.testing.assert_array_equal(np_u32(m["idx"]), O["idx"], "chunk %d indices" % i)
@@ -199,3 +200,24 @@ def test_overlapping_chunks_with_boundary_processing(ctx, mode, placement):
     assert moved[on["boundary"].bool()].any()
     b.close()
     nb.close()
+
+
+@pytest.mark.parametrize("mode,placement", [(L.MODE_R, L.PLACE_CENTER), (L.MODE_Q, L.PLACE_MASSPOINT)])
+def test_terrain2d_update_matches_oracle(ctx, mode, placement):
+    """The reference's default world sampler shape (BMF_FIELD_TERRAIN_2D, the
+    perturbed heightmap of NoiseSampler.cpp:148-194 with WorldOctree.cpp:49-55's
+    settings) through a batched update: the x-plane fill evaluates each (x, z)
+    column's height once; every chunk matches the oracle."""
+    descs, rows = workloads.lod_update(n=96, seed=21)
+    for dsc, r in zip(descs, rows):
+        dsc.dim = min(dsc.dim, 65)
+        r[4] = dsc.dim
+        dsc.origin[1] = float(r[1]) - 128.0  # the band of this field: |y| <= 300
+        r[1] = dsc.origin[1]
+    field = workloads.terrain2d_field()
+    b = Batch(ctx, descs, field, mode=mode, placement=placement, iters=4, smooth_normals=True)
+    run_sized(b, True)
+    b.run(use_graph=True)
+    assert compare_update(b, rows, mode, placement, 4, False, True, L.FIELD_TERRAIN_2D,
+                          workloads.TERRAIN_2D_PARAMS) >= 20
+    b.close()
