@@ -129,6 +129,9 @@ SIGNATURES = {
     "bmf_fit_forward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.POINTER(c_int64),
                                   c_void_p]),
     "bmf_fit_backward": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "bmf_fit_loss_spheres": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p]),
+    "bmf_fit_adam": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_float, c_float,
+                               c_float, c_float, c_void_p]),
     "bmf_fit_destroy": (c_int32, [c_void_p]),
 }
 

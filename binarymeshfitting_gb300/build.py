@@ -19,7 +19,7 @@ LIB = os.path.join(BUILD, "libbmf_gb300.so")
 DROPIN_SRC = os.path.join(HERE, "dropin", "bmf_dropin.cpp")
 DROPIN = os.path.join(BUILD, "bmf_dropin")
 SOURCES = ["bmf_sample.cu", "bmf_extract.cu", "bmf_process.cu", "bmf_capi.cu", "bmf_noalloc.cu", "bmf_lod.cu",
-           "bmf_adjoint64.cu"]
+           "bmf_adjoint64.cu", "bmf_fit_loss.cu"]
 # Sources whose arithmetic does not mirror the reference's float rounding may
 # contract multiplies and adds (every other TU is built with --fmad=false).
 FMA_SOURCES = {"bmf_adjoint64.cu"}

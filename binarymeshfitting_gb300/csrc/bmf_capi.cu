@@ -1090,7 +1090,9 @@ struct bmf_fit {
   uint2* d_clist = nullptr;       // work list of active cells (+ counter after it)
   const float* last_density = nullptr;
   int64_t* h_pinned = nullptr;
+  float* d_lpart = nullptr;       // per-block partial sums of bmf_fit_loss_spheres
 };
+constexpr int kFitLossPartials = 1024;
 
 extern "C" {
 
@@ -1099,7 +1101,7 @@ bmf_status bmf_fit_destroy(bmf_fit* f) {
   void* ptrs[] = {f->d_chunks, f->d_units, f->d_flags, f->d_tot, f->d_words, f->d_totals, f->ws.vcnt, f->ws.icnt,
                   f->ws.gpl, f->ps.off, f->ps.cursor, f->ps.adj, f->ps.dual_p, f->ps.dual_n, f->ps.tmp, f->d_idxg,
                   f->d_vkey, f->d_valence, f->d_boundary, f->d_g, f->d_qlist, f->d_qseed, f->d_clist, f->d_order,
-                  f->d_pqueue, f->d_qflag};
+                  f->d_pqueue, f->d_qflag, f->d_lpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (f->h_pinned) cudaFreeHost(f->h_pinned);
@@ -1165,6 +1167,7 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
              (cudaMalloc(&f->d_qseed, sizeof(float) * 9 * (vcap + 1)) == cudaSuccess &&
               cudaMalloc(&f->d_qflag, vcap + 1) == cudaSuccess)) &&
             cudaMalloc(&f->d_clist, sizeof(uint2) * (vcap + icap / 4 + 2)) == cudaSuccess &&
+            cudaMalloc(&f->d_lpart, sizeof(float) * kFitLossPartials) == cudaSuccess &&
             cudaMallocHost(&f->h_pinned, sizeof(int64_t) * 4) == cudaSuccess &&
             cudaMemcpy(f->d_chunks, hc.data(), sizeof(ChunkDev) * n_chunks, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(f->d_units, units.data(), sizeof(int) * (n_chunks + 1), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -1227,6 +1230,31 @@ bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uin
     if (h_counts[0] > f->vcap || h_counts[1] > f->icap)
       return fail(ctx, BMF_ERR_CAPACITY, "bmf_fit_forward: output capacity exceeded (needed totals reported)");
   }
+  return BMF_OK;
+}
+
+bmf_status bmf_fit_loss_spheres(bmf_fit* f, const float* d_pos, const float* d_spheres, int32_t n_spheres,
+                                float* d_loss, float* d_grad_pos, void* stream) {
+  if (!f) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = f->ctx;
+  if (!d_pos || !d_spheres || n_spheres <= 0 || !d_loss || !d_grad_pos || !f->last_density || !f->d_lpart)
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_fit_loss_spheres: null buffer, no spheres or no forward yet");
+  BMF_LAUNCHED(ctx, launch_fit_loss_spheres(f->d_chunks, f->n, f->d_tot, f->d_totals, f->vcap, d_pos, d_spheres,
+                                            n_spheres, d_grad_pos, f->d_lpart, kFitLossPartials, d_loss,
+                                            (cudaStream_t)stream));
+  BMF_CUDA(ctx, cudaPeekAtLastError());
+  return BMF_OK;
+}
+
+bmf_status bmf_fit_adam(bmf_fit* f, float* d_param, const float* d_grad, float* d_m, float* d_v, int64_t n,
+                        int32_t* d_step, float lr, float beta1, float beta2, float eps, void* stream) {
+  if (!f) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = f->ctx;
+  if (!d_param || !d_grad || !d_m || !d_v || !d_step || n < 0 || !std::isfinite(lr) || !(beta1 >= 0.0f) ||
+      !(beta1 < 1.0f) || !(beta2 >= 0.0f) || !(beta2 < 1.0f) || !(eps > 0.0f))
+    return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_fit_adam: null buffer, n < 0 or bad hyper-parameters");
+  BMF_LAUNCHED(ctx, launch_adam(d_param, d_grad, d_m, d_v, n, d_step, lr, beta1, beta2, eps, (cudaStream_t)stream));
+  BMF_CUDA(ctx, cudaPeekAtLastError());
   return BMF_OK;
 }
 

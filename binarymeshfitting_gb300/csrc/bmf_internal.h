@@ -93,6 +93,15 @@ void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items,
                          uint32_t* exact, cudaStream_t st);
 // the band fill applies to fields of the form (py - h) - a * FBM with a > 0
 bool fill_band_supported(const FieldDev& field);
+// The batched-fitting loss (sum over chunks of the mean squared sphere-union
+// distance of the chunk's vertices) into *loss and its position gradient into
+// grad (vcap * 3, zero past the vertex total); n_partial per-block partial sums.
+int launch_fit_loss_spheres(const ChunkDev* d_chunks, int n_chunks, const uint32_t* d_tot, const int64_t* d_totals,
+                            int64_t vcap, const float* pos, const float* spheres, int k, float* grad, float* partial,
+                            int n_partial, float* loss, cudaStream_t st);
+// Adam over n parameters with the step count on the device (advanced after)
+int launch_adam(float* p, const float* g, float* m, float* v, int64_t n, int* step, float lr, float b1, float b2,
+                float eps, cudaStream_t st);
 // exact densities for the samples the count kernel listed in ws.fix (the
 // inexact ends of crossings; after launch_count, before launch_emit)
 void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, float* dens,

@@ -64,6 +64,42 @@ class FitPlan:
                                                       ctypes.c_void_p(out.data_ptr()), _stream()))
         return out
 
+    def loss_spheres(self, spheres: torch.Tensor, loss: torch.Tensor = None, grad: torch.Tensor = None):
+        """bmf_fit_loss_spheres on the last forward's positions: (loss (1,),
+        dL/dpos (vcap, 3), zero past the vertex total); asynchronous."""
+        sp = spheres.contiguous()
+        assert sp.is_cuda and sp.dtype == torch.float32 and sp.shape[0] == self.n and sp.shape[-1] == 4
+        loss = loss if loss is not None else torch.empty(1, dtype=torch.float32, device=self.ctx.device)
+        grad = grad if grad is not None else torch.empty((self.vcap, 3), dtype=torch.float32, device=self.ctx.device)
+        self.ctx._check(self.ctx.lib.bmf_fit_loss_spheres(self.h, ctypes.c_void_p(self.pos.data_ptr()),
+                                                          ctypes.c_void_p(sp.data_ptr()), sp.shape[1],
+                                                          ctypes.c_void_p(loss.data_ptr()),
+                                                          ctypes.c_void_p(grad.data_ptr()), _stream()))
+        return loss, grad
+
+    def step_grad(self, density: torch.Tensor, spheres: torch.Tensor, loss: torch.Tensor, grad_pos: torch.Tensor,
+                  grad_density: torch.Tensor):
+        """One fitting step's device work without a host sync (capturable in a
+        CUDA graph): forward, sphere-union loss and its position gradient,
+        backward into grad_density."""
+        self.forward(density, sync=False)
+        self.loss_spheres(spheres, loss, grad_pos)
+        self.ctx._check(self.ctx.lib.bmf_fit_backward(self.h, ctypes.c_void_p(grad_pos.data_ptr()), self.vcap,
+                                                      ctypes.c_void_p(grad_density.data_ptr()), _stream()))
+
+    def adam(self, param: torch.Tensor, grad: torch.Tensor, state: dict, lr=1e-2, betas=(0.9, 0.999), eps=1e-8):
+        """bmf_fit_adam: one Adam step in place on param; state holds the
+        moments and the device step count (created on the first call)."""
+        if not state:
+            state.update(m=torch.zeros_like(param), v=torch.zeros_like(param),
+                         step=torch.zeros(1, dtype=torch.int32, device=param.device))
+        self.ctx._check(self.ctx.lib.bmf_fit_adam(self.h, ctypes.c_void_p(param.data_ptr()),
+                                                  ctypes.c_void_p(grad.data_ptr()),
+                                                  ctypes.c_void_p(state["m"].data_ptr()),
+                                                  ctypes.c_void_p(state["v"].data_ptr()), param.numel(),
+                                                  ctypes.c_void_p(state["step"].data_ptr()), lr, betas[0], betas[1],
+                                                  eps, _stream()))
+
     def close(self):
         if self.h:
             self.ctx.lib.bmf_fit_destroy(self.h)

@@ -319,6 +319,26 @@ BMF_API bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, i
  * backward: do not change the density between forward and backward. */
 BMF_API bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uint32_t* d_idx,
                                    int64_t* d_chunk_info, int64_t* h_counts, void* stream);
+/* The loss of the batched-fitting workload on the device (no counterpart in
+ * the reference): for each chunk, the mean over its output vertices of the
+ * squared signed distance to the nearest of its n_spheres spheres
+ * (|p - c| - r), summed over the chunks, into *d_loss (one float); and
+ * dL/d(positions) into d_grad_pos (vcap * 3 floats, zero past the vertex
+ * total).  d_pos holds the last forward's positions; d_spheres is n_chunks *
+ * n_spheres rows {centre xyz, radius} (park unused rows far away).  Reads the
+ * vertex totals on the device: with bmf_fit_forward(h_counts = NULL) and
+ * bmf_fit_backward(n_grad_verts = vcap) a whole fitting step runs without a
+ * host sync.  The sum is reduced in a fixed order (reproducible). */
+BMF_API bmf_status bmf_fit_loss_spheres(bmf_fit* f, const float* d_pos, const float* d_spheres, int32_t n_spheres,
+                                        float* d_loss, float* d_grad_pos, void* stream);
+/* One Adam step (Kingma & Ba; torch.optim.Adam's arithmetic without weight
+ * decay or amsgrad) over n learnable values, the optimizer of the batched
+ * fitting workload (no counterpart in the reference): d_m / d_v are the
+ * moment buffers (zero before the first step), *d_step the step count on the
+ * device (0 before the first step; advanced by the call), so a CUDA graph that
+ * replays the call advances it.  One pass over the four arrays. */
+BMF_API bmf_status bmf_fit_adam(bmf_fit* f, float* d_param, const float* d_grad, float* d_m, float* d_v, int64_t n,
+                                int32_t* d_step, float lr, float beta1, float beta2, float eps, void* stream);
 /* dL/d(density) (n_chunks*dim^3, overwritten) from dL/d(positions) of the
  * last forward; d_grad_pos holds n_grad_verts * 3 floats. */
 BMF_API bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_verts, float* d_grad_density,

@@ -253,3 +253,74 @@ def test_chunk_sweep_fit_matches_whole_mesh_fit(ctx):
     gs = torch.cat([p[3] for p in parts]).double().cpu().numpy()
     assert nv0 > 0 and np.abs(gs).max() > 0
     assert np.abs(gb - gs).max() <= 1e-5 * np.abs(gs).max()
+
+
+def test_device_sphere_loss_matches_torch_and_captures_in_a_graph():
+    """bmf_fit_loss_spheres (loss and position gradient read off the device
+    chunk table) against the torch sphere-union loss and its autograd
+    gradient; then a whole fitting step (forward, loss, backward) captured as a
+    CUDA graph gives the eager step's loss bit for bit and its density gradient
+    up to the order of the chain rule's float atomics."""
+    from binarymeshfitting_gb300.fitting import FitPlan, sphere_union_loss
+    ctx = Context(0)
+    n, dim = 6, 33
+    dens, spheres = workloads.fit_batch(n, dim=dim, seed=12)
+    plan = FitPlan(ctx, n, dim, L.PLACE_QEF, 4)
+    pos, _, info = plan.forward(dens)
+    leaf = pos.detach().clone().requires_grad_(True)
+    want = sphere_union_loss(leaf, info, spheres)
+    (gwant,) = torch.autograd.grad(want, leaf)
+    loss, grad = plan.loss_spheres(spheres)
+    nv = pos.shape[0]
+    assert abs(float(loss) - float(want)) <= 1e-5 * abs(float(want))
+    assert torch.allclose(grad[:nv], gwant, rtol=1e-5, atol=1e-7)
+    assert (grad[nv:] == 0).all()
+    # eager asynchronous step vs the same step replayed from a CUDA graph
+    lb, gp = torch.zeros(1, device="cuda"), torch.empty((plan.vcap, 3), device="cuda")
+    g_eager, g_graph = torch.empty_like(dens), torch.empty_like(dens)
+    plan.step_grad(dens, spheres, lb, gp, g_eager)
+    torch.cuda.synchronize()
+    loss_eager = float(lb)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        plan.step_grad(dens, spheres, lb, gp, g_graph)
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        plan.step_grad(dens, spheres, lb, gp, g_graph)
+    g_graph.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(lb) == loss_eager
+    assert torch.allclose(g_graph, g_eager, rtol=1e-5, atol=1e-6 * float(g_eager.abs().max()))
+    g_ref = plan.backward(gwant)  # the same adjoint applied to torch's position gradient
+    assert float((g_eager - g_ref).norm()) <= 1e-4 * float(g_ref.norm())
+    plan.close()
+    ctx.close()
+
+
+def test_device_adam_matches_torch_adam():
+    """bmf_fit_adam against torch.optim.Adam (same hyper-parameters, no weight
+    decay) over five steps, on a length that is not a multiple of four and on
+    an unaligned view (the scalar path)."""
+    from binarymeshfitting_gb300.fitting import FitPlan
+    ctx = Context(0)
+    plan = FitPlan(ctx, 1, 17, L.PLACE_MASSPOINT, 0)
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    for n, off in ((100_003, 0), (4099, 1)):
+        base = torch.randn(n + off, device="cuda", generator=gen)
+        p_ours = base.clone()[off:]
+        p_ref = torch.nn.Parameter(base.clone()[off:].clone())
+        opt = torch.optim.Adam([p_ref], lr=3e-2, betas=(0.9, 0.999), eps=1e-8)
+        state = {}
+        for k in range(5):
+            g = torch.randn(n, device="cuda", generator=gen)
+            p_ref.grad = g.clone()
+            opt.step()
+            plan.adam(p_ours, g, state, lr=3e-2)
+        torch.cuda.synchronize()
+        assert int(state["step"]) == 5
+        assert torch.allclose(p_ours, p_ref.detach(), rtol=1e-5, atol=1e-6)
+    plan.close()
+    ctx.close()
