@@ -1055,6 +1055,26 @@ __device__ __forceinline__ int packed_mask(uint32_t nbits, int ox, int oy, int o
 constexpr int kTileWords = 16;
 constexpr int kEmitWarps = 8;
 
+// One 4-byte global -> shared copy in flight (cp.async; the staged pieces are
+// 4-byte words of scattered lines, below the 16-byte unit of bulk copies), and
+// the wait for all of a thread's copies.  BMF_EMIT_ASYNC 0 keeps plain loads.
+#ifndef BMF_EMIT_ASYNC
+#define BMF_EMIT_ASYNC 1
+#endif
+__device__ __forceinline__ void stage_async(uint32_t* dst, const uint32_t* src) {
+#if BMF_EMIT_ASYNC
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src) : "memory");
+#else
+  *dst = __ldg(src);
+#endif
+}
+__device__ __forceinline__ void stage_wait() {
+#if BMF_EMIT_ASYNC
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+#endif
+}
+
 struct RTile {
   NbCache nb[kTileWords];
   uint32_t ib[kTileWords], p0[kTileWords], p1[kTileWords], p2[kTileWords];
@@ -1102,6 +1122,8 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
     // (word, neighbour line) loads the line's blocks zb-1..zb+1; one item per
     // (word, owner line) its vertex bases in blocks zb, zb+1; one per word its
     // index base and count planes
+    // (asynchronous global -> shared copies: a lane issues every copy of its
+    // items and waits once, instead of a load-then-store per item)
     for (int k = lane; k < nt * 21; k += 32) {
       const int t = k / 21, it = k - t * 21;
       const int dim = R.dim[t], zc = R.zc[t], x = R.x[t], y = R.y[t], zb = R.zb[t];
@@ -1114,9 +1136,9 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
           dst[0] = dst[1] = dst[2] = 0u;
         } else {
           const uint32_t* L = words + cw + (xx * dim + yy) * zc + zb;
-          dst[0] = zb > 0 ? __ldg(L - 1) : 0u;
-          dst[1] = __ldg(L);
-          dst[2] = zb + 1 < zc ? __ldg(L + 1) : 0u;
+          if (zb > 0) stage_async(dst, L - 1); else dst[0] = 0u;
+          stage_async(dst + 1, L);
+          if (zb + 1 < zc) stage_async(dst + 2, L + 1); else dst[2] = 0u;
         }
       } else if (it < 20) {
         const int l = it - 16;
@@ -1124,19 +1146,20 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
         uint32_t* dst = R.nb[t].vb + (l >> 1) * 4 + (l & 1) * 2;
         if (xx < dim && yy < dim) {
           const uint32_t* V = ws.vcnt + cw + (xx * dim + yy) * zc + zb;
-          dst[0] = __ldg(V);
-          dst[1] = zb + 1 < zc ? __ldg(V + 1) : 0u;
+          stage_async(dst, V);
+          if (zb + 1 < zc) stage_async(dst + 1, V + 1); else dst[1] = 0u;
         } else {
           dst[0] = dst[1] = 0u;
         }
       } else {
         const int64_t wi = cw + (x * dim + y) * zc + zb;
-        R.ib[t] = __ldg(ws.icnt + wi);
-        R.p0[t] = __ldg(ws.gpl + 3 * wi);
-        R.p1[t] = __ldg(ws.gpl + 3 * wi + 1);
-        R.p2[t] = __ldg(ws.gpl + 3 * wi + 2);
+        stage_async(&R.ib[t], ws.icnt + wi);
+        stage_async(&R.p0[t], ws.gpl + 3 * wi);
+        stage_async(&R.p1[t], ws.gpl + 3 * wi + 1);
+        stage_async(&R.p2[t], ws.gpl + 3 * wi + 2);
       }
     }
+    stage_wait();
     __syncwarp();
     // 3. active cells per word (owned crossings or triangles), flattened
     {
