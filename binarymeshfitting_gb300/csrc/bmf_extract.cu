@@ -1042,16 +1042,17 @@ __device__ __forceinline__ int packed_mask(uint32_t nbits, int ox, int oy, int o
 // entries at a time and stages, per word, its neighbourhood (NbCache: the
 // occupancy words of lines (x-1..x+2, y-1..y+2) in blocks zb-1..zb+1 and the
 // scanned vertex bases of lines (x..x+1, y..y+1) in blocks zb..zb+1), its
-// index base and its triangle-count planes in shared memory.  Then one lane
-// per active cell of the tile (a flattened scan of the words' active-cell
-// counts) writes exactly what the reference writes for that cell: its owned
-// vertices (ids from the word base and the crossing words,
-// calculate_isovertex positions, boundary, key, init_valence) and its
-// triangles (slot from the word's index base and the count planes).  Every
-// mask, valence and neighbour vertex id is read from shared memory; only the
-// two endpoint densities of a vertex come from global memory.  Warps work on
-// their own tiles with no block-wide barrier, so one warp's staging loads
-// overlap the others' cell work.
+// index base and its triangle-count planes in shared memory.  Then the tile's
+// output is written in two flattened lists, so that every lane does the same
+// work: one lane per vertex (the k-th vertex of a word is found from the
+// popcounts of its crossing words; calculate_isovertex position, boundary,
+// key, init_valence), then one lane per triangle (the k-th triangle of a word
+// from its count planes; the cell's Marching-Cubes case and its three vertex
+// ids, polygonize_cell order).  Ids and slots come from the scanned counts, so
+// the output is exactly the reference's.  Every mask, valence and neighbour
+// vertex id is read from shared memory; only the two endpoint densities of a
+// vertex come from global memory.  Warps work on their own tiles with no
+// block-wide barrier, so one warp's staging loads overlap the others' work.
 constexpr int kTileWords = 16;
 constexpr int kEmitWarps = 8;
 
@@ -1078,11 +1079,20 @@ __device__ __forceinline__ void stage_wait() {
 struct RTile {
   NbCache nb[kTileWords];
   uint32_t ib[kTileWords], p0[kTileWords], p1[kTileWords], p2[kTileWords];
-  uint32_t X[kTileWords], Y[kTileWords], Z[kTileWords], act[kTileWords];
+  uint32_t X[kTileWords], Y[kTileWords], Z[kTileWords];
   int x[kTileWords], y[kTileWords], zb[kTileWords], dim[kTileWords], zc[kTileWords];
   int64_t cw[kTileWords], dens[kTileWords], vout[kTileWords], iout[kTileWords];
-  int off[kTileWords + 1];
+  int voff[kTileWords + 1], toff[kTileWords + 1];  // exclusive vertex / triangle offsets of the tile's words
 };
+
+// The tile word holding flattened item j: the last t < nt with off[t] <= j.
+__device__ __forceinline__ int tile_word(const int* off, int nt, int j) {
+  int t = 0;
+#pragma unroll
+  for (int s = kTileWords / 2; s > 0; s >>= 1)
+    if (t + s < nt && off[t + s] <= j) t += s;
+  return t;
+}
 
 __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const ChunkDev* __restrict__ chunks,
                                                                  const uint32_t* __restrict__ words,
@@ -1161,9 +1171,10 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
     }
     stage_wait();
     __syncwarp();
-    // 3. active cells per word (owned crossings or triangles), flattened
+    // 3. per word: owned crossings, vertex count and triangle count (count
+    // planes), scanned over the tile in one word (vertices low, triangles high)
     {
-      int cnt = 0;
+      uint32_t packed = 0u;
       if (lane < nt) {
         const NbCache& nb = R.nb[lane];
         const int dim = R.dim[lane], x = R.x[lane], y = R.y[lane], zb = R.zb[lane];
@@ -1173,111 +1184,132 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
         uint32_t Z = wc ^ ((wc >> 1) | (nb.w[(1 * 4 + 1) * 3 + 2] << 31));
         const int valid = dim - 1 - 32 * zb;
         if (valid < 32) Z &= valid <= 0 ? 0u : ((1u << valid) - 1u);
-        const uint32_t act = R.p0[lane] | R.p1[lane] | R.p2[lane] | X | Y | Z;
         R.X[lane] = X;
         R.Y[lane] = Y;
         R.Z[lane] = Z;
-        R.act[lane] = act;
-        cnt = __popc(act);
+        const uint32_t nv = __popc(X) + __popc(Y) + __popc(Z);
+        const uint32_t ntri = __popc(R.p0[lane]) + 2u * __popc(R.p1[lane]) + 4u * __popc(R.p2[lane]);
+        packed = nv | (ntri << 16);  // at most 96 and 160 per word
       }
-      int incl = cnt;
+      uint32_t incl = packed;
 #pragma unroll
       for (int o = 1; o < kTileWords; o <<= 1) {
-        const int v = __shfl_up_sync(kFull, incl, o);
+        const uint32_t v = __shfl_up_sync(kFull, incl, o);
         if (lane >= o) incl += v;
       }
-      if (lane < kTileWords) R.off[lane + 1] = incl;
-      if (lane == 0) R.off[0] = 0;
+      if (lane < kTileWords) {
+        R.voff[lane + 1] = (int)(incl & 0xFFFFu);
+        R.toff[lane + 1] = (int)(incl >> 16);
+      }
+      if (lane == 0) R.voff[0] = R.toff[0] = 0;
     }
     __syncwarp();
-    const int total = R.off[nt];
-    // 4. one lane per active cell
-    for (int j = lane; j < total; j += 32) {
-      int lo = 0, hi = nt - 1;  // last t with off[t] <= j
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (R.off[mid] <= j) lo = mid; else hi = mid - 1;
-      }
-      const int t = lo;
-      const int l = nth_set_bit(R.act[t], j - R.off[t]);
-      const NbCache& nb = R.nb[t];
-      const int dim = R.dim[t], x = R.x[t], y = R.y[t], zb = R.zb[t];
-      const int z = 32 * zb + l;
-      const uint32_t lt = lane_lt(l);
+    // 4. one lane per vertex: the k-th vertex of word t is at the cell l whose
+    // preceding cells own k or fewer crossings, the (k - that)-th of its axes
+    const int nvt = R.voff[nt];
+    for (int j = lane; j < nvt; j += 32) {
+      const int t = tile_word(R.voff, nt, j);
+      const int k = j - R.voff[t];
       const uint32_t X = R.X[t], Y = R.Y[t], Z = R.Z[t];
-      const uint32_t own = ((X >> l) & 1u) | (((Y >> l) & 1u) << 1) | (((Z >> l) & 1u) << 2);
-      const int64_t vout = R.vout[t];
-      // inside bits of lines (x-1..x+1, y-1..y+1) at samples z-1..z+1
-      uint32_t nbits = 0u;
+      int l = 0;
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          const int zr0 = l + 31, b = zr0 >> 5;  // z - 1 relative to block zb - 1
-          const uint32_t* w = nb.w + (i * 4 + j) * 3;
-          const uint64_t q = ((uint64_t)w[b + 1] << 32) | w[b];
-          nbits |= ((uint32_t)(q >> (zr0 & 31)) & 7u) << (3 * (3 * i + j));
-        }
-      if (own) {
-        const float* D = dens + R.dens[t];
-        uint32_t vid = nb.vb[0] + __popc(X & lt) + __popc(Y & lt) + __popc(Z & lt);
-        for (int a = 0; a < 3; ++a) {
-          if (!((own >> a) & 1u)) continue;
-          const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
-          const int64_t gv = vout + vid;
-          ++vid;
-          if (gv >= out.vcap) continue;
-          const float s0 = dens_at(D, dim, x, y, z), s1 = dens_at(D, dim, x1, y1, z1);
-          const float mu = (0.0f - s0) / (s1 - s0);
-          const float q0[3] = {(float)x, (float)y, (float)z};
-          const float dl[3] = {(float)(x1 - x), (float)(y1 - y), (float)(z1 - z)};
-          float* P = out.pos + 3 * gv;
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            const float dv = dl[k] * mu;
-            P[k] = dv + q0[k];
-          }
-          if (out.boundary)
-            out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
-                                x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
-          if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
-          if (out.vkey) out.vkey[gv] = vertex_key(x, y, z, a);
-          if (out.valence) {
-            // init_valence: uses of this edge by the (up to) four interior
-            // cells around it (polygonize skips far-face cells, DMCChunk.cpp:528)
-            int val = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const int d1 = k >> 1, d2 = k & 1;
-              int ox = 0, oy = 0, oz = 0;
-              if (a == 0) { oy = -d1; oz = -d2; }
-              else if (a == 1) { ox = -d1; oz = -d2; }
-              else { ox = -d1; oy = -d2; }
-              const int e = 4 * a + 2 * d1 + d2;
-              const int cx = x + ox, cy = y + oy, cz = z + oz;
-              if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
-              val += (int)((s_uses[packed_mask(nbits, ox, oy, oz)] >> (4 * e)) & 0xF);
-            }
-            out.valence[gv] = (uint8_t)val;
-          }
-        }
+      for (int s = 16; s > 0; s >>= 1) {
+        const uint32_t m = lane_lt(l + s);
+        if ((int)(__popc(X & m) + __popc(Y & m) + __popc(Z & m)) <= k) l += s;
       }
-      // triangles: polygonize_cell order
-      if (x >= dim - 1 || y >= dim - 1 || z >= dim - 1) continue;
-      const uint64_t tw = s_tri[packed_mask(nbits, 0, 0, 0)];
-      const int t3 = 3 * (int)(tw >> 60);
-      if (t3 == 0) continue;
-      const int before = __popc(R.p0[t] & lt) + 2 * __popc(R.p1[t] & lt) + 4 * __popc(R.p2[t] & lt);
-      int64_t gi = R.iout[t] + (int64_t)R.ib[t] + 3 * before;
-      for (int k = 0; k < t3; ++k, ++gi) {
-        const int e = tri_edge(tw, k);
+      const uint32_t lt = lane_lt(l);
+      const int r = k - (int)(__popc(X & lt) + __popc(Y & lt) + __popc(Z & lt));
+      uint32_t own = ((X >> l) & 1u) | (((Y >> l) & 1u) << 1) | (((Z >> l) & 1u) << 2);
+      if (r >= 1) own &= own - 1u;
+      if (r >= 2) own &= own - 1u;
+      const int a = __ffs(own) - 1;
+      const NbCache& nb = R.nb[t];
+      const int64_t gv = R.vout[t] + (int64_t)nb.vb[0] + k;
+      if (gv >= out.vcap) continue;
+      const int dim = R.dim[t], x = R.x[t], y = R.y[t], z = 32 * R.zb[t] + l;
+      const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+      const float* D = dens + R.dens[t];
+      const float s0 = dens_at(D, dim, x, y, z), s1 = dens_at(D, dim, x1, y1, z1);
+      const float mu = (0.0f - s0) / (s1 - s0);
+      const float q0[3] = {(float)x, (float)y, (float)z};
+      const float dl[3] = {(float)(x1 - x), (float)(y1 - y), (float)(z1 - z)};
+      float* P = out.pos + 3 * gv;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float dv = dl[c] * mu;
+        P[c] = dv + q0[c];
+      }
+      if (out.boundary)
+        out.boundary[gv] = (x == 0 || y == 0 || z == 0 || x == dim - 1 || y == dim - 1 || z == dim - 1 ||
+                            x1 == dim - 1 || y1 == dim - 1 || z1 == dim - 1);
+      if (out.nrm) { out.nrm[3 * gv] = 0.0f; out.nrm[3 * gv + 1] = 0.0f; out.nrm[3 * gv + 2] = 0.0f; }
+      if (out.vkey) out.vkey[gv] = vertex_key(x, y, z, a);
+      if (out.valence) {
+        // inside bits of lines (x-1..x+1, y-1..y+1) at samples z-1..z+1
+        uint32_t nbits = 0u;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj) {
+            const int zr0 = l + 31, b = zr0 >> 5;  // z - 1 relative to block zb - 1
+            const uint32_t* w = nb.w + (i * 4 + jj) * 3;
+            const uint64_t q = ((uint64_t)w[b + 1] << 32) | w[b];
+            nbits |= ((uint32_t)(q >> (zr0 & 31)) & 7u) << (3 * (3 * i + jj));
+          }
+        // init_valence: uses of this edge by the (up to) four interior cells
+        // around it (polygonize skips far-face cells, DMCChunk.cpp:528)
+        int val = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int d1 = c >> 1, d2 = c & 1;
+          const int ox = a == 0 ? 0 : -d1, oy = a == 0 ? -d1 : (a == 1 ? 0 : -d2), oz = a == 2 ? 0 : -d2;
+          const int e = 4 * a + 2 * d1 + d2;
+          const int cx = x + ox, cy = y + oy, cz = z + oz;
+          if (cx < 0 || cy < 0 || cz < 0 || cx > dim - 2 || cy > dim - 2 || cz > dim - 2) continue;
+          val += (int)((s_uses[packed_mask(nbits, ox, oy, oz)] >> (4 * e)) & 0xF);
+        }
+        out.valence[gv] = (uint8_t)val;
+      }
+    }
+    // 5. one lane per triangle: the k-th triangle of word t is in the cell l
+    // whose preceding cells hold k or fewer (count planes), its (k - that)-th
+    const int ntt = R.toff[nt];
+    for (int j = lane; j < ntt; j += 32) {
+      const int t = tile_word(R.toff, nt, j);
+      const int k = j - R.toff[t];
+      const uint32_t c0 = R.p0[t], c1 = R.p1[t], c2 = R.p2[t];
+      int l = 0;
+#pragma unroll
+      for (int s = 16; s > 0; s >>= 1) {
+        const uint32_t m = lane_lt(l + s);
+        if ((int)(__popc(c0 & m) + 2 * __popc(c1 & m) + 4 * __popc(c2 & m)) <= k) l += s;
+      }
+      const uint32_t lt = lane_lt(l);
+      const int r = k - (int)(__popc(c0 & lt) + 2 * __popc(c1 & lt) + 4 * __popc(c2 & lt));
+      const NbCache& nb = R.nb[t];
+      // the cell's case: corner (dx, dy, dz) is bit 4 dx + 2 dy + dz
+      int mask = 0;
+#pragma unroll
+      for (int d = 0; d < 4; ++d) {
+        const uint32_t* w = nb.w + ((1 + (d >> 1)) * 4 + 1 + (d & 1)) * 3;
+        const uint64_t q = ((uint64_t)w[2] << 32) | w[1];
+        mask |= (int)((q >> l) & 3u) << (2 * d);
+      }
+      const uint64_t tw = s_tri[mask];
+      if (3 * r + 3 > 3 * (int)(tw >> 60)) continue;  // the planes and the case table agree
+      const int dim = R.dim[t], x = R.x[t], y = R.y[t], zb = R.zb[t], z = 32 * zb + l;
+      const int64_t gi = R.iout[t] + (int64_t)R.ib[t] + 3 * (int64_t)k;
+      const int64_t vout = R.vout[t];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const int e = tri_edge(tw, 3 * r + i);
         // EDGE_V owner of edge e: axis e >> 2, offsets from its two low bits
         const int ea = e >> 2, d1 = (e >> 1) & 1, d2 = e & 1;
         const int ox = ea == 0 ? 0 : d1, oy = ea == 0 ? d1 : (ea == 1 ? 0 : d2), oz = ea == 2 ? 0 : d2;
         const uint32_t vid = nb_vertex_id(nb, dim, x, y, zb, ox, oy, z + oz, ea);
-        if (gi < out.icap) {
-          out.idx[gi] = vid;
-          if (out.idx_global) out.idx_global[gi] = (uint32_t)(vout + vid);
+        if (gi + i < out.icap) {
+          out.idx[gi + i] = vid;
+          if (out.idx_global) out.idx_global[gi + i] = (uint32_t)(vout + vid);
         }
       }
     }
