@@ -53,11 +53,18 @@ __device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t
     v[k] = __ldg(idx + N * t + k);
     if ((int64_t)v[k] >= nvb) v[k] = 0;  // an index outside the mesh reads vertex 0 instead of faulting
   }
+  // each corner position is loaded once; the centroid and the face normal
+  // read the same registers
+  float P[N][3];
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) P[k][c] = sweep_ld<COH>(pos + 3 * v[k] + c);
   float p[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
   for (int k = 0; k < N; ++k) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) p[c] = p[c] + sweep_ld<COH>(pos + 3 * v[k] + c);
+    for (int c = 0; c < 3; ++c) p[c] = p[c] + P[k][c];
   }
 #pragma unroll
   for (int c = 0; c < 3; ++c) p[c] = p[c] / (float)N;
@@ -77,8 +84,8 @@ __device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t
       if (v[0] != v[1] && v[1] != v[2] && v[0] != v[2]) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          a[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[1] + c);
-          b[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[2] + c);
+          a[c] = P[0][c] - P[1][c];
+          b[c] = P[0][c] - P[2][c];
         }
       }
       nrm3(a, na);
@@ -88,19 +95,18 @@ __device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t
       for (int c = 0; c < 3; ++c) o[c] = -o[c];
     } else {
       float a[3], b[3], na[3], nb[3], n1[3], n2[3];
-      const uint32_t v3 = v[N - 1];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        a[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[1] + c);
-        b[c] = sweep_ld<COH>(pos + 3 * v[0] + c) - sweep_ld<COH>(pos + 3 * v[2] + c);
+        a[c] = P[0][c] - P[1][c];
+        b[c] = P[0][c] - P[2][c];
       }
       nrm3(a, na);
       nrm3(b, nb);
       cross3(na, nb, n1);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        a[c] = sweep_ld<COH>(pos + 3 * v[2] + c) - sweep_ld<COH>(pos + 3 * v3 + c);
-        b[c] = sweep_ld<COH>(pos + 3 * v[2] + c) - sweep_ld<COH>(pos + 3 * v[0] + c);
+        a[c] = P[2][c] - P[N - 1][c];
+        b[c] = P[2][c] - P[0][c];
       }
       nrm3(a, na);
       nrm3(b, nb);
