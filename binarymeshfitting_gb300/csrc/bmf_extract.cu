@@ -953,15 +953,28 @@ __global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_c
       adj_vertex<MODE>(T, ch, words, ws, __ldg(vkey + v), adj + o, room);
     }
     __syncthreads();
+    // the sweeps in 32-bit chunk-relative indices over chunk-based pointers
+    // (vertex ids, primitive ids and adjacency offsets stay mesh-wide)
+    const uint32_t np_c = (uint32_t)max((int64_t)0, p1 - p0), nv_c = (uint32_t)max((int64_t)0, v1 - v0);
+    const uint32_t nvb32 = (uint32_t)min(nvb, (int64_t)UINT32_MAX);
+    const uint32_t npl32 = (uint32_t)min(n_prims, (int64_t)UINT32_MAX);
+    const uint32_t* idx_c = idx + N * p0;
+    float* dp_c = dual_p + 4 * p0;
+    float* dn_c = dual_n + 2 * p0;
+    const uint32_t* off_c = off + v0;
+    const uint8_t* val_c = valence + v0;
+    const uint8_t* bnd_c = boundary + v0;
+    float* pos_c = pos + 3 * v0;
+    float* nrm_c = nrm ? nrm + 3 * v0 : nullptr;
     for (int m = 0; m < iters; ++m) {
       const int normal_mode = !sn ? 0 : ((m == 0 || m < max_norms || m < 3) ? 1 : 2);
       const int set_colors = (m < iters - 1) ? ((m == 3) || (m == 0 && iters <= 3)) : 0;
-      for (int64_t t = p0 + threadIdx.x; t < p1; t += kThreads)
-        dual_prim<N, true, true>(t, nvb, idx, pos, nrm, dual_p, dual_n, normal_mode);
+      for (uint32_t t = threadIdx.x; t < np_c; t += kThreads)
+        dual_prim<N, true, true>(t, nvb32, idx_c, pos, nrm, dp_c, dn_c, normal_mode);
       __syncthreads();
-      for (int64_t v = v0 + threadIdx.x; v < v1; v += kThreads)
-        primal_vertex<true, true>(v, n_prims, adj_cap, off, nullptr, valence, adj, boundary, dual_p, dual_n, pos, nrm,
-                            process_boundary, sn, set_colors);
+      for (uint32_t v = threadIdx.x; v < nv_c; v += kThreads)
+        primal_vertex<true, true>(v, npl32, adj_cap, off_c, nullptr, val_c, adj, bnd_c, dual_p, dual_n, pos_c, nrm_c,
+                                  process_boundary, sn, set_colors);
       __syncthreads();
     }
   }

@@ -42,16 +42,19 @@ __device__ __forceinline__ void cross3(const float a[3], const float b[3], float
 // 1 face normal, 2 sum of vertex normals.  PACKED: primitive t's dual point
 // and normal go to ((float4*)dual_p)[t] = (p, n.x) and ((float2*)dual_n)[t] =
 // (n.y, n.z) -- one 16-byte and one 8-byte gather per primitive in the primal
-// step instead of six 4-byte ones; the values are the same.
-template <int N, bool COH = false, bool PACKED = false>
-__device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t* __restrict__ idx,
+// step instead of six 4-byte ones; the values are the same.  I: the index
+// type of t and nvb -- int64_t over a whole mesh, or uint32_t within one
+// chunk (idx and the dual arrays then start at the chunk's first primitive;
+// vertex ids stay mesh-wide).
+template <int N, bool COH = false, bool PACKED = false, typename I = int64_t>
+__device__ __forceinline__ void dual_prim(I t, I nvb, const uint32_t* __restrict__ idx,
                                           const float* __restrict__ pos, const float* __restrict__ nrm,
                                           float* __restrict__ dual_p, float* __restrict__ dual_n, int normal_mode) {
   uint32_t v[N];
 #pragma unroll
   for (int k = 0; k < N; ++k) {
     v[k] = __ldg(idx + N * t + k);
-    if ((int64_t)v[k] >= nvb) v[k] = 0;  // an index outside the mesh reads vertex 0 instead of faulting
+    if ((I)v[k] >= nvb) v[k] = 0;  // an index outside the mesh reads vertex 0 instead of faulting
   }
   // each corner position is loaded once; the centroid and the face normal
   // read the same registers
@@ -140,8 +143,11 @@ __device__ __forceinline__ void dual_prim(int64_t t, int64_t nvb, const uint32_t
   }
 }
 
-template <bool COH = false, bool PACKED = false>
-__device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t adj_cap,
+// I: the index type of v and np_lim, as for dual_prim (within one chunk, off,
+// cursor, valence, boundary, pos and nrm start at the chunk's first vertex;
+// adjacency offsets and primitive ids stay mesh-wide).
+template <bool COH = false, bool PACKED = false, typename I = int64_t>
+__device__ __forceinline__ void primal_vertex(I v, I np_lim, int64_t adj_cap,
                                               const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
                                               const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
                                               const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
@@ -162,7 +168,7 @@ __device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t
     // which keep the one-by-one order (the same rounding)
     for (; k0 + 2 <= n; k0 += 2) {
       const uint32_t t0 = sweep_ld<COH>(a + k0), t1 = sweep_ld<COH>(a + k0 + 1);
-      const bool ok0 = (int64_t)t0 < np_lim, ok1 = (int64_t)t1 < np_lim;
+      const bool ok0 = (I)t0 < np_lim, ok1 = (I)t1 < np_lim;
       const float4 q0 = ok0 ? sweep_ld<COH>(reinterpret_cast<const float4*>(dual_p) + t0) : make_float4(0, 0, 0, 0);
       const float4 q1 = ok1 ? sweep_ld<COH>(reinterpret_cast<const float4*>(dual_p) + t1) : make_float4(0, 0, 0, 0);
       float2 r0 = make_float2(0.0f, 0.0f), r1 = make_float2(0.0f, 0.0f);
@@ -182,7 +188,7 @@ __device__ __forceinline__ void primal_vertex(int64_t v, int64_t np_lim, int64_t
   }
   for (uint32_t k = k0; k < n; ++k) {
     const uint32_t t = sweep_ld<COH>(a + k);
-    if ((int64_t)t >= np_lim) continue;  // never read past the dual points
+    if ((I)t >= np_lim) continue;  // never read past the dual points
     if (PACKED) {
       const float4 q = sweep_ld<COH>(reinterpret_cast<const float4*>(dual_p) + t);
       p[0] = p[0] + q.x;
