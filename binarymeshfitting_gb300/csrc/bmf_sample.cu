@@ -191,12 +191,17 @@ __device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const float4* _
 }
 
 // Band fill (BAND = true).  The terrain density is d = (py - h) - a * FBM with
-// py constant along a line, and every octave's noise is bounded: the corner
-// weights of a sample sum to one and a corner's gradient dot product is at
-// most |dx| + |dy| + |dz|, whose weighted sums are each at most 1/2
-// (x (1 - fade x) + (1 - x) fade x <= 1/2), so |noise| <= 3/2.  Before each
+// py constant along a line, and every octave's noise is bounded: at offsets
+// (u, v, w) in the lattice cell the corner weights W_c (products of fade and
+// 1 - fade) are non-negative and sum to one, and a corner's gradient has two
+// components +/-1 and one 0, so its dot product is at most m_c, the sum of the
+// two largest of |u - cx|, |v - cy|, |w - cz|; hence |noise| <= F(u, v, w) =
+// sum_c W_c m_c.  Each partial derivative of F is at most fade' + 1 <= 2.875
+// in magnitude, so F is at most its maximum over a grid of spacing h plus
+// 4.3125 h: 1.0364 + 0.0216 on a 201^3 grid (recomputed by the test suite),
+// below kNoiseBound = 1.0625.  Before each
 // octave o a run therefore knows its FBM sums to within
-// T_o = 3/2 * sum_{j >= o} |amp_j|: when every sample's partial sum S lies
+// T_o = kNoiseBound * sum_{j >= o} |amp_j|: when every sample's partial sum S lies
 // below (py - h) / a - T_o (all outside) or above (py - h) / a + T_o (all
 // inside), the signs -- the occupancy words -- are final and the run stops.
 // Its samples then hold the partial density (right sign, inexact value) and
@@ -210,7 +215,7 @@ __device__ __forceinline__ void oct_line_cell(OctLine& s, int Z, const float4* _
 #define BMF_BAND_CTAS 3
 #endif
 constexpr int kBandCtas = BMF_BAND_CTAS;  // resident CTAs per SM the band fill's registers are sized for
-constexpr float kNoiseBound = 1.5f;
+constexpr float kNoiseBound = 1.0625f;  // |improved noise| <= 1.058 (above)
 constexpr float kBandMargin = 1e-3f;  // float rounding of the sums, far below this
 
 // Dynamic shared memory: the density stage (16-sample half blocks of the
@@ -254,7 +259,7 @@ __global__ void __launch_bounds__(kFillLines, BAND ? kBandCtas : 3) k_fill_terra
   float4* s_ab = s_dyn + (BAND ? 0 : kStageFloats / 4);          // [octave][line]: a0, b0, a1, b1
   int* s_zp = reinterpret_cast<int*>(s_ab + (size_t)oct * kFillLines);  // [octave][line]: Zp
   if (BAND && threadIdx.x == 0) {
-    // T_o = 3/2 sum_{j >= o} |amp_j|: the total, then less one octave at a
+    // T_o = kNoiseBound sum_{j >= o} |amp_j|: the total, then less one octave at a
     // time (rounding far below the margin)
     float tot = 0.0f, a = 1.0f;
     for (int o = 0; o < oct; ++o, a = a * gain) tot += fabsf(a) * kNoiseBound;
