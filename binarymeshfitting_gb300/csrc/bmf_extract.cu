@@ -183,12 +183,15 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
   const int lane = threadIdx.x & 31;
   const bool listing = ws.clist != nullptr;
   const bool xin = x + 1 < dim;  // line x + 1 exists (cells and x-crossings of this plane)
+  // a word's y is its index times the rounded-up 2^32 / zc, high half: exact
+  // while index * zc < 2^32
+  const uint64_t zmagic = ((1ull << 32) + (uint64_t)zc - 1u) / (uint64_t)zc;
   for (int base = 0; base < nw; base += kCountThreads) {
     const int wi = base + threadIdx.x;
+    const int y = (int)(((uint64_t)(uint32_t)wi * zmagic) >> 32), zb = wi - y * zc;
     uint32_t vc = 0u, ic = 0u, p0 = 0u, p1 = 0u, p2 = 0u, act = 0u;
     uint32_t f00 = 0u, f10 = 0u, f01 = 0u, fnx = 0u;  // band fill: samples to make exact
     if (wi < nw && cm) {
-      const int y = wi / zc, zb = wi - y * zc;
       const bool yin = y + 1 < dim, nin = zb + 1 < zc;
       const uint32_t* L00 = W + ((int64_t)x * dim + y) * zc + zb;
       const uint32_t w00 = __ldg(L00), n00 = nin ? __ldg(L00 + 1) : 0u;
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         ws.gpl[3 * o + 2] = p2;
       }
     }
-    if (MODE == 0 && ws.exact) {
+    if (MODE == 0 && ws.exact && __any_sync(kFull, (f00 | f10 | f01 | fnx) != 0u)) {
       // one global reservation per warp for the samples to make exact
       const int nf = __popc(f00) + __popc(f10) + __popc(f01) + __popc(fnx);
       int incl = nf;
@@ -271,7 +274,6 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         fbase = __shfl_sync(kFull, fbase, 31);
         if (nf) {
           int64_t slot = (int64_t)fbase + incl - nf;
-          const int y = wi / zc, zb = wi - y * zc;
           const uint32_t s00 = (uint32_t)((((int64_t)x * dim + y) * dim) + 32 * zb);
           auto put = [&](uint32_t m, uint32_t sbase) {
             for (; m; m &= m - 1u, ++slot)
@@ -284,7 +286,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         }
       }
     }
-    if (listing) {
+    if (listing && __any_sync(kFull, act != 0u)) {
       // one global reservation per warp; Mode R lists busy words, Mode Q
       // each word's active cells in bit order
       const int na = MODE == 0 ? (act != 0u ? 1 : 0) : __popc(act);
@@ -303,7 +305,6 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         if (MODE == 0) {
           if (slot < ws.clist_cap) ws.clist[slot] = make_uint2((uint32_t)c, (uint32_t)(x * nw + wi));
         } else {
-          const int y = wi / zc, zb = wi - y * zc;
           const uint32_t key0 = vertex_key(x, y, 32 * zb, 0);  // the cell as a vertex key (k = 0)
           for (uint32_t m = act; m; m &= m - 1u, ++slot)
             if (slot < ws.clist_cap)
