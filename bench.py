@@ -44,9 +44,9 @@ OPS_PER_LAYER = 20          # 4 corners (mul + fma), alpha and beta (3 lerps of 
 # count by samples, the emit, scan and sweeps by output indices.
 DRAM_UPDATE_SAMPLES = 1_785_478_272
 DRAM_UPDATE_INDICES = 167_847_141
-DRAM_BYTES = {"fill": 415.3e6 + 1405.9e6 + 9.0e6 + 3.8e6,     # k_fill_terrain<16, band> + k_fill_fixup
-              "count": 331.1e6 + 1458.8e6, "scan": 590.5e6 + 531.0e6, "emit": 1774.8e6 + 2410.4e6,
-              "sweeps": 12763.1e6 + 8367.6e6}
+DRAM_BYTES = {"fill": 390.4e6 + 1312.7e6 + 19.9e6 + 10.4e6,   # k_fill_terrain<16, band> + k_fill_fixup
+              "count": 331.0e6 + 1462.8e6, "scan": 590.6e6 + 530.9e6, "emit": 1858.0e6 + 2279.9e6,
+              "sweeps": 12626.5e6 + 8305.1e6}
 
 
 def fill_fp32_ops(rows, params):
@@ -247,7 +247,8 @@ def config(args):
             "topology": "mode R (reference Marching-Cubes triangles)" if args.mode == "R" else
             "mode Q (DMC quads, placement %d)" % args.placement,
             "smoothing_iters": args.iters, "smoothed_normals": not args.no_normals,
-            "l2": "inputs larger than L2: 7.1 GB density written per step", "parallelism": "replicas" if
+            "l2": "working set larger than L2: each step moves about 30 GB through DRAM (ncu), no flush "
+                  "between steps", "parallelism": "replicas" if
             args.gpus == 1 else "weak: one independent update per GPU"}
 
 

@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
   // a word's y is its index times the rounded-up 2^32 / zc, high half: exact
   // while index * zc < 2^32
   const uint64_t zmagic = ((1ull << 32) + (uint64_t)zc - 1u) / (uint64_t)zc;
+  const uint32_t* Wx = W + (int64_t)x * nw;  // the plane's words
   for (int base = 0; base < nw; base += kCountThreads) {
     const int wi = base + threadIdx.x;
     const int y = (int)(((uint64_t)(uint32_t)wi * zmagic) >> 32), zb = wi - y * zc;
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
     uint32_t f00 = 0u, f10 = 0u, f01 = 0u, fnx = 0u;  // band fill: samples to make exact
     if (wi < nw && cm) {
       const bool yin = y + 1 < dim, nin = zb + 1 < zc;
-      const uint32_t* L00 = W + ((int64_t)x * dim + y) * zc + zb;
+      const uint32_t* L00 = Wx + wi;  // the word (x, y, zb)
       const uint32_t w00 = __ldg(L00), n00 = nin ? __ldg(L00 + 1) : 0u;
       const uint32_t w01 = yin ? __ldg(L00 + zc) : 0u, n01 = (yin && nin) ? __ldg(L00 + zc + 1) : 0u;
       const uint32_t* L10 = L00 + (int64_t)dim * zc;
