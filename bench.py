@@ -542,7 +542,10 @@ def run_gb300(args):
                 "dram_achieved": dram["sweeps"] / (st_ms[5] / 1000.0) / 1e9,
                 "dram_frac": dram["sweeps"] / (st_ms[5] / 1000.0) / 1e9 / hbm_peak,
                 "ms_per_launch": st_ms[5],
-                "fill": {"kernels": ("k_sample_label (x-plane CTAs; one height evaluation per (x, z) column)"
+                "fill": {"kernels": ("k_columns2d (one thread per (x, z) column height) + k_sample_label "
+                                     "(occupancy words from the heights) + k_fill_fixup (densities at the ends of "
+                                     "crossings only)" if args.field == "2d" and args.mode == "R" else
+                                     "k_sample_label (x-plane CTAs; one height evaluation per (x, z) column)"
                                      if args.field == "2d" else
                                      "k_fill_terrain<16, band> + k_fill_fixup (terrain FBM, occupancy words, exact "
                                      "densities at the ends of crossings)" if args.mode == "R" else
@@ -550,7 +553,7 @@ def run_gb300(args):
                          "ms": st_ms[0], "samples_per_s": samples / (st_ms[0] / 1000.0),
                          "dram_bytes": dram["fill"] if (args.mode == "R" and args.field == "fbm") else None,
                          "density_write_gbs": (4 * samples + 4 * words) / (st_ms[0] / 1000.0) / 1e9
-                         if args.field == "2d" else None,
+                         if args.field == "2d" and args.mode != "R" else None,
                          "full_fill_fp32_ops": fill_ops, "full_fill_fp32_ops_per_sample": fill_ops / samples,
                          "full_fill_equivalent_tops": fill_ops / (st_ms[0] / 1000.0) / 1e12,
                          "full_fill_equivalent_frac": fill_ops / (st_ms[0] / 1000.0) / 1e12 / fp32_peak,

@@ -93,6 +93,10 @@ struct bmf_batch {
   // them; d_exact is its per-sample exactness mask (words layout)
   int fill_band = 0;
   uint32_t* d_exact = nullptr;
+  // the 2D heightmap's band form (the column fill): the fill stores each
+  // (x, z) column height (words layout: chunk.words + x * dim + z) and the
+  // occupancy words, no densities; the fix-up computes the crossing ends'
+  float* d_cols = nullptr;
   uint2* d_fix = nullptr;  // samples to make exact (+ counter), sized 2 vcap + 1
   int64_t fix_cap = 0;
   // Mode R work list, sized by the output capacity (vcap + icap / 3 + 1)
@@ -621,11 +625,35 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
     }
     b->fill_grid = fill_terrain_resident_ctas(b->fill_run, (int)b->field.p[5], b->fill_band != 0);
   }
+  if (b->field.kind == BMF_FIELD_TERRAIN_2D && b->opts.mode == BMF_MODE_R && fill_band_supported(b->field)) {
+    // column items {chunk, first column}, largest chunks first
+    std::vector<int2> items;
+    const int per = columns2d_item();
+    for (int i : order) {
+      const int nc = b->h_chunks[i].dim * b->h_chunks[i].dim;
+      for (int k = 0; k < nc; k += per) items.push_back(make_int2(i, k));
+    }
+    b->n_fill_items = (int)items.size();
+    if ((s = bail(cudaMalloc(&b->d_fill_items, sizeof(int2) * items.size()), "column items")) != BMF_OK) return s;
+    if ((s = bail(cudaMemcpy(b->d_fill_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice),
+                  "upload column items")) != BMF_OK)
+      return s;
+    if ((s = bail(cudaMalloc(&b->d_cols, sizeof(float) * words), "column heights")) != BMF_OK) return s;
+    b->fill_band = 1;
+  }
   *out = b;
   return BMF_OK;
 }
 
 namespace {
+
+// The band form of the fill is on: the terrain FBM's band fill, or the 2D
+// heightmap's column fill.
+bool batch_band(const bmf_batch* b) {
+  if (!b->fill_band) return false;
+  if (b->field.kind == BMF_FIELD_TERRAIN_FBM) return b->d_exact && b->fill_mode != 0;
+  return b->field.kind == BMF_FIELD_TERRAIN_2D && b->d_cols;
+}
 
 // The work list of active cells for an output arena of (vcap, icap) (+ its counter).
 bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
@@ -640,7 +668,7 @@ bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   b->ws.clist = b->d_clist;
   b->ws.ccount = (uint32_t*)(b->d_clist + b->clist_cap);
   b->ws.clist_cap = b->clist_cap;
-  if (b->d_exact) {
+  if (b->d_exact || b->d_cols) {
     // band fill: every crossing (one vertex each in Mode R) lists at most its two ends
     const int64_t fcap = 2 * vcap + 1;
     if (fcap > b->fix_cap) {
@@ -654,8 +682,9 @@ bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
     b->ws.fcount = (uint32_t*)(b->d_fix + b->fix_cap);
     b->ws.fix_cap = b->fix_cap;
   }
-  const bool band = b->fill_band && b->d_exact && b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0;
-  b->ws.exact = band ? b->d_exact : nullptr;
+  const bool band = batch_band(b);
+  b->ws.exact = band && b->field.kind == BMF_FIELD_TERRAIN_FBM ? b->d_exact : nullptr;
+  b->ws.all_inexact = band && b->field.kind == BMF_FIELD_TERRAIN_2D ? 1 : 0;
   return BMF_OK;
 }
 
@@ -665,16 +694,22 @@ bool batch_keys(const bmf_batch* b) {
 }
 
 // Density fill + occupancy words of a whole update.
-bool batch_band(const bmf_batch* b) {
-  return b->fill_band && b->d_exact && b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0;
-}
 
 void batch_fill(bmf_batch* b, cudaStream_t st) {
   if (b->field.kind == BMF_FIELD_TERRAIN_FBM && b->fill_mode != 0)
     launch_fill_terrain(b->fill_run, b->d_chunks, b->d_fill_items, b->n_fill_items,
                         b->fill_mode == 2 ? b->d_queue : nullptr, b->fill_grid, b->field, b->d_dens, b->d_words,
                         b->d_flags, batch_band(b) ? b->d_exact : nullptr, st);
-  else
+  else if (b->d_cols) {
+    // the 2D heightmap: every column height once, then the words (and, with
+    // the column fill off, every density) from them
+    launch_columns2d(b->d_chunks, b->d_fill_items, b->n_fill_items, b->field, b->d_cols, st);
+    if (batch_band(b))
+      launch_words2d(b->d_chunks, b->n, b->d_units, b->n_units, b->field, b->d_cols, b->d_words, b->d_flags, st);
+    else
+      launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
+                          b->d_words, b->d_flags, st, b->d_cols);
+  } else
     launch_sample_label(b->d_chunks, b->n, b->d_units, b->n_units, b->max_dim, b->field, nullptr, b->d_dens,
                         b->d_words, b->d_flags, st);
 }
@@ -725,13 +760,13 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   batch_fill(b, st);
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   const bool band = batch_band(b);
-  if (band) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st);
+  if (band) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st, b->d_cols);
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
              out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, batch_keys(b) ? b->d_vkey : nullptr};
-  int64_t k = (band ? 5 : 4) + launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units,
+  int64_t k = (band ? 5 : 4) + (b->d_cols ? 1 : 0) + launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units,
                               b->d_words, b->d_dens, b->d_flags, b->ws, mo, b->d_totals, st);
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
@@ -882,7 +917,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[2], st));
   // the band fill's exact-density fix-up belongs to the fill stage
-  if (batch_band(b)) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st);
+  if (batch_band(b)) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st, b->d_cols);
   BMF_CUDA(ctx, cudaEventRecord(ev[7], st));
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   BMF_CUDA(ctx, cudaEventRecord(ev[3], st));
@@ -913,7 +948,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[2], ev[7], ev[3]));
   for (int k = 3; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
-  ctx->launches += (batch_band(b) ? 5 : 4) + ek + pk;
+  ctx->launches += (batch_band(b) ? 5 : 4) + (b->d_cols ? 1 : 0) + ek + pk;
   return BMF_OK;
 }
 
@@ -950,10 +985,10 @@ bmf_status bmf_batch_set_tuning(bmf_batch* b, const bmf_batch_tuning* t) {
   if (t->fill_mode < 0 || t->fill_mode > 2 || (!terrain && t->fill_mode != 0) ||
       (t->fill_run != 4 && t->fill_run != 8 && t->fill_run != 16) ||
       (t->sweep_block != 128 && t->sweep_block != 256 && t->sweep_block != 512) ||
-      (t->fill_band != 0 && t->fill_band != 1) || (t->fill_band && !b->d_exact))
+      (t->fill_band != 0 && t->fill_band != 1) || (t->fill_band && !b->d_exact && !b->d_cols))
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT,
                 "bmf_batch_set_tuning: fill_mode 0..2 (1, 2 for terrain fields only), fill_run 4/8/16, "
-                "sweep_block 128/256/512, fill_band 0/1 (1 for Mode R terrain plans only)");
+                "sweep_block 128/256/512, fill_band 0/1 (1 for Mode R terrain and 2D heightmap plans only)");
   b->fill_mode = t->fill_mode;
   if (t->fill_run != b->fill_run || t->fill_band != b->fill_band) {
     b->fill_run = t->fill_run;
@@ -1292,7 +1327,8 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   void* ptrs[] = {b->d_chunks, b->d_units, b->d_flags, b->d_tot, b->d_totals, b->d_dens, b->d_words,
                   b->ws.vcnt, b->ws.icnt, b->ws.gpl, b->ps.off, b->ps.cursor, b->ps.adj, b->ps.dual_p,
                   b->ps.dual_n, b->ps.tmp, b->d_idxg, b->d_valence, b->d_boundary, b->d_vkey,
-                  b->d_fill_items, b->d_queue, b->d_order, b->d_pqueue, b->d_clist, b->d_exact, b->d_fix};
+                  b->d_fill_items, b->d_queue, b->d_order, b->d_pqueue, b->d_clist, b->d_exact, b->d_fix,
+                  b->d_cols};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);

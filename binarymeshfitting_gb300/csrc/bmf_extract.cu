@@ -227,15 +227,16 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         vc = __popc(X) + __popc(Y) + __popc(Z);
         ic = 3u * t;
         act = p0 | p1 | p2 | X | Y | Z;
-        if (ws.exact && (X | Y | Z)) {
+        if ((ws.exact || ws.all_inexact) && (X | Y | Z)) {
           // the band fill's inexact samples at the ends of this word's crossings:
           // own samples (X, Y, Z starts, Z ends), line x + 1 (X), line y + 1 (Y),
-          // and bit 0 of the next word (the end of a crossing from bit 31)
-          const uint32_t* E = ws.exact + ch.words + ((int64_t)x * dim + y) * zc + zb;
-          f00 = (X | Y | Z | (Z << 1)) & ~__ldg(E);
-          f10 = X ? (X & ~__ldg(E + (int64_t)dim * zc)) : 0u;
-          f01 = Y ? (Y & ~__ldg(E + zc)) : 0u;
-          fnx = (Z >> 31) ? (~__ldg(E + 1) & 1u) : 0u;
+          // and bit 0 of the next word (the end of a crossing from bit 31); with
+          // all_inexact every one of them
+          const uint32_t* E = ws.exact ? ws.exact + ch.words + ((int64_t)x * dim + y) * zc + zb : nullptr;
+          f00 = (X | Y | Z | (Z << 1)) & (E ? ~__ldg(E) : kFull);
+          f10 = X ? (X & (E ? ~__ldg(E + (int64_t)dim * zc) : kFull)) : 0u;
+          f01 = Y ? (Y & (E ? ~__ldg(E + zc) : kFull)) : 0u;
+          fnx = (Z >> 31) ? ((E ? ~__ldg(E + 1) : kFull) & 1u) : 0u;
         }
       } else {
         // interior quad edges: the four cells around the edge exist
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         ws.gpl[3 * o + 2] = p2;
       }
     }
-    if (MODE == 0 && ws.exact && __any_sync(kFull, (f00 | f10 | f01 | fnx) != 0u)) {
+    if (MODE == 0 && (ws.exact || ws.all_inexact) && __any_sync(kFull, (f00 | f10 | f01 | fnx) != 0u)) {
       // one global reservation per warp for the samples to make exact
       const int nf = __popc(f00) + __popc(f10) + __popc(f01) + __popc(fnx);
       int incl = nf;

@@ -70,18 +70,33 @@ struct WordScratch {
   // as {chunk, sample index in the chunk}; *fcount (zeroed before the count
   // kernel) entries, at most fix_cap kept.  A crossing has two ends, so the
   // list holds at most twice the vertex count (2 vcap + 1 suffices).
+  // all_inexact (the 2D heightmap's column fill, which stores no densities):
+  // every sample counts as inexact, with no mask.
   const uint32_t* exact = nullptr;
   uint2* fix = nullptr;
   uint32_t* fcount = nullptr;
   int64_t fix_cap = 0;
+  int all_inexact = 0;
 };
 
 // Fill + label.  A terrain field of a single chunk goes through the line
 // kernel (k_fill_terrain) directly; batches pass their own item queue to
 // launch_fill_terrain.
+// cols (nullable, BMF_FIELD_TERRAIN_2D): the (x, z) column heights from
+// launch_columns2d, stored at chunk.words + x * dim + z (a chunk's dim^2
+// columns fit its words' span); without it the x-plane CTAs evaluate them.
 void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units, int max_dim,
                          const FieldDev& field, const float* dens_in, float* dens_out, uint32_t* words,
-                         uint32_t* flags, cudaStream_t st);
+                         uint32_t* flags, cudaStream_t st, const float* cols = nullptr);
+// The 2D heightmap's column heights of a batch into cols (layout above), over
+// items {chunk, first column} of columns2d_item() columns each.
+void launch_columns2d(const ChunkDev* d_chunks, const int2* d_items, int n_items, const FieldDev& field, float* cols,
+                      cudaStream_t st);
+int columns2d_item();
+// The 2D heightmap's occupancy words and contains_mesh flags from the column
+// heights alone (the column fill: no densities).
+void launch_words2d(const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
+                    const FieldDev& field, const float* cols, uint32_t* words, uint32_t* flags, cudaStream_t st);
 // Terrain FBM fill over line items {chunk, first line} (kFillLines lines
 // each; d_items null = chunk 0's items in order).  d_queue non-null: grid
 // persistent CTAs take items from the queue (reset here); else one CTA per item.
@@ -91,7 +106,9 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
 void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items, int n_items, int* d_queue,
                          int grid, const FieldDev& field, float* dens_out, uint32_t* words, uint32_t* flags,
                          uint32_t* exact, cudaStream_t st);
-// the band fill applies to fields of the form (py - h) - a * FBM with a > 0
+// the band fill applies to fields of the form (py - h) - a * FBM with a > 0,
+// and (as the column fill: words and column heights, no densities) to the 2D
+// heightmap
 bool fill_band_supported(const FieldDev& field);
 // The batched-fitting loss (sum over chunks of the mean squared sphere-union
 // distance of the chunk's vertices) into *loss and its position gradient into
@@ -103,9 +120,10 @@ int launch_fit_loss_spheres(const ChunkDev* d_chunks, int n_chunks, const uint32
 int launch_adam(float* p, const float* g, float* m, float* v, int64_t n, int* step, float lr, float b1, float b2,
                 float eps, cudaStream_t st);
 // exact densities for the samples the count kernel listed in ws.fix (the
-// inexact ends of crossings; after launch_count, before launch_emit)
+// inexact ends of crossings; after launch_count, before launch_emit); cols:
+// the 2D heightmap's column heights (launch_sample_label), else null
 void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, float* dens,
-                       cudaStream_t st);
+                       cudaStream_t st, const float* cols = nullptr);
 int fill_terrain_items(int dim);          // items of one chunk
 int fill_terrain_lines();                 // lines per item
 int fill_terrain_resident_ctas(int run, int octaves, bool band);  // persistent grid: SMs x resident CTAs per SM

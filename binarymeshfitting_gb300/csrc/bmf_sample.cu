@@ -23,6 +23,7 @@ __device__ __forceinline__ int find_chunk(const int* __restrict__ unit_start, in
 }
 
 constexpr int kMaxColumn = 1024;  // samples per axis (kMaxDim)
+constexpr int kColumnItem = 256;  // columns per k_columns2d CTA
 
 // flags bits: 1 = a word that is neither empty nor full, 2 = a full word,
 // 4 = an empty word.  contains_mesh = (f & 1) || ((f & 6) == 6), the
@@ -30,11 +31,14 @@ constexpr int kMaxColumn = 1024;  // samples per axis (kMaxDim)
 __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict__ chunks, int n_chunks,
                                                       const int* __restrict__ unit_start, FieldDev field,
                                                       const float* __restrict__ dens_in, float* __restrict__ dens_out,
-                                                      uint32_t* __restrict__ words, uint32_t* __restrict__ flags) {
+                                                      uint32_t* __restrict__ words, uint32_t* __restrict__ flags,
+                                                      const float* __restrict__ cols) {
   extern __shared__ uint32_t sw[];
   __shared__ int perm2[512];
   __shared__ float4 gtab[512];
-  __shared__ float s_col[kMaxColumn];  // BMF_FIELD_TERRAIN_2D: the height noise of the plane's (x, z) columns
+  // BMF_FIELD_TERRAIN_2D: the height noise of the plane's (x, z) columns,
+  // evaluated here or (cols non-null) read from k_columns2d's output
+  __shared__ float s_col[kMaxColumn];
   const int u = blockIdx.x;
   const int c = find_chunk(unit_start, n_chunks, u);
   const ChunkDev ch = chunks[c];
@@ -53,7 +57,8 @@ __global__ void __launch_bounds__(256) k_sample_label(const ChunkDev* __restrict
   if (col2d) {  // one height evaluation per column, shared by the plane's dim samples of it
     const float pxc = ch.ox + (float)x * ch.scale;
     for (int z = threadIdx.x; z < dim; z += blockDim.x)
-      s_col[z] = terrain2d_height(field, perm2, pxc, ch.oz + (float)z * ch.scale);
+      s_col[z] = cols ? __ldg(cols + ch.words + (int64_t)x * dim + z)
+                      : terrain2d_height(field, perm2, pxc, ch.oz + (float)z * ch.scale);
     __syncthreads();
   }
 
@@ -563,7 +568,7 @@ void launch_fill_terrain(int run, const ChunkDev* d_chunks, const int2* d_items,
 }
 
 bool fill_band_supported(const FieldDev& field) {
-  return field.kind == BMF_FIELD_TERRAIN_FBM && field.p[1] > 0.0f;
+  return (field.kind == BMF_FIELD_TERRAIN_FBM && field.p[1] > 0.0f) || field.kind == BMF_FIELD_TERRAIN_2D;
 }
 
 // ---------------------------------------------------------------------------
@@ -599,9 +604,11 @@ __device__ float terrain_exact(const FieldDev& f, const int* __restrict__ perm2,
   return __fmaf_rn(-ampl, sum, py - h0);
 }
 
+// The 2D heightmap's column fill stores no densities: the listed samples
+// take theirs from the stored column height, with the fill's operations.
 __global__ void __launch_bounds__(256) k_fill_fixup(const ChunkDev* __restrict__ chunks, const uint2* __restrict__ list,
                                                     const uint32_t* __restrict__ count, int64_t cap, FieldDev field,
-                                                    float* __restrict__ dens) {
+                                                    float* __restrict__ dens, const float* __restrict__ cols) {
   __shared__ int perm2[512];
   __shared__ float4 gtab[512];
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
@@ -615,12 +622,17 @@ __global__ void __launch_bounds__(256) k_fill_fixup(const ChunkDev* __restrict__
     const ChunkDev ch = chunks[ent.x];
     const uint32_t dim = (uint32_t)ch.dim, line = ent.y / dim;
     const int z = (int)(ent.y - line * dim), x = (int)(line / dim), y = (int)(line - (uint32_t)x * dim);
-    dens[ch.dens + (int64_t)ent.y] = terrain_exact(field, perm2, gtab, ch, x, y, z);
+    if (cols) {
+      const float py = ch.oy + (float)y * ch.scale;
+      dens[ch.dens + (int64_t)ent.y] = terrain2d_density(field, py, __ldg(cols + ch.words + (int64_t)x * dim + z));
+    } else {
+      dens[ch.dens + (int64_t)ent.y] = terrain_exact(field, perm2, gtab, ch, x, y, z);
+    }
   }
 }
 
 void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, float* dens,
-                       cudaStream_t st) {
+                       cudaStream_t st, const float* cols) {
   static std::atomic<int> grid[64] = {};
   const int g = per_device_once(grid, [](int dev) {
     int sms = 0, per_sm = 0;
@@ -628,7 +640,7 @@ void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const Fi
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_fixup, 256, 0);
     return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   });
-  k_fill_fixup<<<g, 256, 0, st>>>(d_chunks, ws.fix, ws.fcount, ws.fix_cap, field, dens);
+  k_fill_fixup<<<g, 256, 0, st>>>(d_chunks, ws.fix, ws.fcount, ws.fix_cap, field, dens, cols);
 }
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
@@ -689,9 +701,103 @@ void launch_word_flags(const ChunkDev* d_chunks, int n_chunks, const uint32_t* w
   k_word_flags<<<n_chunks, 256, 0, st>>>(d_chunks, words, flags);
 }
 
+// The 2D heightmap's (x, z) column heights of a batch, one thread per column
+// over items of kColumnItem consecutive columns of one chunk ({chunk, first
+// column}, column = x * dim + z), stored at chunk.words + column: every
+// column is evaluated once, by a full CTA, instead of by the dim threads of
+// an x-plane's CTA while the rest wait.
+__global__ void __launch_bounds__(kColumnItem) k_columns2d(const ChunkDev* __restrict__ chunks,
+                                                         const int2* __restrict__ items, FieldDev field,
+                                                         float* __restrict__ cols) {
+  __shared__ int perm2[512];
+  for (int i = threadIdx.x; i < 512; i += blockDim.x) perm2[i] = field.perm[i & 255];
+  __syncthreads();
+  const int2 it = items[blockIdx.x];
+  const ChunkDev& ch = chunks[it.x];
+  const int dim = ch.dim, col = it.y + (int)threadIdx.x;
+  if (col >= dim * dim) return;
+  const int x = col / dim, z = col - x * dim;
+  const float pxc = ch.ox + (float)x * ch.scale;
+  cols[ch.words + (int64_t)col] = terrain2d_height(field, perm2, pxc, ch.oz + (float)z * ch.scale);
+}
+
+void launch_columns2d(const ChunkDev* d_chunks, const int2* d_items, int n_items, const FieldDev& field, float* cols,
+                      cudaStream_t st) {
+  if (n_items > 0) k_columns2d<<<n_items, kColumnItem, 0, st>>>(d_chunks, d_items, field, cols);
+}
+int columns2d_item() { return kColumnItem; }
+
+// The 2D heightmap's occupancy words from its column heights, no densities
+// (the column fill).  One warp per x-plane at a time (persistent; a warp's
+// planes ascend, so it finds each plane's chunk by searching forward from
+// the previous one, 32 candidates a step).  Per block zb a lane holds the
+// height of column z = 32 zb + lane; per line y every lane evaluates its
+// sample's density sign with the full fill's operations and a ballot forms
+// the word, which lane y % 32 keeps, so each lane stores one word per 32 lines.
+__global__ void __launch_bounds__(256) k_words2d(const ChunkDev* __restrict__ chunks, int n_chunks,
+                                                 const int* __restrict__ unit_start, int n_units, FieldDev field,
+                                                 const float* __restrict__ cols, uint32_t* __restrict__ words,
+                                                 uint32_t* __restrict__ flags) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  int c = 0;
+  for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n_units; u += nwarps) {
+    for (;;) {
+      const int cand = c + 1 + lane;
+      const uint32_t le = __ballot_sync(kFull, cand < n_chunks && __ldg(unit_start + cand) <= u);
+      c += __popc(le);  // unit_start increases, so le is a prefix of the lanes
+      if (le != kFull) break;
+    }
+    const ChunkDev& ch = chunks[c];
+    const int x = u - __ldg(unit_start + c), dim = ch.dim, zc = ch.zc;
+    const float oy = ch.oy, scale = ch.scale;
+    const float* colx = cols + ch.words + (int64_t)x * dim;
+    uint32_t* wx = words + ch.words + (int64_t)x * dim * zc;
+    uint32_t f = 0u;
+    for (int zb = 0; zb < zc; ++zb) {
+      const int z = 32 * zb + lane;
+      const bool zin = z < dim;
+      const float n = zin ? __ldg(colx + z) : 0.0f;
+      for (int yb = 0; yb < dim; yb += 32) {
+        uint32_t mine = 0u;
+        const int ny = min(32, dim - yb);
+        for (int j = 0; j < ny; ++j) {
+          const float py = oy + (float)(yb + j) * scale;
+          const uint32_t w = __ballot_sync(kFull, zin && terrain2d_density(field, py, n) < 0.0f);
+          if (lane == j) mine = w;
+        }
+        if (lane < ny) {
+          wx[(int64_t)(yb + lane) * zc + zb] = mine;
+          f |= (mine != 0u && mine != kFull) ? 1u : (mine == kFull ? 2u : 4u);
+        }
+      }
+    }
+    f |= __shfl_xor_sync(kFull, f, 16);
+    f |= __shfl_xor_sync(kFull, f, 8);
+    f |= __shfl_xor_sync(kFull, f, 4);
+    f |= __shfl_xor_sync(kFull, f, 2);
+    f |= __shfl_xor_sync(kFull, f, 1);
+    if (lane == 0 && f) atomicOr(flags + c, f);
+  }
+}
+
+void launch_words2d(const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units,
+                    const FieldDev& field, const float* cols, uint32_t* words, uint32_t* flags, cudaStream_t st) {
+  static std::atomic<int> grid[64] = {};
+  const int g = per_device_once(grid, [](int dev) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_words2d, 256, 0);
+    return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  });
+  const int need = (n_units + 7) / 8;  // eight warps per CTA, one plane each at a time
+  if (need > 0) k_words2d<<<min(g, need), 256, 0, st>>>(d_chunks, n_chunks, d_unit_start, n_units, field, cols, words,
+                                                       flags);
+}
+
 void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_unit_start, int n_units, int max_dim,
                          const FieldDev& field, const float* dens_in, float* dens_out, uint32_t* words,
-                         uint32_t* flags, cudaStream_t st) {
+                         uint32_t* flags, cudaStream_t st, const float* cols) {
   if (field.kind == BMF_FIELD_TERRAIN_FBM && n_chunks == 1) {
     launch_fill_terrain(16, d_chunks, nullptr, fill_terrain_items(max_dim), nullptr, 0, field, dens_out, words, flags,
                         nullptr, st);
@@ -700,7 +806,7 @@ void launch_sample_label(const ChunkDev* d_chunks, int n_chunks, const int* d_un
   const int max_zc = (max_dim + 31) / 32;
   const size_t smem = (size_t)max_dim * max_zc * sizeof(uint32_t);
   k_sample_label<<<n_units, 256, smem, st>>>(d_chunks, n_chunks, d_unit_start, field, dens_in, dens_out, words,
-                                             flags);
+                                             flags, field.kind == BMF_FIELD_TERRAIN_2D ? cols : nullptr);
 }
 
 void launch_cell_masks(int dim, const uint32_t* W, uint8_t* masks, cudaStream_t st) {

@@ -221,3 +221,33 @@ def test_terrain2d_update_matches_oracle(ctx, mode, placement):
     assert compare_update(b, rows, mode, placement, 4, False, True, L.FIELD_TERRAIN_2D,
                           workloads.TERRAIN_2D_PARAMS) >= 20
     b.close()
+
+
+def test_terrain2d_column_fill_matches_full_fill(ctx):
+    """The 2D heightmap's band form -- the column fill: occupancy words and
+    (x, z) column heights only, densities at the ends of crossings computed
+    from the stored heights by the fix-up -- gives an arena bit-identical to
+    the full fill's, with and without graph replay."""
+    import torch
+    descs, rows = workloads.lod_update(n=160, seed=23)
+    for dsc, r in zip(descs, rows):
+        dsc.dim = min(dsc.dim, 65)
+        dsc.origin[1] = float(r[1]) - 128.0
+    b = Batch(ctx, descs, workloads.terrain2d_field(), mode=L.MODE_R, iters=4, smooth_normals=True)
+    assert b.tuning()["fill_band"] == 1
+    run_sized(b, True)
+    bufs = b.bufs
+    b.set_tuning(fill_band=0)
+    nv, ni = b.run(use_graph=False)
+    assert nv > 0
+    ref = {k: bufs[k][:n].clone() for k, n in (("pos", nv), ("nrm", nv), ("idx", ni), ("boundary", nv))}
+    ref["info"] = bufs["info"].clone()
+    b.set_tuning(fill_band=1)
+    for use_graph in (False, True):
+        assert b.run(use_graph=use_graph) == (nv, ni)
+        for k, r in ref.items():
+            g = bufs[k][:r.shape[0]]
+            if r.is_floating_point():
+                r, g = r.view(torch.int32), g.view(torch.int32)
+            assert torch.equal(r, g), (k, use_graph)
+    b.close()
