@@ -95,7 +95,9 @@ struct bmf_batch {
   uint32_t* d_exact = nullptr;
   // the 2D heightmap's band form (the column fill): the fill stores each
   // (x, z) column height (words layout: chunk.words + x * dim + z) and the
-  // occupancy words, no densities; the fix-up computes the crossing ends'
+  // occupancy words, no densities; the emit computes a crossing end's
+  // density from its column height.  With the band off, the fill still
+  // evaluates the heights here once and writes every density from them.
   float* d_cols = nullptr;
   uint2* d_fix = nullptr;  // samples to make exact (+ counter), sized 2 vcap + 1
   int64_t fix_cap = 0;
@@ -668,7 +670,7 @@ bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   b->ws.clist = b->d_clist;
   b->ws.ccount = (uint32_t*)(b->d_clist + b->clist_cap);
   b->ws.clist_cap = b->clist_cap;
-  if (b->d_exact || b->d_cols) {
+  if (b->d_exact) {
     // band fill: every crossing (one vertex each in Mode R) lists at most its two ends
     const int64_t fcap = 2 * vcap + 1;
     if (fcap > b->fix_cap) {
@@ -684,7 +686,10 @@ bmf_status batch_list_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
   }
   const bool band = batch_band(b);
   b->ws.exact = band && b->field.kind == BMF_FIELD_TERRAIN_FBM ? b->d_exact : nullptr;
-  b->ws.all_inexact = band && b->field.kind == BMF_FIELD_TERRAIN_2D ? 1 : 0;
+  const bool col2d = band && b->field.kind == BMF_FIELD_TERRAIN_2D;
+  b->ws.cols2d = col2d ? b->d_cols : nullptr;
+  b->ws.c2d_g = b->field.p[0];
+  b->ws.c2d_height = b->field.p[1];
   return BMF_OK;
 }
 
@@ -759,8 +764,8 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
   BMF_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n, st));
   batch_fill(b, st);
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
-  const bool band = batch_band(b);
-  if (band) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st, b->d_cols);
+  const bool band = batch_band(b) && b->field.kind == BMF_FIELD_TERRAIN_FBM;  // the 2D column fill needs no fix-up
+  if (band) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st);
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   launch_chunk_offsets(b->d_chunks, b->n, b->d_tot, b->d_flags, out->vcap, out->icap, out->d_chunk_info,
                        b->d_totals, st);
@@ -917,7 +922,8 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   launch_count(b->opts.mode, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_flags, b->ws, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[2], st));
   // the band fill's exact-density fix-up belongs to the fill stage
-  if (batch_band(b)) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st, b->d_cols);
+  const bool fixup = batch_band(b) && b->field.kind == BMF_FIELD_TERRAIN_FBM;
+  if (fixup) launch_fill_fixup(b->d_chunks, b->ws, b->field, b->d_dens, st);
   BMF_CUDA(ctx, cudaEventRecord(ev[7], st));
   launch_scan_chunks(b->d_chunks, b->n, b->ws, b->d_tot, st, b->d_order);
   BMF_CUDA(ctx, cudaEventRecord(ev[3], st));
@@ -948,7 +954,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
   BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[2], ev[7], ev[3]));
   for (int k = 3; k < 6; ++k) BMF_CUDA(ctx, cudaEventElapsedTime(&h_stage_ms[k], ev[k], ev[k + 1]));
   for (auto& e : ev) cudaEventDestroy(e);
-  ctx->launches += (batch_band(b) ? 5 : 4) + (b->d_cols ? 1 : 0) + ek + pk;
+  ctx->launches += (fixup ? 5 : 4) + (b->d_cols ? 1 : 0) + ek + pk;
   return BMF_OK;
 }
 

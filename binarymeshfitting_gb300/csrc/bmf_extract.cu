@@ -227,16 +227,15 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         vc = __popc(X) + __popc(Y) + __popc(Z);
         ic = 3u * t;
         act = p0 | p1 | p2 | X | Y | Z;
-        if ((ws.exact || ws.all_inexact) && (X | Y | Z)) {
+        if (ws.exact && (X | Y | Z)) {
           // the band fill's inexact samples at the ends of this word's crossings:
           // own samples (X, Y, Z starts, Z ends), line x + 1 (X), line y + 1 (Y),
-          // and bit 0 of the next word (the end of a crossing from bit 31); with
-          // all_inexact every one of them
-          const uint32_t* E = ws.exact ? ws.exact + ch.words + ((int64_t)x * dim + y) * zc + zb : nullptr;
-          f00 = (X | Y | Z | (Z << 1)) & (E ? ~__ldg(E) : kFull);
-          f10 = X ? (X & (E ? ~__ldg(E + (int64_t)dim * zc) : kFull)) : 0u;
-          f01 = Y ? (Y & (E ? ~__ldg(E + zc) : kFull)) : 0u;
-          fnx = (Z >> 31) ? ((E ? ~__ldg(E + 1) : kFull) & 1u) : 0u;
+          // and bit 0 of the next word (the end of a crossing from bit 31)
+          const uint32_t* E = ws.exact + ch.words + ((int64_t)x * dim + y) * zc + zb;
+          f00 = (X | Y | Z | (Z << 1)) & ~__ldg(E);
+          f10 = X ? (X & ~__ldg(E + (int64_t)dim * zc)) : 0u;
+          f01 = Y ? (Y & ~__ldg(E + zc)) : 0u;
+          fnx = (Z >> 31) ? (~__ldg(E + 1) & 1u) : 0u;
         }
       } else {
         // interior quad edges: the four cells around the edge exist
@@ -260,7 +259,7 @@ __global__ void __launch_bounds__(kCountThreads) k_count(const ChunkDev* __restr
         ws.gpl[3 * o + 2] = p2;
       }
     }
-    if (MODE == 0 && (ws.exact || ws.all_inexact) && __any_sync(kFull, (f00 | f10 | f01 | fnx) != 0u)) {
+    if (MODE == 0 && ws.exact && __any_sync(kFull, (f00 | f10 | f01 | fnx) != 0u)) {
       // one global reservation per warp for the samples to make exact
       const int nf = __popc(f00) + __popc(f10) + __popc(f01) + __popc(fnx);
       int incl = nf;
@@ -1098,8 +1097,22 @@ struct RTile {
   uint32_t X[kTileWords], Y[kTileWords], Z[kTileWords];
   int x[kTileWords], y[kTileWords], zb[kTileWords], dim[kTileWords], zc[kTileWords];
   int64_t cw[kTileWords], dens[kTileWords], vout[kTileWords], iout[kTileWords];
+  float oy[kTileWords], sc[kTileWords];  // the chunk's y origin and scale (2D column fill)
   int voff[kTileWords + 1], toff[kTileWords + 1];  // exclusive vertex / triangle offsets of the tile's words
 };
+
+// A crossing end's density: read from the fill's densities, or (2D heightmap
+// column fill) computed from the sample's column height with the full fill's
+// operations.
+__device__ __forceinline__ float end_density(const WordScratch& ws, const float* D, int64_t cw, float oy, float sc,
+                                             int dim, int x, int y, int z) {
+  if (ws.cols2d) {
+    const float py = oy + (float)y * sc;
+    const float dy = py * ws.c2d_g;
+    return -dy - __ldg(ws.cols2d + cw + (int64_t)x * dim + z) * ws.c2d_height;
+  }
+  return dens_at(D, dim, x, y, z);
+}
 
 // The tile word holding flattened item j: the last t < nt with off[t] <= j.
 __device__ __forceinline__ int tile_word(const int* off, int nt, int j) {
@@ -1142,6 +1155,8 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
       R.dens[lane] = ch.dens;
       R.vout[lane] = ch.vout;
       R.iout[lane] = ch.iout;
+      R.oy[lane] = ch.oy;
+      R.sc[lane] = ch.scale;
     }
     __syncwarp();
     // 2. stage the neighbourhoods (zeros outside the chunk): one item per
@@ -1245,7 +1260,10 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
       const int dim = R.dim[t], x = R.x[t], y = R.y[t], z = 32 * R.zb[t] + l;
       const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
       const float* D = dens + R.dens[t];
-      const float s0 = dens_at(D, dim, x, y, z), s1 = dens_at(D, dim, x1, y1, z1);
+      const int64_t cw = R.cw[t];
+      const float oy = R.oy[t], sc = R.sc[t];
+      const float s0 = end_density(ws, D, cw, oy, sc, dim, x, y, z);
+      const float s1 = end_density(ws, D, cw, oy, sc, dim, x1, y1, z1);
       const float mu = (0.0f - s0) / (s1 - s0);
       const float q0[3] = {(float)x, (float)y, (float)z};
       const float dl[3] = {(float)(x1 - x), (float)(y1 - y), (float)(z1 - z)};

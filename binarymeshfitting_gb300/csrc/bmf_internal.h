@@ -70,13 +70,16 @@ struct WordScratch {
   // as {chunk, sample index in the chunk}; *fcount (zeroed before the count
   // kernel) entries, at most fix_cap kept.  A crossing has two ends, so the
   // list holds at most twice the vertex count (2 vcap + 1 suffices).
-  // all_inexact (the 2D heightmap's column fill, which stores no densities):
-  // every sample counts as inexact, with no mask.
   const uint32_t* exact = nullptr;
   uint2* fix = nullptr;
   uint32_t* fcount = nullptr;
   int64_t fix_cap = 0;
-  int all_inexact = 0;
+  // The 2D heightmap's column fill (Mode R batches, nullable): no densities
+  // are stored; the emit computes a crossing end's density from its (x, z)
+  // column height (at chunk.words + x * dim + z) as the full fill does,
+  // -(py * g) - n * height with py = chunk.oy + y * scale.
+  const float* cols2d = nullptr;
+  float c2d_g = 0.0f, c2d_height = 0.0f;
 };
 
 // Fill + label.  A terrain field of a single chunk goes through the line
@@ -120,10 +123,9 @@ int launch_fit_loss_spheres(const ChunkDev* d_chunks, int n_chunks, const uint32
 int launch_adam(float* p, const float* g, float* m, float* v, int64_t n, int* step, float lr, float b1, float b2,
                 float eps, cudaStream_t st);
 // exact densities for the samples the count kernel listed in ws.fix (the
-// inexact ends of crossings; after launch_count, before launch_emit); cols:
-// the 2D heightmap's column heights (launch_sample_label), else null
+// inexact ends of crossings; after launch_count, before launch_emit)
 void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, float* dens,
-                       cudaStream_t st, const float* cols = nullptr);
+                       cudaStream_t st);
 int fill_terrain_items(int dim);          // items of one chunk
 int fill_terrain_lines();                 // lines per item
 int fill_terrain_resident_ctas(int run, int octaves, bool band);  // persistent grid: SMs x resident CTAs per SM

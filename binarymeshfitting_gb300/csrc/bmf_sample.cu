@@ -604,11 +604,9 @@ __device__ float terrain_exact(const FieldDev& f, const int* __restrict__ perm2,
   return __fmaf_rn(-ampl, sum, py - h0);
 }
 
-// The 2D heightmap's column fill stores no densities: the listed samples
-// take theirs from the stored column height, with the fill's operations.
 __global__ void __launch_bounds__(256) k_fill_fixup(const ChunkDev* __restrict__ chunks, const uint2* __restrict__ list,
                                                     const uint32_t* __restrict__ count, int64_t cap, FieldDev field,
-                                                    float* __restrict__ dens, const float* __restrict__ cols) {
+                                                    float* __restrict__ dens) {
   __shared__ int perm2[512];
   __shared__ float4 gtab[512];
   for (int i = threadIdx.x; i < 512; i += blockDim.x) {
@@ -622,17 +620,12 @@ __global__ void __launch_bounds__(256) k_fill_fixup(const ChunkDev* __restrict__
     const ChunkDev ch = chunks[ent.x];
     const uint32_t dim = (uint32_t)ch.dim, line = ent.y / dim;
     const int z = (int)(ent.y - line * dim), x = (int)(line / dim), y = (int)(line - (uint32_t)x * dim);
-    if (cols) {
-      const float py = ch.oy + (float)y * ch.scale;
-      dens[ch.dens + (int64_t)ent.y] = terrain2d_density(field, py, __ldg(cols + ch.words + (int64_t)x * dim + z));
-    } else {
-      dens[ch.dens + (int64_t)ent.y] = terrain_exact(field, perm2, gtab, ch, x, y, z);
-    }
+    dens[ch.dens + (int64_t)ent.y] = terrain_exact(field, perm2, gtab, ch, x, y, z);
   }
 }
 
 void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const FieldDev& field, float* dens,
-                       cudaStream_t st, const float* cols) {
+                       cudaStream_t st) {
   static std::atomic<int> grid[64] = {};
   const int g = per_device_once(grid, [](int dev) {
     int sms = 0, per_sm = 0;
@@ -640,7 +633,7 @@ void launch_fill_fixup(const ChunkDev* d_chunks, const WordScratch& ws, const Fi
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fill_fixup, 256, 0);
     return (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
   });
-  k_fill_fixup<<<g, 256, 0, st>>>(d_chunks, ws.fix, ws.fcount, ws.fix_cap, field, dens, cols);
+  k_fill_fixup<<<g, 256, 0, st>>>(d_chunks, ws.fix, ws.fcount, ws.fix_cap, field, dens);
 }
 
 int fill_terrain_items(int dim) { return (dim * dim + kFillLines - 1) / kFillLines; }
