@@ -279,8 +279,11 @@ typedef struct {
   int32_t sweep_block; /* threads per CTA of the dual / primal sweeps: 128, 256 or 512 */
   int32_t fill_band;   /* 1: band fill (Mode R terrain plans, fill_mode 1 or 2): a run stops evaluating octaves
                           once the bound on the remaining octaves fixes every sample's sign, and only the ends of
-                          sign-changing edges get exact densities (the mesh reads no others); 0: every sample's
-                          density exact.  Both give bit-identical meshes.  Default 1 where supported. */
+                          sign-changing edges get exact densities (the mesh reads no others); for Mode R plans of
+                          BMF_FIELD_TERRAIN_2D the column fill: each (x, z) column height is evaluated once, the
+                          occupancy words come from the heights, and the emit computes the densities it reads
+                          from them (no density is stored); 0: every sample's density exact.  Both give
+                          bit-identical meshes.  Default 1 where supported. */
   int32_t reserved[4];
 } bmf_batch_tuning;
 BMF_API bmf_status bmf_batch_get_tuning(const bmf_batch* b, bmf_batch_tuning* t);
