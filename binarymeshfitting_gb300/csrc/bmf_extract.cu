@@ -1162,43 +1162,43 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
     // 2. stage the neighbourhoods (zeros outside the chunk): one item per
     // (word, neighbour line) loads the line's blocks zb-1..zb+1; one item per
     // (word, owner line) its vertex bases in blocks zb, zb+1; one per word its
-    // index base and count planes
+    // index base and count planes -- three loops, so a warp's lanes take the
+    // same branch
     // (asynchronous global -> shared copies: a lane issues every copy of its
     // items and waits once, instead of a load-then-store per item)
-    for (int k = lane; k < nt * 21; k += 32) {
-      const int t = k / 21, it = k - t * 21;
-      const int dim = R.dim[t], zc = R.zc[t], x = R.x[t], y = R.y[t], zb = R.zb[t];
-      const int64_t cw = R.cw[t];
-      if (it < 16) {
-        const int i = it >> 2, j = it & 3;
-        const int xx = x - 1 + i, yy = y - 1 + j;
-        uint32_t* dst = R.nb[t].w + (i * 4 + j) * 3;
-        if (xx < 0 || yy < 0 || xx >= dim || yy >= dim) {
-          dst[0] = dst[1] = dst[2] = 0u;
-        } else {
-          const uint32_t* L = words + cw + (xx * dim + yy) * zc + zb;
-          if (zb > 0) stage_async(dst, L - 1); else dst[0] = 0u;
-          stage_async(dst + 1, L);
-          if (zb + 1 < zc) stage_async(dst + 2, L + 1); else dst[2] = 0u;
-        }
-      } else if (it < 20) {
-        const int l = it - 16;
-        const int xx = x + (l >> 1), yy = y + (l & 1);
-        uint32_t* dst = R.nb[t].vb + (l >> 1) * 4 + (l & 1) * 2;
-        if (xx < dim && yy < dim) {
-          const uint32_t* V = ws.vcnt + cw + (xx * dim + yy) * zc + zb;
-          stage_async(dst, V);
-          if (zb + 1 < zc) stage_async(dst + 1, V + 1); else dst[1] = 0u;
-        } else {
-          dst[0] = dst[1] = 0u;
-        }
+    for (int k = lane; k < nt * 16; k += 32) {
+      const int t = k >> 4, i = (k >> 2) & 3, j = k & 3;
+      const int dim = R.dim[t], zc = R.zc[t], zb = R.zb[t];
+      const int xx = R.x[t] - 1 + i, yy = R.y[t] - 1 + j;
+      uint32_t* dst = R.nb[t].w + (i * 4 + j) * 3;
+      if (xx < 0 || yy < 0 || xx >= dim || yy >= dim) {
+        dst[0] = dst[1] = dst[2] = 0u;
       } else {
-        const int64_t wi = cw + (x * dim + y) * zc + zb;
-        stage_async(&R.ib[t], ws.icnt + wi);
-        stage_async(&R.p0[t], ws.gpl + 3 * wi);
-        stage_async(&R.p1[t], ws.gpl + 3 * wi + 1);
-        stage_async(&R.p2[t], ws.gpl + 3 * wi + 2);
+        const uint32_t* L = words + R.cw[t] + (xx * dim + yy) * zc + zb;
+        if (zb > 0) stage_async(dst, L - 1); else dst[0] = 0u;
+        stage_async(dst + 1, L);
+        if (zb + 1 < zc) stage_async(dst + 2, L + 1); else dst[2] = 0u;
       }
+    }
+    for (int k = lane; k < nt * 4; k += 32) {
+      const int t = k >> 2, l = k & 3;
+      const int dim = R.dim[t], zc = R.zc[t], zb = R.zb[t];
+      const int xx = R.x[t] + (l >> 1), yy = R.y[t] + (l & 1);
+      uint32_t* dst = R.nb[t].vb + (l >> 1) * 4 + (l & 1) * 2;
+      if (xx < dim && yy < dim) {
+        const uint32_t* V = ws.vcnt + R.cw[t] + (xx * dim + yy) * zc + zb;
+        stage_async(dst, V);
+        if (zb + 1 < zc) stage_async(dst + 1, V + 1); else dst[1] = 0u;
+      } else {
+        dst[0] = dst[1] = 0u;
+      }
+    }
+    if (lane < nt) {
+      const int64_t wi = R.cw[lane] + (R.x[lane] * R.dim[lane] + R.y[lane]) * R.zc[lane] + R.zb[lane];
+      stage_async(&R.ib[lane], ws.icnt + wi);
+      stage_async(&R.p0[lane], ws.gpl + 3 * wi);
+      stage_async(&R.p1[lane], ws.gpl + 3 * wi + 1);
+      stage_async(&R.p2[lane], ws.gpl + 3 * wi + 2);
     }
     stage_wait();
     __syncwarp();
