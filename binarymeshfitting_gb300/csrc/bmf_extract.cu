@@ -75,6 +75,7 @@ struct SmemTabs {
   uint64_t tri[256];
   uint64_t uses[256];
   uint64_t grp[256];
+  uint64_t etris[256];  // per case and edge e: bits [5 e, 5 e + 5) mark the triangles that use e
 };
 __device__ __forceinline__ void load_tabs(SmemTabs& t) {
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
@@ -154,6 +155,23 @@ constexpr CaseCounts make_case_counts() {
   return c;
 }
 static __device__ const CaseCounts g_case_counts = make_case_counts();
+
+// Per corner mask and edge e: which of the case's triangles (bit t, t < 5)
+// use edge e, at bits [5 e, 5 e + 5) -- derived from the triangle table.
+struct EdgeTris {
+  uint64_t w[256];
+};
+constexpr EdgeTris make_edge_tris() {
+  constexpr uint64_t tri[256] = BMF_TRI_CASES_INIT;
+  EdgeTris r{};
+  for (int m = 0; m < 256; ++m) {
+    const int nt = (int)(tri[m] >> 60);
+    for (int t = 0; t < nt; ++t)
+      for (int i = 0; i < 3; ++i) r.w[m] |= 1ull << (5 * (int)((tri[m] >> (4 * (3 * t + i))) & 0xFu) + t);
+  }
+  return r;
+}
+static __device__ const EdgeTris g_edge_tris = make_edge_tris();
 
 constexpr int kCountThreads = 64;
 
@@ -754,21 +772,21 @@ void launch_place_bwd(int placement, int wide, const ChunkDev* d_chunks, int n_c
 // chunk); W is the chunk's words, 32-bit offsets.
 __device__ __forceinline__ uint32_t line_bits3(const uint32_t* __restrict__ W, int dim, int zc, int x, int y, int z0) {
   if (x < 0 || y < 0 || x >= dim || y >= dim) return 0u;
-  const int b0 = z0 >> 5;  // arithmetic shift: block -1 for z0 = -1
+  const int b0 = z0 >> 5, s = z0 & 31;  // arithmetic shift: block -1 for z0 = -1
   const uint32_t* L = W + (x * dim + y) * zc;
-  const uint32_t lo = (b0 >= 0 && b0 < zc) ? __ldg(L + b0) : 0u;
-  const uint32_t hi = (b0 + 1 < zc) ? __ldg(L + b0 + 1) : 0u;
-  const uint64_t q = ((uint64_t)hi << 32) | lo;
-  return (uint32_t)(q >> (z0 & 31)) & 7u;
+  uint32_t bits = (b0 >= 0 && b0 < zc) ? __ldg(L + b0) >> s : 0u;
+  if (s > 29 && b0 + 1 < zc) bits |= __ldg(L + b0 + 1) << (32 - s);  // the three bits cross into the next word
+  return bits & 7u;
 }
 
 // Which case tables a kernel stages in shared memory.
-template <bool TRI, bool USES, bool GRP>
+template <bool TRI, bool USES, bool GRP, bool ETRIS = false>
 __device__ __forceinline__ void load_tabs_some(SmemTabs& t) {
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
     if (TRI) t.tri[i] = __ldg(g_tri_cases + i);
     if (USES) t.uses[i] = __ldg(g_edge_uses + i);
     if (GRP) t.grp[i] = __ldg(g_group_cases + i);
+    if (ETRIS) t.etris[i] = g_edge_tris.w[i];
   }
   __syncthreads();
 }
@@ -815,17 +833,15 @@ __device__ __forceinline__ void adj_vertex(const SmemTabs& T, const ChunkDev& ch
       const uint32_t base = nbits >> (3 * (3 * (1 + ox) + (1 + oy)) + 1 + oz);
       const int m = (int)((base & 3u) | (((base >> 3) & 3u) << 2) | (((base >> 9) & 3u) << 4) |
                           (((base >> 12) & 3u) << 6));
-      if (!tab_uses(T, m, e)) continue;
-      const uint64_t tw = T.tri[m];
-      const int nt = (int)(tw >> 60);
+      // the cell's triangles that use edge e, ascending (polygonize_cell order)
+      uint32_t tm = (uint32_t)(T.etris[m] >> (5 * e)) & 31u;
+      if (!tm) continue;
       const int wi = (cx * dim + cy) * zc + (cz >> 5);
       const uint32_t lt = lane_lt(cz & 31);
       const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
                            4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
       const int64_t first = pbase + __ldg(ibase + wi) / 3u + pre;
-      for (int t = 0; t < nt; ++t)
-        if ((tri_edge(tw, 3 * t) == e || tri_edge(tw, 3 * t + 1) == e || tri_edge(tw, 3 * t + 2) == e) && n < room)
-          out[n++] = (uint32_t)(first + t);
+      for (; tm && n < room; tm &= tm - 1u) out[n++] = (uint32_t)(first + __ffs(tm) - 1);
     }
   } else {
     const int g = k;
@@ -861,7 +877,7 @@ __global__ void __launch_bounds__(256) k_adj_build(const ChunkDev* __restrict__ 
                                                    const int64_t* __restrict__ d_counts, int64_t vcap,
                                                    uint32_t* __restrict__ adj) {
   __shared__ SmemTabs T;
-  load_tabs_some<MODE == 0, MODE == 0, MODE != 0>(T);
+  load_tabs_some<false, false, MODE != 0, MODE == 0>(T);
   const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= (d_counts ? min(vcap, d_counts[0]) : vcap)) return;
   const int c = find_chunk_by_vertex(chunks, n_chunks, v);
@@ -902,7 +918,7 @@ __global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_c
   __shared__ uint32_t s_warp[kWarps];
   __shared__ uint32_t s_total;
   __shared__ int s_item;
-  load_tabs_some<MODE == 0, MODE == 0, MODE != 0>(T);
+  load_tabs_some<false, false, MODE != 0, MODE == 0>(T);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t nvb = d_counts ? min(nv, d_counts[0]) : nv;
   const int64_t npb = d_counts ? min(n_prims, d_counts[1] / N) : n_prims;
