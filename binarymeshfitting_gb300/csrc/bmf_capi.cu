@@ -11,6 +11,7 @@
 
 #include "../../include/bmf.h"
 #include "bmf_device.cuh"
+#include "bmf_trace.h"
 #include "bmf_internal.h"
 
 using namespace bmf;
@@ -327,6 +328,7 @@ int64_t bmf_launch_count(const bmf_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 bmf_status bmf_sample_label(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
                             uint32_t* d_words, int32_t* h_contains_mesh, void* stream) {
+  BMF_TRACE("bmf_sample_label");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   if (!desc_ok(desc) || !field_ok(field) || !d_words)
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_sample_label: bad descriptor, field or words pointer");
@@ -356,6 +358,7 @@ bmf_status bmf_sample_label(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_
 
 bmf_status bmf_sample_block(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field, float* d_density,
                             void* stream) {
+  BMF_TRACE("bmf_sample_block");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   if (!desc_ok(desc) || !field_ok(field) || field->kind == BMF_FIELD_GRID || !d_density)
     return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_sample_block: bad descriptor, field or density pointer");
@@ -368,6 +371,7 @@ bmf_status bmf_sample_block(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_
 
 bmf_status bmf_label_grid(bmf_ctx* ctx, int32_t dim, const float* d_density, uint32_t* d_words,
                           int32_t* h_contains_mesh, void* stream) {
+  BMF_TRACE("bmf_label_grid");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   bmf_chunk_desc d{};
   d.scale = 1.0f;
@@ -378,6 +382,7 @@ bmf_status bmf_label_grid(bmf_ctx* ctx, int32_t dim, const float* d_density, uin
 }
 
 bmf_status bmf_cell_masks(bmf_ctx* ctx, int32_t dim, const uint32_t* d_words, uint8_t* d_masks, void* stream) {
+  BMF_TRACE("bmf_cell_masks");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   if (!dim_ok(dim) || !d_words || !d_masks) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_cell_masks: bad args");
   launch_cell_masks(dim, d_words, d_masks, (cudaStream_t)stream);
@@ -387,6 +392,7 @@ bmf_status bmf_cell_masks(bmf_ctx* ctx, int32_t dim, const uint32_t* d_words, ui
 
 bmf_status bmf_polygonize(bmf_ctx* ctx, int32_t dim, const float* d_density, const uint32_t* d_words, int32_t mode,
                           int32_t placement, bmf_mesh* out, void* stream) {
+  BMF_TRACE("bmf_polygonize");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   bmf_status s;
   if ((s = mesh_valid(ctx, out)) != BMF_OK) return s;
@@ -430,6 +436,7 @@ bmf_status bmf_polygonize(bmf_ctx* ctx, int32_t dim, const float* d_density, con
 
 bmf_status bmf_process(bmf_ctx* ctx, bmf_mesh* mesh, int32_t iters, int32_t process_boundary,
                        int32_t smooth_normals, void* stream) {
+  BMF_TRACE("bmf_process");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   bmf_status s;
   if ((s = mesh_valid(ctx, mesh)) != BMF_OK) return s;
@@ -440,6 +447,7 @@ bmf_status bmf_process(bmf_ctx* ctx, bmf_mesh* mesh, int32_t iters, int32_t proc
 
 bmf_status bmf_lod_generate(bmf_ctx* ctx, const bmf_lod_params* p, bmf_chunk_desc* d_descs, int32_t cap,
                             int32_t* d_count, void* stream) {
+  BMF_TRACE("bmf_lod_generate");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   if (!p || !d_descs || !d_count || cap <= 0 || cap > kLodMaxLeaves || p->max_level < 0 || p->max_level > 20 ||
       p->min_level < 0 || !dim_ok(p->dim) || !(p->root_size > 0.0f))
@@ -454,6 +462,7 @@ bmf_status bmf_lod_generate(bmf_ctx* ctx, const bmf_lod_params* p, bmf_chunk_des
 
 bmf_status bmf_format(bmf_ctx* ctx, const bmf_mesh* mesh, int32_t unwind, int32_t smooth_normals, float* d_p,
                       float* d_n, float* d_c, int64_t cap, int64_t* h_count, void* stream) {
+  BMF_TRACE("bmf_format");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   if (!mesh || !mesh->d_pos || !d_p || !d_n || !d_c || cap < 0 || mesh->n_verts < 0 || mesh->n_idx < 0 ||
       (unwind && (mesh->prim_size != 4 || !mesh->d_idx)) || (unwind && smooth_normals && !mesh->d_nrm))
@@ -478,6 +487,7 @@ bmf_status bmf_format(bmf_ctx* ctx, const bmf_mesh* mesh, int32_t unwind, int32_
 
 bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf_field* field,
                              const bmf_extract_opts* opts, bmf_mesh* out, void* stream) {
+  BMF_TRACE("bmf_extract_chunk");
   if (!ctx) return BMF_ERR_INVALID_ARGUMENT;
   bmf_status s;
   if ((s = mesh_valid(ctx, out)) != BMF_OK) return s;
@@ -539,6 +549,7 @@ bmf_status bmf_extract_chunk(bmf_ctx* ctx, const bmf_chunk_desc* desc, const bmf
 
 bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t n_chunks, const bmf_field* field,
                             const bmf_extract_opts* opts, bmf_batch** out) {
+  BMF_TRACE("bmf_batch_create");
   if (!ctx || !out) return BMF_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   if (!h_descs || n_chunks <= 0 || !field_ok(field) || field->kind == BMF_FIELD_GRID || !opts ||
@@ -795,6 +806,7 @@ bool same_out(const bmf_batch_out& a, const bmf_batch_out& b) {
 }  // namespace
 
 bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, int32_t sync, void* stream) {
+  BMF_TRACE("bmf_batch_run");
   if (!b) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = b->ctx;
   if (!out || !out->d_pos || !out->d_idx || out->vcap < 0 || out->icap < 0)
@@ -847,6 +859,7 @@ bmf_status bmf_batch_run(bmf_batch* b, bmf_batch_out* out, int32_t use_graph, in
 }
 
 bmf_status bmf_batch_wait(bmf_batch* b, bmf_batch_out* out, int32_t timeout_ms) {
+  BMF_TRACE("bmf_batch_wait");
   if (!b) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = b->ctx;
   if (!out || timeout_ms < 0) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_wait: no output or timeout < 0");
@@ -873,6 +886,7 @@ bmf_status bmf_batch_wait(bmf_batch* b, bmf_batch_out* out, int32_t timeout_ms) 
 }
 
 bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_descs, int32_t n_chunks, void* stream) {
+  BMF_TRACE("bmf_batch_set_descs");
   if (!b) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = b->ctx;
   if (!h_descs || n_chunks != b->n) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_set_descs: count differs");
@@ -905,6 +919,7 @@ bmf_status bmf_batch_set_descs(bmf_batch* b, const bmf_chunk_desc* h_descs, int3
 }
 
 bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms, void* stream) {
+  BMF_TRACE("bmf_batch_profile");
   if (!b || !h_stage_ms) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = b->ctx;
   if (!out || !out->d_pos || !out->d_idx) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_batch_profile: no output");
@@ -960,6 +975,7 @@ bmf_status bmf_batch_profile(bmf_batch* b, bmf_batch_out* out, float* h_stage_ms
 
 bmf_status bmf_batch_format(bmf_batch* b, const bmf_batch_out* out, int32_t unwind, int32_t smooth_normals,
                             float* d_p, float* d_n, float* d_c, int64_t cap, void* stream) {
+  BMF_TRACE("bmf_batch_format");
   if (!b) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = b->ctx;
   const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
@@ -1018,6 +1034,7 @@ float median_of(std::vector<float> v) {
 
 bmf_status bmf_batch_autotune(bmf_batch* b, bmf_batch_out* out, int32_t reps, void* stream, bmf_batch_tuning* chosen,
                               float* h_ms, int32_t max_report, int32_t* n_report) {
+  BMF_TRACE("bmf_batch_autotune");
   if (!b) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = b->ctx;
   if (!out || !out->d_pos || !out->d_idx || reps <= 0)
@@ -1152,6 +1169,7 @@ bmf_status bmf_fit_destroy(bmf_fit* f) {
 
 bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t placement, int32_t iters,
                           int64_t vcap, int64_t icap, int32_t flags, bmf_fit** out) {
+  BMF_TRACE("bmf_fit_create");
   if (!ctx || !out) return BMF_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   if (n_chunks <= 0 || !dim_ok(dim) || (placement != BMF_PLACE_MASSPOINT && placement != BMF_PLACE_QEF) ||
@@ -1230,6 +1248,7 @@ bmf_status bmf_fit_create(bmf_ctx* ctx, int32_t n_chunks, int32_t dim, int32_t p
 
 bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uint32_t* d_idx, int64_t* d_chunk_info,
                            int64_t* h_counts, void* stream) {
+  BMF_TRACE("bmf_fit_forward");
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = f->ctx;
   if (!d_density || !d_pos || !d_idx) return fail(ctx, BMF_ERR_INVALID_ARGUMENT, "bmf_fit_forward: null buffer");
@@ -1276,6 +1295,7 @@ bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uin
 
 bmf_status bmf_fit_loss_spheres(bmf_fit* f, const float* d_pos, const float* d_spheres, int32_t n_spheres,
                                 float* d_loss, float* d_grad_pos, void* stream) {
+  BMF_TRACE("bmf_fit_loss_spheres");
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = f->ctx;
   if (!d_pos || !d_spheres || n_spheres <= 0 || !d_loss || !d_grad_pos || !f->last_density || !f->d_lpart)
@@ -1289,6 +1309,7 @@ bmf_status bmf_fit_loss_spheres(bmf_fit* f, const float* d_pos, const float* d_s
 
 bmf_status bmf_fit_adam(bmf_fit* f, float* d_param, const float* d_grad, float* d_m, float* d_v, int64_t n,
                         int32_t* d_step, float lr, float beta1, float beta2, float eps, void* stream) {
+  BMF_TRACE("bmf_fit_adam");
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = f->ctx;
   if (!d_param || !d_grad || !d_m || !d_v || !d_step || n < 0 || !std::isfinite(lr) || !(beta1 >= 0.0f) ||
@@ -1301,6 +1322,7 @@ bmf_status bmf_fit_adam(bmf_fit* f, float* d_param, const float* d_grad, float* 
 
 bmf_status bmf_fit_backward(bmf_fit* f, const float* d_grad_pos, int64_t n_grad_verts, float* d_grad_density,
                             void* stream) {
+  BMF_TRACE("bmf_fit_backward");
   if (!f) return BMF_ERR_INVALID_ARGUMENT;
   bmf_ctx* ctx = f->ctx;
   if (!d_grad_pos || !d_grad_density || !f->last_density || n_grad_verts < 0)

@@ -112,6 +112,22 @@ class FitPlan:
             pass
 
 
+def save_checkpoint(path, density: torch.Tensor, state: dict, **extra):
+    """The fitting loop's checkpoint: the learnable grids and the Adam state of
+    FitPlan.adam (both moments and the device step count), with torch.save;
+    extra entries (step number, hyper-parameters) are stored beside them."""
+    torch.save({"density": density.detach().cpu(), "m": state["m"].detach().cpu(),
+                "v": state["v"].detach().cpu(), "step": state["step"].detach().cpu(), "extra": extra}, path)
+
+
+def load_checkpoint(path, device):
+    """(density, Adam state, extra) from save_checkpoint, on device; the loop
+    continues with FitPlan.adam(density, grad, state) as if never stopped."""
+    ck = torch.load(path, map_location="cpu", weights_only=True)
+    state = {k: ck[k].to(device) for k in ("m", "v", "step")}
+    return ck["density"].to(device).contiguous(), state, ck["extra"]
+
+
 class ExtractFit(torch.autograd.Function):
     """positions = extract(density) with the topology held fixed."""
 
