@@ -44,9 +44,9 @@ OPS_PER_LAYER = 20          # 4 corners (mul + fma), alpha and beta (3 lerps of 
 # count by samples, the emit, scan and sweeps by output indices.
 DRAM_UPDATE_SAMPLES = 1_785_478_272
 DRAM_UPDATE_INDICES = 167_847_141
-DRAM_BYTES = {"fill": 390.4e6 + 1312.7e6 + 19.9e6 + 10.4e6,   # k_fill_terrain<16, band> + k_fill_fixup
-              "count": 331.0e6 + 1462.8e6, "scan": 590.6e6 + 530.9e6, "emit": 1858.0e6 + 2279.9e6,
-              "sweeps": 12626.5e6 + 8305.1e6}
+DRAM_BYTES = {"fill": 388.8e6 + 1311.7e6 + 19.9e6 + 10.4e6,   # k_fill_terrain<16, band> + k_fill_fixup
+              "count": 331.4e6 + 1463.0e6, "scan": 590.5e6 + 531.0e6, "emit": 1913.4e6 + 2286.5e6,
+              "sweeps": 12652.0e6 + 8302.2e6}
 
 
 def fill_fp32_ops(rows, params):
