@@ -25,9 +25,13 @@ enum Slot {
 
 constexpr int kMaxDim = 512;
 // below this many chunks the sweeps run as whole-mesh kernels: one CTA per
-// chunk needs several chunks per resident CTA (~450 on a GB300) to balance
-// (measured: 4096 mixed chunks gain 3 %, 512 equal chunks lose 3 %)
+// chunk needs several chunks per resident CTA to balance.  Mode R batches of
+// the mixed-LOD update run chunk by chunk from 512 chunks (processing stage,
+// whole-mesh -> chunk by chunk: 512 chunks 1.79 -> 1.68 ms, 1024 chunks 2.48
+// -> 1.73, 1536 chunks 3.21 -> 2.03); Mode Q batches and fit plans from 2048
+// (512 equal Mode Q chunks lose 3 % chunk by chunk)
 constexpr int kChunkSweepMinChunks = 2048;
+constexpr int kChunkSweepMinChunksR = 512;
 // fit plans: the adjoint sweeps run chunk by chunk from this many chunks (one
 // 512-thread CTA per chunk, four per SM)
 constexpr int kChunkSweepBwdMinChunks = 256;
@@ -760,7 +764,7 @@ bmf_status batch_proc_scratch(bmf_batch* b, int64_t vcap, int64_t icap) {
 // the sweeps run chunk by chunk (one CTA per chunk, largest chunks first).
 StructuredAdj batch_adj(const bmf_batch* b) {
   StructuredAdj sa{b->opts.mode, b->d_chunks, b->n, b->d_words, b->ws, b->d_vkey};
-  if (b->n >= kChunkSweepMinChunks) {
+  if (b->n >= (b->opts.mode == BMF_MODE_R ? kChunkSweepMinChunksR : kChunkSweepMinChunks)) {
     sa.tot = b->d_tot;
     sa.order = b->d_order;
     sa.queue = b->d_pqueue;

@@ -271,10 +271,11 @@ def test_batch_matches_oracle_per_chunk(ctx, mode, placement, iters, use_graph):
 
 @pytest.mark.parametrize("mode", [L.MODE_R, L.MODE_Q])
 def test_chunk_sweeps_match_whole_mesh_sweeps(ctx, mode):
-    """A batch of 2048 chunks or more runs its sweeps chunk by chunk (one CTA
-    per chunk); smaller batches run them as whole-mesh kernels.  Split in two
-    small batches, the same chunks give bit-identical positions, normals and
-    indices; a sample of chunks also matches the oracle."""
+    """A Mode R batch of 512 chunks or more (Mode Q: 2048) runs its sweeps
+    chunk by chunk (one CTA per chunk); smaller batches run them as whole-mesh
+    kernels.  Split into batches below the threshold, the same chunks give
+    bit-identical positions, normals and indices; a sample of chunks also
+    matches the oracle."""
     from binarymeshfitting_gb300.engine import Batch
     descs, rows = workloads.lod_update(n=2100, seed=9)
     for dsc, r in zip(descs, rows):  # small chunks keep the test quick
@@ -284,7 +285,7 @@ def test_chunk_sweeps_match_whole_mesh_sweeps(ctx, mode):
     big = Batch(ctx, descs, workloads.terrain_field(), **kw)
     big.allocate(3000000, 12000000, normals=True)
     nv, ni = big.run(use_graph=True)
-    parts = [(0, 1000), (1000, 2100)]
+    parts = [(k, k + 420) for k in range(0, 2100, 420)]  # below both thresholds
     got_v = 0
     checked = 0
     for lo, hi in parts:
