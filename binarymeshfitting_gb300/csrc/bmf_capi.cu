@@ -29,7 +29,8 @@ constexpr int kMaxDim = 512;
 // the mixed-LOD update run chunk by chunk from 512 chunks (processing stage,
 // whole-mesh -> chunk by chunk: 512 chunks 1.79 -> 1.68 ms, 1024 chunks 2.48
 // -> 1.73, 1536 chunks 3.21 -> 2.03); Mode Q batches and fit plans from 2048
-// (512 equal Mode Q chunks lose 3 % chunk by chunk)
+// (Mode Q chunk by chunk: mixed 512 / 1024 chunks 1.59 -> 2.21 / 2.24 -> 2.75
+// ms, 512 equal chunks lose 3 %)
 constexpr int kChunkSweepMinChunks = 2048;
 constexpr int kChunkSweepMinChunksR = 512;
 // fit plans: the adjoint sweeps run chunk by chunk from this many chunks (one
