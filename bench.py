@@ -604,10 +604,13 @@ def run_gb300(args):
         pb.run(use_graph=True, sync=False, stream=stream)
         done[k & 1].record(stream)
         with torch.cuda.stream(copy_stream):
-            copy_stream.wait_event(done[k & 1])
-            hp.copy_(pbufs["pos"][:nv], non_blocking=True)
+            # indices and chunk table are final once the extraction is: their
+            # read-back runs while the smoothing sweeps still compute
+            pb.wait_extraction(copy_stream)
             hi.copy_(pbufs["idx"][:ni], non_blocking=True)
             hn.copy_(pbufs["info"], non_blocking=True)
+            copy_stream.wait_event(done[k & 1])
+            hp.copy_(pbufs["pos"][:nv], non_blocking=True)
             if hnr is not None:
                 hnr.copy_(pbufs["nrm"][:nv], non_blocking=True)
             hb.copy_(pbufs["boundary"][:nv], non_blocking=True)
@@ -629,7 +632,8 @@ def run_gb300(args):
     e2e = {"value": args.chunks * world / (e2e_ms / 1000.0), "unit": "chunks/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
            "read_back": "positions, indices, chunk table" + (", normals" if normals else "") + ", boundary flags",
-           "pipeline": "two plans; step i's read-back on a copy stream overlaps step i + 1"}
+           "pipeline": "two plans; step i's read-back on a copy stream overlaps step i + 1, its indices and "
+                       "chunk table from the end of its extraction (bmf_batch_wait_extraction)"}
     b2.close()
     del plans, hosts, bufs2
 

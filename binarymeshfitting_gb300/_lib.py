@@ -114,6 +114,7 @@ SIGNATURES = {
     "bmf_batch_destroy": (c_int32, [c_void_p]),
     "bmf_batch_set_descs": (c_int32, [c_void_p, ctypes.POINTER(ChunkDesc), c_int32, c_void_p]),
     "bmf_batch_wait": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), c_int32]),
+    "bmf_batch_wait_extraction": (c_int32, [c_void_p, c_void_p]),
     "bmf_batch_profile": (c_int32, [c_void_p, ctypes.POINTER(BatchOut), ctypes.POINTER(c_float), c_void_p]),
     "bmf_lod_generate": (c_int32, [c_void_p, ctypes.POINTER(LodParams), c_void_p, c_int32, c_void_p, c_void_p]),
     "bmf_format": (c_int32, [c_void_p, ctypes.POINTER(Mesh), c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64,

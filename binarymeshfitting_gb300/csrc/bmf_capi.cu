@@ -81,6 +81,7 @@ struct bmf_batch {
   ChunkDev* h_stage = nullptr;       // pinned staging for bmf_batch_set_descs
   cudaEvent_t stage_done = nullptr;  // the last staging copy has been consumed
   cudaEvent_t run_done = nullptr;    // recorded after every bmf_batch_run (bmf_batch_wait polls it)
+  cudaEvent_t extract_done = nullptr;  // recorded inside every run after the emit (bmf_batch_wait_extraction)
   cudaStream_t aux = nullptr;        // private stream for bmf_batch_wait's read of the totals
   bool ran = false;
   // terrain fill: line items {chunk, first line}, largest chunks first, and
@@ -659,6 +660,8 @@ bmf_status bmf_batch_create(bmf_ctx* ctx, const bmf_chunk_desc* h_descs, int32_t
     if ((s = bail(cudaMalloc(&b->d_cols, sizeof(float) * words), "column heights")) != BMF_OK) return s;
     b->fill_band = 1;
   }
+  if ((s = bail(cudaEventCreateWithFlags(&b->extract_done, cudaEventDisableTiming), "extraction event")) != BMF_OK)
+    return s;
   *out = b;
   return BMF_OK;
 }
@@ -787,8 +790,20 @@ bmf_status batch_record(bmf_batch* b, const bmf_batch_out* out, cudaStream_t st,
                        b->d_totals, st);
   MeshOut mo{out->d_pos, out->d_nrm, proc ? b->d_boundary : out->d_boundary, proc ? b->d_valence : nullptr,
              out->d_idx, proc ? b->d_idxg : nullptr, out->vcap, out->icap, batch_keys(b) ? b->d_vkey : nullptr};
-  int64_t k = (band ? 5 : 4) + (b->d_cols ? 1 : 0) + launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units,
-                              b->d_words, b->d_dens, b->d_flags, b->ws, mo, b->d_totals, st);
+  int64_t k = (band ? 5 : 4) + (b->d_cols ? 1 : 0);
+  k += launch_emit(b->opts.mode, b->opts.placement, b->d_chunks, b->n, b->d_units, b->n_units, b->d_words, b->d_dens,
+                   b->d_flags, b->ws, mo, b->d_totals, st);
+  // indices and chunk table are final here (bmf_batch_wait_extraction); an
+  // external record, so that under capture the graph records the event itself
+  // and streams outside the graph can wait on it
+  if (b->extract_done) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    BMF_CUDA(ctx, cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusActive)
+      BMF_CUDA(ctx, cudaEventRecordWithFlags(b->extract_done, st, cudaEventRecordExternal));
+    else
+      BMF_CUDA(ctx, cudaEventRecord(b->extract_done, st));
+  }
   if (proc) {
     const int N = b->opts.mode == BMF_MODE_R ? 3 : 4;
     const StructuredAdj sa = batch_adj(b);
@@ -887,6 +902,14 @@ bmf_status bmf_batch_wait(bmf_batch* b, bmf_batch_out* out, int32_t timeout_ms) 
   out->n_idx = b->h_pinned[1];
   if (out->n_verts > out->vcap || out->n_idx > out->icap)
     return fail(ctx, BMF_ERR_CAPACITY, "bmf_batch_wait: output capacity exceeded (needed totals reported)");
+  return BMF_OK;
+}
+
+bmf_status bmf_batch_wait_extraction(bmf_batch* b, void* stream) {
+  BMF_TRACE("bmf_batch_wait_extraction");
+  if (!b) return BMF_ERR_INVALID_ARGUMENT;
+  bmf_ctx* ctx = b->ctx;
+  if (b->extract_done) BMF_CUDA(ctx, cudaStreamWaitEvent((cudaStream_t)stream, b->extract_done, 0));
   return BMF_OK;
 }
 
@@ -1368,6 +1391,7 @@ bmf_status bmf_batch_destroy(bmf_batch* b) {
   if (b->h_stage) cudaFreeHost(b->h_stage);
   if (b->stage_done) cudaEventDestroy(b->stage_done);
   if (b->run_done) cudaEventDestroy(b->run_done);
+  if (b->extract_done) cudaEventDestroy(b->extract_done);
   if (b->aux) cudaStreamDestroy(b->aux);
   delete b;
   return BMF_OK;

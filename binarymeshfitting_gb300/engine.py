@@ -255,6 +255,12 @@ class Batch:
         self.ctx._check(self.ctx.lib.bmf_batch_wait(self.h, ctypes.byref(self.out), int(timeout_ms)))
         return int(self.out.n_verts), int(self.out.n_idx)
 
+    def wait_extraction(self, stream=None):
+        """bmf_batch_wait_extraction: `stream` (default: the current one) waits on
+        the device until the last run's extraction is done -- indices and chunk
+        table final -- while its smoothing may still run."""
+        self.ctx._check(self.ctx.lib.bmf_batch_wait_extraction(self.h, _stream(stream)))
+
     def set_descs(self, descs, stream=None):
         arr = (L.ChunkDesc * self.n)(*descs)
         self.ctx._check(self.ctx.lib.bmf_batch_set_descs(self.h, arr, self.n, _stream(stream)))

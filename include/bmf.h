@@ -215,6 +215,14 @@ BMF_API bmf_status bmf_batch_destroy(bmf_batch* b);
  * not block (the reference's watcher thread, WorldWatcher.cpp) polls with 0.
  * No counterpart in the reference (its extraction is synchronous). */
 BMF_API bmf_status bmf_batch_wait(bmf_batch* b, bmf_batch_out* out, int32_t timeout_ms);
+/* Makes `stream` wait, on the device (no host sync), until the extraction of
+ * the plan's last enqueued run is done: the indices and the chunk table are
+ * final there while the smoothing sweeps still run, so a caller can start
+ * copying or consuming the topology early (the positions, normals and boundary
+ * flags are final only when the run is).  An event recorded inside the run
+ * (inside its graph too); a plan that has not run yet makes this a no-op.
+ * No counterpart in the reference (its extraction is synchronous). */
+BMF_API bmf_status bmf_batch_wait_extraction(bmf_batch* b, void* stream);
 /* Replaces the plan's chunk descriptors with those of the next update (same
  * count and the same dim per slot, e.g. the next frame of a streaming world):
  * an asynchronous pinned host->device copy on `stream`, so the captured graph
