@@ -1114,6 +1114,10 @@ struct RTile {
   int x[kTileWords], y[kTileWords], zb[kTileWords], dim[kTileWords], zc[kTileWords];
   int64_t cw[kTileWords], dens[kTileWords], vout[kTileWords], iout[kTileWords];
   float oy[kTileWords], sc[kTileWords];  // the chunk's y origin and scale (2D column fill)
+  // per word, the crossing words of the owner lines (x + i, y + j), i, j in
+  // {0, 1}: X and Y in blocks zb, zb + 1 ([i][j][b]) and Z in block zb -- what
+  // a triangle's three vertex ids are counted from (tile_vertex_id)
+  uint32_t ox_[kTileWords][8], oy_[kTileWords][8], oz_[kTileWords][4];
   int voff[kTileWords + 1], toff[kTileWords + 1];  // exclusive vertex / triangle offsets of the tile's words
 };
 
@@ -1137,6 +1141,20 @@ __device__ __forceinline__ int tile_word(const int* off, int nt, int j) {
   for (int s = kTileWords / 2; s > 0; s >>= 1)
     if (t + s < nt && off[t + s] <= j) t += s;
   return t;
+}
+
+// Chunk-local id of the vertex on the axis-a crossing owned by sample
+// (x + i, y + j, zabs), i, j in {0, 1}, zabs in blocks zb, zb + 1 of tile word
+// t: nb_vertex_id's count, from the word's staged owner-line crossing words.
+__device__ __forceinline__ uint32_t tile_vertex_id(const RTile& R, int t, int i, int j, int zabs, int a) {
+  const int b = (zabs >> 5) - R.zb[t], l = zabs & 31;
+  const int q = i * 2 + j;
+  const uint32_t X = R.ox_[t][q * 2 + b], Y = R.oy_[t][q * 2 + b], lt = lane_lt(l);
+  uint32_t id = R.nb[t].vb[i * 4 + j * 2 + b] + __popc(X & lt) + __popc(Y & lt);
+  if (l > 0) id += __popc(R.oz_[t][q] & lt);  // then b == 0
+  if (a >= 1) id += (X >> l) & 1u;
+  if (a >= 2) id += (Y >> l) & 1u;
+  return id;
 }
 
 __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const ChunkDev* __restrict__ chunks,
@@ -1234,6 +1252,21 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
         R.X[lane] = X;
         R.Y[lane] = Y;
         R.Z[lane] = Z;
+        // the owner lines' crossing words, as nb_vertex_id forms them
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = q >> 1, j = q & 1;
+#pragma unroll
+          for (int b = 0; b < 2; ++b) {
+            const uint32_t w0 = nb.w[((i + 1) * 4 + (j + 1)) * 3 + b + 1];
+            R.ox_[lane][q * 2 + b] = (x + i + 1 < dim) ? w0 ^ nb.w[((i + 2) * 4 + (j + 1)) * 3 + b + 1] : 0u;
+            R.oy_[lane][q * 2 + b] = (y + j + 1 < dim) ? w0 ^ nb.w[((i + 1) * 4 + (j + 2)) * 3 + b + 1] : 0u;
+          }
+          const uint32_t w0 = nb.w[((i + 1) * 4 + (j + 1)) * 3 + 1];
+          uint32_t Zq = w0 ^ ((w0 >> 1) | (nb.w[((i + 1) * 4 + (j + 1)) * 3 + 2] << 31));
+          if (valid < 32) Zq &= valid <= 0 ? 0u : ((1u << valid) - 1u);
+          R.oz_[lane][q] = Zq;
+        }
         const uint32_t nv = __popc(X) + __popc(Y) + __popc(Z);
         const uint32_t ntri = __popc(R.p0[lane]) + 2u * __popc(R.p1[lane]) + 4u * __popc(R.p2[lane]);
         packed = nv | (ntri << 16);  // at most 96 and 160 per word
@@ -1347,7 +1380,7 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
       }
       const uint64_t tw = s_tri[mask];
       if (3 * r + 3 > 3 * (int)(tw >> 60)) continue;  // the planes and the case table agree
-      const int dim = R.dim[t], x = R.x[t], y = R.y[t], zb = R.zb[t], z = 32 * zb + l;
+      const int z = 32 * R.zb[t] + l;
       const int64_t gi = R.iout[t] + (int64_t)R.ib[t] + 3 * (int64_t)k;
       const int64_t vout = R.vout[t];
 #pragma unroll
@@ -1356,7 +1389,7 @@ __global__ void __launch_bounds__(32 * kEmitWarps, 4) k_emit_words_r(const Chunk
         // EDGE_V owner of edge e: axis e >> 2, offsets from its two low bits
         const int ea = e >> 2, d1 = (e >> 1) & 1, d2 = e & 1;
         const int ox = ea == 0 ? 0 : d1, oy = ea == 0 ? d1 : (ea == 1 ? 0 : d2), oz = ea == 2 ? 0 : d2;
-        const uint32_t vid = nb_vertex_id(nb, dim, x, y, zb, ox, oy, z + oz, ea);
+        const uint32_t vid = tile_vertex_id(R, t, ox, oy, z + oz, ea);
         if (gi + i < out.icap) {
           out.idx[gi + i] = vid;
           if (out.idx_global) out.idx_global[gi + i] = (uint32_t)(vout + vid);
