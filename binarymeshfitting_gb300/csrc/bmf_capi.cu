@@ -1304,6 +1304,7 @@ bmf_status bmf_fit_forward(bmf_fit* f, const float* d_density, float* d_pos, uin
       sa.tot = f->d_tot;
       sa.order = f->d_order;
       sa.queue = f->d_pqueue;
+      sa.wide_adj = true;  // bmf_fit_backward's adjoint sweeps read it
     }
     k += launch_process(4, f->vcap, f->icap / 4, f->d_totals, d_pos, nullptr, f->d_boundary, f->d_valence, f->d_idxg,
                         f->iters, 0, 0, f->ps, &sa, st);

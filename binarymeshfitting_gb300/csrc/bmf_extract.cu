@@ -793,10 +793,13 @@ __device__ __forceinline__ void load_tabs_some(SmemTabs& t) {
 
 // The adjacency list of one vertex (key: its packed grid position) of chunk
 // ch, at most room entries, into out.
-template <int MODE>
+// OUT = uint16_t with rel = the chunk's first primitive: the list holds
+// chunk-relative ids (the chunk-by-chunk sweeps, for chunks of at most 65535
+// primitives: half the bytes in the gathers' working set).
+template <int MODE, typename OUT = uint32_t>
 __device__ __forceinline__ void adj_vertex(const SmemTabs& T, const ChunkDev& ch, const uint32_t* __restrict__ words,
-                                           const WordScratch& ws, uint32_t key, uint32_t* __restrict__ out,
-                                           int room) {
+                                           const WordScratch& ws, uint32_t key, OUT* __restrict__ out,
+                                           int room, int64_t rel = 0) {
   const int dim = ch.dim, zc = ch.zc;
   const int64_t iout = ch.iout;
   const uint32_t* W = words + ch.words;
@@ -841,7 +844,7 @@ __device__ __forceinline__ void adj_vertex(const SmemTabs& T, const ChunkDev& ch
       const uint32_t pre = __popc(__ldg(pl + 3 * wi) & lt) + 2 * __popc(__ldg(pl + 3 * wi + 1) & lt) +
                            4 * __popc(__ldg(pl + 3 * wi + 2) & lt);
       const int64_t first = pbase + __ldg(ibase + wi) / 3u + pre;
-      for (; tm && n < room; tm &= tm - 1u) out[n++] = (uint32_t)(first + __ffs(tm) - 1);
+      for (; tm && n < room; tm &= tm - 1u) out[n++] = (OUT)(first + __ffs(tm) - 1 - rel);
     }
   } else {
     const int g = k;
@@ -866,7 +869,7 @@ __device__ __forceinline__ void adj_vertex(const SmemTabs& T, const ChunkDev& ch
       while (j > 0 && ids[j - 1] > id) { ids[j] = ids[j - 1]; --j; }
       ids[j] = id;
     }
-    for (int i = 0; i < n && i < room; ++i) out[i] = ids[i];
+    for (int i = 0; i < n && i < room; ++i) out[i] = (OUT)(ids[i] - rel);
   }
 }
 
@@ -912,7 +915,7 @@ __global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_c
     const int64_t* __restrict__ d_counts, uint32_t* __restrict__ off, const uint8_t* __restrict__ valence,
     uint32_t* __restrict__ adj, const uint8_t* __restrict__ boundary, const uint32_t* __restrict__ idx,
     float* __restrict__ pos, float* __restrict__ nrm, float* __restrict__ dual_p, float* __restrict__ dual_n,
-    int iters, int process_boundary, int sn) {
+    int iters, int process_boundary, int sn, int wide_adj) {
   constexpr int kThreads = chunk_sweep_threads<MODE>(), kWarps = kThreads / 32;
   __shared__ SmemTabs T;
   __shared__ uint32_t s_warp[kWarps];
@@ -965,10 +968,18 @@ __global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_c
       __syncthreads();
     }
     // adjacency, in each vertex's own CSR range and inside adj
+    // a chunk of at most 65535 primitives keeps 16-bit chunk-relative ids, in
+    // the first half of its own span of adj (its lists hold as many entries
+    // as it has indices)
+    const bool compact = !wide_adj && p1 - p0 <= 65535;
+    uint16_t* adj16 = reinterpret_cast<uint16_t*>(adj + ch.iout);
     for (int64_t v = v0 + threadIdx.x; v < v1; v += kThreads) {
       const uint32_t o = off[v];
       const int room = (int)max((int64_t)0, min((int64_t)__ldg(valence + v), adj_cap - (int64_t)o));
-      adj_vertex<MODE>(T, ch, words, ws, __ldg(vkey + v), adj + o, room);
+      if (compact)
+        adj_vertex<MODE, uint16_t>(T, ch, words, ws, __ldg(vkey + v), adj16 + (o - (uint32_t)ch.iout), room, p0);
+      else
+        adj_vertex<MODE>(T, ch, words, ws, __ldg(vkey + v), adj + o, room);
     }
     __syncthreads();
     // the sweeps in 32-bit chunk-relative indices over chunk-based pointers
@@ -990,9 +1001,15 @@ __global__ void __launch_bounds__(chunk_sweep_threads<MODE>(), chunk_sweep_min_c
       for (uint32_t t = threadIdx.x; t < np_c; t += kThreads)
         dual_prim<N, true, true>(t, nvb32, idx_c, pos, nrm, dp_c, dn_c, normal_mode);
       __syncthreads();
-      for (uint32_t v = threadIdx.x; v < nv_c; v += kThreads)
-        primal_vertex<true, true>(v, npl32, adj_cap, off_c, nullptr, val_c, adj, bnd_c, dual_p, dual_n, pos_c, nrm_c,
-                                  process_boundary, sn, set_colors);
+      if (compact) {
+        for (uint32_t v = threadIdx.x; v < nv_c; v += kThreads)
+          primal_vertex<true, true, uint32_t, uint16_t>(v, np_c, adj_cap, off_c, nullptr, val_c, adj, bnd_c, dp_c, dn_c,
+                                                        pos_c, nrm_c, process_boundary, sn, set_colors, ch.iout);
+      } else {
+        for (uint32_t v = threadIdx.x; v < nv_c; v += kThreads)
+          primal_vertex<true, true>(v, npl32, adj_cap, off_c, nullptr, val_c, adj, bnd_c, dual_p, dual_n, pos_c, nrm_c,
+                                    process_boundary, sn, set_colors);
+      }
       __syncthreads();
     }
   }
@@ -1019,7 +1036,7 @@ void launch_sweep_chunks(const StructuredAdj& sa, int N, int64_t nv, int64_t n_p
   k_sweep_chunks<M, NN><<<sweep_chunks_grid<M, NN>(), chunk_sweep_threads<M>(), 0, st>>>(                     \
       sa.chunks, sa.tot, sa.order, sa.n_chunks, sa.queue, sa.words, sa.ws, sa.vkey, nv, n_prims, adj_cap,        \
       d_counts, s.off, valence, s.adj, boundary, idx, pos, nrm, s.dual_p, s.dual_n, iters, process_boundary,      \
-      smooth_normals)
+      smooth_normals, sa.wide_adj ? 1 : 0)
   if (sa.mode == 0) {
     if (N == 3) BMF_SWEEP_CHUNKS(0, 3); else BMF_SWEEP_CHUNKS(0, 4);
   } else {

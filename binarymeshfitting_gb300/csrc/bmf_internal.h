@@ -181,6 +181,10 @@ struct StructuredAdj {
   const uint32_t* tot = nullptr;  // per chunk {vertices, indices}
   const int* order = nullptr;     // chunk indices, largest first
   int* queue = nullptr;           // one int, reset by launch_process
+  // the chunk-by-chunk sweeps keep 16-bit chunk-relative adjacency lists for
+  // chunks of at most 65535 primitives unless a later pass reads the
+  // adjacency (the fit's adjoint sweeps want 32-bit mesh-wide ids)
+  bool wide_adj = false;
 };
 void launch_adj_build(int mode, const ChunkDev* d_chunks, int n_chunks, const uint32_t* words, WordScratch ws,
                       const uint32_t* vkey, const uint32_t* off, const int64_t* d_counts, int64_t vcap,

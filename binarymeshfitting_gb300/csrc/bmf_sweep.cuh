@@ -146,21 +146,24 @@ __device__ __forceinline__ void dual_prim(I t, I nvb, const uint32_t* __restrict
 // I: the index type of v and np_lim, as for dual_prim (within one chunk, off,
 // cursor, valence, boundary, pos and nrm start at the chunk's first vertex;
 // adjacency offsets and primitive ids stay mesh-wide).
-template <bool COH = false, bool PACKED = false, typename I = int64_t>
+// AT = uint16_t: the lists hold 16-bit ids relative to the chunk's first
+// primitive (dual_p / dual_n then start there), stored from adj + abase on
+// with the CSR offsets counted from abase.
+template <bool COH = false, bool PACKED = false, typename I = int64_t, typename AT = uint32_t>
 __device__ __forceinline__ void primal_vertex(I v, I np_lim, int64_t adj_cap,
                                               const uint32_t* __restrict__ off, const uint32_t* __restrict__ cursor,
                                               const uint8_t* __restrict__ valence, const uint32_t* __restrict__ adj,
                                               const uint8_t* __restrict__ boundary, const float* __restrict__ dual_p,
                                               const float* __restrict__ dual_n, float* __restrict__ pos,
                                               float* __restrict__ nrm, int process_boundary, int smooth_normals,
-                                              int set_colors) {
+                                              int set_colors, int64_t abase = 0) {
   // list length: adj_next (MeshProcessor.cpp:247); with a prebuilt adjacency it equals init_valence
   const uint32_t ov = sweep_ld<COH>(off + v);
   const int64_t room = adj_cap - (int64_t)ov;
   const uint32_t n = (uint32_t)max((int64_t)0, min((int64_t)(cursor ? min(cursor[v], (uint32_t)valence[v])
                                                                     : (uint32_t)valence[v]), room));
   if (n == 0 || (!process_boundary && boundary[v])) return;
-  const uint32_t* a = adj + ov;
+  const AT* a = reinterpret_cast<const AT*>(adj + abase) + ((int64_t)ov - abase);
   float p[3] = {0.0f, 0.0f, 0.0f}, nn[3] = {0.0f, 0.0f, 0.0f};
   uint32_t k0 = 0;
   if (PACKED) {
