@@ -236,9 +236,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def tier_split(n):
+    """'2048x33^3 + 1434x65^3 + 614x129^3' for the n-chunk update's tiers (the
+    split workloads.lod_update draws)."""
+    tiers = ((32, 0.50), (64, 0.35), (128, 0.15))
+    counts = [int(round(n * f)) for _, f in tiers]
+    counts[0] += n - sum(counts)
+    return " + ".join("%dx%d^3" % (c, r + 1) for (r, _), c in zip(tiers, counts))
+
+
 def config(args):
     return {"workload": "lod_update_%d" % args.chunks,
-            "chunks": args.chunks, "chunk_samples": "2048x33^3 + 1434x65^3 + 614x129^3",
+            "chunks": args.chunks, "chunk_samples": tier_split(args.chunks),
             "field": ("terrain y-64-40*FBM(p), 5 octaves perlin, freq 0.01, lacunarity 2, gain 0.5, seed 1337"
                       if args.field == "fbm" else
                       "perturbed 2D heightmap -(0.25 y) - 75 n(x, z) (the reference's default world sampler shape): "

@@ -60,3 +60,19 @@ def test_fill_fp32_op_count():
     want = (dim ** 3 * (bench.OPS_PER_SAMPLE_OCTAVE + bench.OPS_PER_SAMPLE)
             + dim ** 2 * (bench.OPS_PER_LINE_OCTAVE + bench.OPS_PER_LINE) + dim ** 2 * 2 * bench.OPS_PER_LAYER)
     assert bench.fill_fp32_ops(one, params) == want
+
+
+def test_bench_tier_split_matches_generator():
+    """The bench's config names the update's tiers as the generator draws them,
+    for the default 4096 chunks and for other batch sizes."""
+    import collections
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), ".."))
+    import bench
+    assert bench.tier_split(4096) == "2048x33^3 + 1434x65^3 + 614x129^3"
+    for n in (4096, 2048, 777, 256):
+        _, rows = workloads.lod_update(n=n)
+        got = collections.Counter(rows[:, 4].astype(int))
+        want = " + ".join("%dx%d^3" % (got[d], d) for d in (33, 65, 129))
+        assert bench.tier_split(n) == want, (n, bench.tier_split(n), want)
