@@ -256,8 +256,9 @@ def config(args):
             "topology": "mode R (reference Marching-Cubes triangles)" if args.mode == "R" else
             "mode Q (DMC quads, placement %d)" % args.placement,
             "smoothing_iters": args.iters, "smoothed_normals": not args.no_normals,
-            "l2": "working set larger than L2: each step moves about 30 GB through DRAM (ncu), no flush "
-                  "between steps", "parallelism": "replicas" if
+            "l2": "working set larger than L2: a step moves about %.0f GB through DRAM (ncu on the 4096-chunk "
+                  "update: 29 GB, scaled by chunks), no flush between steps" % (29.0 * args.chunks / 4096),
+            "parallelism": "replicas" if
             args.gpus == 1 else "weak: one independent update per GPU"}
 
 
